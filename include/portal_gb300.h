@@ -1,0 +1,149 @@
+/*
+ * portal_gb300.h -- C ABI of the GB300 (sm_103a) implementation of PORTAL's
+ * polarized line-transfer hot path.
+ *
+ * The reference (PORTAL, Fortran90 + OpenMP) has no library interface: its
+ * hot path is the body of two OpenMP loops.  Each entry point below replaces
+ * one of those loops *and* its body with one batched call, taking the
+ * reference's own arrays in their Fortran layouts (column-major, 1-based
+ * node / level ids, 0 = "no node"), so that a Fortran caller passes its
+ * arrays unchanged through ISO_C_BINDING.
+ *
+ * Conventions
+ *   - Return value: PORTAL_OK (0) or a negative PORTAL_ERR_* code;
+ *     portal_strerror() describes it.  Per-node outcome goes to the optional
+ *     `status` array (PORTAL_NODE_* values), the analogue of the reference's
+ *     `stop` statements, which abort the whole run instead.
+ *   - Input host pointers are borrowed for the duration of the call; the
+ *     context owns every device copy.
+ *   - A context is not re-entrant: call it from one host thread.  Calls are
+ *     synchronous.  The device is the one passed to portal_create.
+ *   - Where an output pointer is NULL the result stays resident on the
+ *     device, inside the context, for the next call to consume (e.g.
+ *     portal_radiation_field with J0 = J2 = NULL followed by
+ *     portal_solve_se with J0 = J2 = NULL runs the whole node loop of
+ *     main_portal.x without a host round trip).
+ */
+#ifndef PORTAL_GB300_H
+#define PORTAL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct portal_ctx portal_ctx;
+
+enum {
+    PORTAL_OK = 0,
+    PORTAL_ERR_CUDA = -1,      /* a CUDA call failed (message: portal_last_error) */
+    PORTAL_ERR_ARG = -2,       /* invalid argument                                 */
+    PORTAL_ERR_STATE = -3,     /* cloud / molecule / preceding result missing      */
+    PORTAL_ERR_DEPTH = -4,     /* a walk needed more than n_depth cells            */
+    PORTAL_ERR_SINGULAR = -5,  /* an SE matrix was singular                        */
+    PORTAL_ERR_NOMEM = -6,     /* device allocation failed                         */
+    PORTAL_ERR_NODEVICE = -7   /* no CUDA device / the build has no sm_103a code   */
+};
+
+/* per-node status bits */
+enum {
+    PORTAL_NODE_OK = 0,
+    PORTAL_NODE_DEPTH = 1,     /* inverse_rt.f90:206-210 would have stopped        */
+    PORTAL_NODE_SINGULAR = 2,  /* em_coefs.f90:170-178 would have stopped          */
+    PORTAL_NODE_REFINE = 4     /* FP32 LU + FP64 refinement did not converge; the
+                                  node was solved by the FP64 LU instead           */
+};
+
+const char *portal_strerror(int code);
+/* Last CUDA / argument error message of this context (or of the last failed
+ * portal_create when ctx is NULL). */
+const char *portal_last_error(const portal_ctx *ctx);
+
+/* Create a context on CUDA device `device`.  Replaces nothing in the
+ * reference (the Fortran program owns all state in its main program,
+ * main_para.f90:1-200); it allocates the stream the context runs on. */
+int portal_create(portal_ctx **ctx, int device);
+int portal_destroy(portal_ctx *ctx);
+
+/* The molecule after main_para.f90:119-120 and :178-185 (frequencies and
+ * level energies in Hz, t_Bij computed), exactly the arrays
+ * eat_lime_no_delaunay returns (eat_lime.f90:151-196):
+ *   j_lev(nlev), e_levs(nlev) [Hz], r_trans(2,r_num) (lower, upper),
+ *   t_Aji(r_num), nu(r_num) [Hz], t_Bij(r_num), kd_v(r_num),
+ *   c_trans(2,c_num) (lower, upper), col_temps(c_temp),
+ *   t_Cji(c_temp,c_num,c_par) [cm^3/s]. */
+int portal_set_molecule(portal_ctx *ctx, int nlev, const int *j_lev, const double *e_levs,
+                        int r_num, const int *r_trans, const double *t_Aji, const double *nu,
+                        const double *t_Bij, const double *kd_v, int c_num, const int *c_trans,
+                        int c_temp, int c_par, const double *col_temps, const double *t_Cji);
+
+/* The LIME cloud after eat_lime_no_delaunay (eat_lime.f90:71-313) and the
+ * del_ne compaction of main_para.f90:124-130:
+ *   XYZ(3,N) normalised by tx = r_max, vel_all(3,N) [m/s], b_all(N) [m/s],
+ *   temp_all(2,N) (kinetic, dust), dust_p(N), h2_dens(N) [m^-3], ab_all(N),
+ *   lev_p(nlev,N) [m^-3], bvec_all(3,N) (global_magfield / dipole_magfield
+ *   output, main_para.f90:149-155), del_ne(N,maxne) 1-based neighbour ids
+ *   sorted ascending per node (unique.f90:43), del_num_ne(N).
+ * The call builds the device layout (SoA, neighbour CSR with per-face
+ * geometry).  The populations lev_p are the ones the radiation field uses;
+ * portal_set_populations replaces them. */
+int portal_set_cloud(portal_ctx *ctx, int node_num, int bulk_node_num, int nlev,
+                     const double *xyz, const double *vel_all, const double *b_all,
+                     const double *temp_all, const double *dust_p, const double *h2_dens,
+                     const double *ab_all, const double *lev_p, const double *bvec_all,
+                     int maxne, const int *del_ne, const int *del_num_ne, double tx);
+
+/* Replace the level populations lev_p(nlev,N) [m^-3] of the cloud. */
+int portal_set_populations(portal_ctx *ctx, const double *lev_p);
+
+/* Radiation field of every bulk node: the inverse_rt half of the node loop
+ * main_para.f90:210-257 (trace_node main_sub.f90:82-84 -> inverse_rt
+ * inverse_rt.f90:1-137, trace_out :139-214, ray_in :217-344) with the
+ * direction set of legendre_all(nth,nph) (miscellaneous.f90:1100-1137), the
+ * gauge vector gvec (main_para.f90:172-176) and the trace step dx
+ * (main_para.f90:135; PORTAL passes the REAL*4 1E-6).
+ * Outputs (any may be NULL):
+ *   J0(r_num,N), J2(r_num,N)  profile-averaged J^0_0, J^2_0 per line,
+ *                             0 for nodes the reference skips (ab_all <= 0,
+ *                             non-bulk nodes);
+ *   status(N)                 PORTAL_NODE_* bits;
+ *   n_segments                ray segments walked (sum of node_count).
+ * Star mode (star_mod = 1) is not supported. */
+int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const double *gvec,
+                           double dx, int n_depth, double *J0, double *J2, int *status,
+                           long long *n_segments);
+
+/* Polarized statistical equilibrium of every bulk node: make_AC
+ * (miscellaneous.f90:288-392) + get_rhovec (em_coefs.f90:115-201, with
+ * setup_stateq pop_eqs.f90:361-653) + the packing of trace_node
+ * (main_sub.f90:112-137), D0 = 0.  J0/J2 (r_num,N) from the host, or NULL to
+ * use the device-resident result of the last portal_radiation_field.
+ * Outputs: pol_pops(N, 2*nlev) column-major (rho^0_0, rho^2_0 per level, as
+ * main_para.f90:271-275 writes them), rates(N,3,2*nlev) (spontaneous,
+ * radiative, collisional; main_para.f90:277-294) or NULL, JJ_20(N,r_num)
+ * (= J2/J0, main_sub.f90:139) or NULL, status(N) or NULL. */
+int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J2,
+                    double *pol_pops, double *rates, double *JJ_20, int *status);
+
+/* Kernel timing of the last call (CUDA events on the context's stream):
+ * times_ms[0] line-table kernel, [1] radiation-field kernel, [2] SE kernel,
+ * [3] emission-coefficient kernel, [4] image walk kernel, [5] image
+ * integration kernel; launches[i] the number of launches each. */
+int portal_last_kernel_times(const portal_ctx *ctx, double *times_ms, int *launches, int n);
+
+/* ---- utilities -------------------------------------------------------- */
+
+/* Wigner 3j and 6j symbols, arguments doubled (2j, 2m) like wigxjpf's
+ * fwig3jj / fwig6jj, which the reference calls at pop_eqs.f90:48-61,
+ * :127-140, :194, :252-265, :331-344 and em_coefs.f90:42-46.  Exact
+ * big-integer Racah sums, rounded once. */
+double portal_wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3);
+double portal_wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
+/* SE coupling constants of L&L04 Eqs. 7.20 as pop_eqs.f90 defines them:
+ * which = 0 t_abs_const (:1-78), 1 t_stim_const (:80-156), 2 t_spont_const
+ * (:158-201; c2 = 0), 3 r_abs_const (:204-281), 4 r_stim_const (:283-359). */
+void portal_coupling_constant(int which, int j, int k, int j2, int k2, double *c0, double *c2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,198 @@
+"""PORTAL's polarized line-transfer hot path on GB300 (sm_103a).
+
+The product is the C-ABI shared library ``_build/libportal_gb300.so`` built
+from ``csrc/`` (declared in ``include/portal_gb300.h``).  This module is the
+host-side mirror of the reference's node loop for Python callers: it loads the
+library with ctypes and exposes one method per entry point, taking the
+reference's arrays (``synth.Cloud`` / ``synth.Molecule`` or plain numpy arrays
+in the reference layouts).
+
+There is no CPU fallback: if the library is missing or no sm_103a device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libportal_gb300.so")
+
+P_D = C.POINTER(C.c_double)
+P_I = C.POINTER(C.c_int)
+
+PORTAL_OK = 0
+NODE_DEPTH, NODE_SINGULAR, NODE_REFINE = 1, 2, 4
+KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_walk", "image_rt")
+
+EXPORTS = (
+    "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
+    "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
+    "portal_radiation_field", "portal_solve_se", "portal_last_kernel_times",
+    "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
+)
+
+_lib = None
+
+
+class PortalError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"PORTAL error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load the library (it must have been built; see build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run portal_gb300.build.build() first")
+    L = C.CDLL(LIB_PATH)
+    L.portal_strerror.restype = C.c_char_p
+    L.portal_strerror.argtypes = [C.c_int]
+    L.portal_last_error.restype = C.c_char_p
+    L.portal_last_error.argtypes = [C.c_void_p]
+    L.portal_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    L.portal_destroy.argtypes = [C.c_void_p]
+    L.portal_set_molecule.argtypes = [C.c_void_p, C.c_int, P_I, P_D, C.c_int, P_I, P_D, P_D, P_D, P_D,
+                                      C.c_int, P_I, C.c_int, C.c_int, P_D, P_D]
+    L.portal_set_cloud.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, P_D, P_D, P_D, P_D, P_D,
+                                   P_D, P_D, P_D, C.c_int, P_I, P_I, C.c_double]
+    L.portal_set_populations.argtypes = [C.c_void_p, P_D]
+    L.portal_radiation_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int,
+                                         P_D, P_D, P_I, C.POINTER(C.c_longlong)]
+    L.portal_solve_se.argtypes = [C.c_void_p, C.c_int, P_D, P_D, P_D, P_D, P_D, P_I]
+    L.portal_last_kernel_times.argtypes = [C.c_void_p, P_D, P_I, C.c_int]
+    L.portal_wigner3j.restype = C.c_double
+    L.portal_wigner3j.argtypes = [C.c_int] * 6
+    L.portal_wigner6j.restype = C.c_double
+    L.portal_wigner6j.argtypes = [C.c_int] * 6
+    L.portal_coupling_constant.restype = None
+    L.portal_coupling_constant.argtypes = [C.c_int] * 5 + [P_D, P_D]
+    _lib = L
+    return L
+
+
+def _p(a, t=P_D):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One device context (portal_create / portal_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().portal_create(C.byref(self._h), device)
+        if rc != PORTAL_OK:
+            raise PortalError(rc, lib().portal_last_error(None).decode())
+        self.nlev = self.r_num = self.N = 0
+
+    def close(self):
+        if self._h:
+            lib().portal_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != PORTAL_OK:
+            msg = lib().portal_last_error(self._h).decode() or lib().portal_strerror(rc).decode()
+            raise PortalError(rc, msg)
+
+    # ---- set-up -----------------------------------------------------------
+    def set_molecule(self, mol):
+        self._mol = dict(j=_i32(mol.j_lev), e=_f64(mol.e_levs), rt=_i32(mol.r_trans), A=_f64(mol.A),
+                         nu=_f64(mol.nu), B=_f64(mol.Bij), kd=_f64(mol.kd_v), ct=_i32(mol.c_trans),
+                         tc=_f64(mol.col_temps), C=_f64(mol.C))
+        m = self._mol
+        self._check(lib().portal_set_molecule(
+            self._h, mol.nlev, _p(m["j"], P_I), _p(m["e"]), mol.r_num, _p(m["rt"], P_I), _p(m["A"]),
+            _p(m["nu"]), _p(m["B"]), _p(m["kd"]), mol.c_num, _p(m["ct"], P_I), mol.c_temp, mol.c_par,
+            _p(m["tc"]), _p(m["C"])))
+        self.nlev, self.r_num = mol.nlev, mol.r_num
+
+    def set_cloud(self, cloud, del_ne=None, del_num_ne=None):
+        """cloud: synth.Cloud.  del_ne / del_num_ne default to the cloud's
+        reference-layout neighbour arrays."""
+        N = cloud.node_num
+        temp = np.empty((N, 2))
+        temp[:, 0] = cloud.t_kin
+        temp[:, 1] = cloud.t_dust
+        dn = _i32(cloud.del_ne() if del_ne is None else del_ne)
+        dnn = _i32(cloud.del_num_ne() if del_num_ne is None else del_num_ne)
+        arrs = [_f64(cloud.xyz), _f64(cloud.vel), _f64(cloud.b_all), _f64(temp), _f64(cloud.dust_p),
+                _f64(cloud.h2_dens), _f64(cloud.ab_all), _f64(cloud.lev_p), _f64(cloud.bvec)]
+        self._check(lib().portal_set_cloud(self._h, N, cloud.bulk_node_num, cloud.nlev,
+                                           *[_p(a) for a in arrs], dn.shape[0], _p(dn, P_I), _p(dnn, P_I),
+                                           float(cloud.tx)))
+        self.N = N
+
+    def set_populations(self, lev_p):
+        self._check(lib().portal_set_populations(self._h, _p(_f64(lev_p))))
+
+    # ---- the node loop ------------------------------------------------------
+    def radiation_field(self, rc, fetch: bool = True):
+        """J0, J2 as (N, r_num) arrays (the reference's (r_num, N) memory),
+        status (N,), number of ray segments."""
+        g = _f64(rc.gvec)
+        nseg = C.c_longlong(0)
+        J0 = np.zeros((self.N, self.r_num)) if fetch else None
+        J2 = np.zeros((self.N, self.r_num)) if fetch else None
+        st = np.zeros(self.N, dtype=np.int32) if fetch else None
+        self._check(lib().portal_radiation_field(self._h, rc.nth, rc.nph, rc.nvel, _p(g), float(rc.dx),
+                                                 rc.n_depth, _p(J0), _p(J2), _p(st, P_I), C.byref(nseg)))
+        return J0, J2, st, int(nseg.value)
+
+    def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False):
+        """pol_pops as (N, 2*nlev) (reference pol_pops(node,:)), status."""
+        pp = np.zeros((2 * self.nlev, self.N)) if fetch else None      # Fortran (N, 2 nlev)
+        jj = np.zeros((self.r_num, self.N)) if jj20 else None
+        st = np.zeros(self.N, dtype=np.int32) if fetch else None
+        j0 = None if J0 is None else _f64(J0)
+        j2 = None if J2 is None else _f64(J2)
+        self._check(lib().portal_solve_se(self._h, kmax, _p(j0), _p(j2), _p(pp), None, _p(jj), _p(st, P_I)))
+        out = (None if pp is None else pp.T.copy(), st)
+        if jj20:
+            out = out + (jj.T.copy(),)
+        return out
+
+    def kernel_times(self):
+        t = np.zeros(len(KERNEL_SLOTS))
+        n = np.zeros(len(KERNEL_SLOTS), dtype=np.int32)
+        self._check(lib().portal_last_kernel_times(self._h, _p(t), _p(n, P_I), len(KERNEL_SLOTS)))
+        return {k: (float(t[i]), int(n[i])) for i, k in enumerate(KERNEL_SLOTS)}
+
+
+def wigner3j(tj1, tj2, tj3, tm1, tm2, tm3) -> float:
+    return lib().portal_wigner3j(tj1, tj2, tj3, tm1, tm2, tm3)
+
+
+def wigner6j(tj1, tj2, tj3, tj4, tj5, tj6) -> float:
+    return lib().portal_wigner6j(tj1, tj2, tj3, tj4, tj5, tj6)
+
+
+def coupling_constant(which, j, k, j2, k2):
+    c0, c2 = C.c_double(), C.c_double()
+    lib().portal_coupling_constant(which, j, k, j2, k2, C.byref(c0), C.byref(c2))
+    return c0.value, c2.value

@@ -1,0 +1,144 @@
+// Shared definitions of the PORTAL GB300 library: the context, device
+// buffers, error plumbing and the small numerics both kernels families use.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "portal_gb300.h"
+
+namespace portal {
+
+// --------------------------------------------------------------------------
+// device buffer (RAII, grows on demand, never shrinks)
+// --------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // returns cudaSuccess or the allocation error
+    cudaError_t reserve(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return e; }
+        n = count;
+        return cudaSuccess;
+    }
+};
+
+enum TimerSlot { T_LINETAB = 0, T_RF = 1, T_SE = 2, T_EMCOEF = 3, T_IMWALK = 4, T_IMRT = 5, T_NSLOT = 6 };
+
+}  // namespace portal
+
+struct portal_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // ---- molecule (host copies, FP64) ----
+    bool have_mol = false;
+    int nlev = 0, r_num = 0, c_num = 0, c_temp = 0, c_par = 0;
+    std::vector<int> j_lev, r_trans, c_trans;
+    std::vector<double> e_levs, A, nu, Bij, kd_v, col_temps, Cji;
+
+    // ---- cloud ----
+    bool have_cloud = false;
+    int N = 0, bulk = 0, nnz = 0, maxdeg = 0;
+    double tx = 0.0;
+    portal::DevBuf<double> pos64;     // (3,N) FP64 positions
+    portal::DevBuf<double> bvec64;    // (3,N)
+    portal::DevBuf<float4> cellv;     // (vx,vy,vz,b) per node
+    portal::DevBuf<int> nb_off;       // N+1
+    portal::DevBuf<int> nb_idx;       // nnz, 0-based
+    portal::DevBuf<float4> edge;      // nnz: (ex,ey,ez,|e|^2/2) from FP64
+    portal::DevBuf<double> levp;      // (nlev,N)
+    portal::DevBuf<double> nmol;      // per node total molecule density (sum lev_p)
+    portal::DevBuf<double> b64, tkin, tdust, dustp, h2, ab;
+    bool has_dust = false;
+
+    // ---- derived / results ----
+    portal::DevBuf<float4> ltab;      // (r_num,N) line table
+    portal::DevBuf<double> J0, J2;    // (r_num,N)
+    portal::DevBuf<int> status;       // N
+    portal::DevBuf<int2> walk;        // per-warp walk scratch
+    portal::DevBuf<unsigned long long> counters;  // [0] work, [1] segments, [2..] misc
+    portal::DevBuf<double> dirtab;    // direction table
+    portal::DevBuf<float> chtab;      // channel tables
+    bool j_valid = false;
+
+    // SE program (device) -- built per (molecule, kmax)
+    int se_kmax = -1, c_dim = 0, n_trans = 0;
+    portal::DevBuf<int> se_ints;
+    portal::DevBuf<double> se_dbls;
+    std::vector<int> count_array;
+    portal::DevBuf<double> pops;      // (N, 2*nlev) column-major result
+    portal::DevBuf<double> rates;     // (N,3,2*nlev)
+    portal::DevBuf<double> jj20;      // (N, r_num)
+    int se_ni = 0;
+    size_t se_offs[16] = {};
+
+    // ---- timing ----
+    cudaEvent_t ev[2 * portal::T_NSLOT] = {};
+    double t_ms[portal::T_NSLOT] = {};
+    int t_launch[portal::T_NSLOT] = {};
+    bool ev_ready = false;
+};
+
+namespace portal {
+
+inline int set_err(portal_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+inline int cuda_fail(portal_ctx *c, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (c) c->err = m;
+    return (e == cudaErrorMemoryAllocation) ? PORTAL_ERR_NOMEM : PORTAL_ERR_CUDA;
+}
+
+#define PCHECK(ctx, call)                                                  \
+    do {                                                                   \
+        cudaError_t _e = (call);                                           \
+        if (_e != cudaSuccess) return portal::cuda_fail((ctx), _e, #call); \
+    } while (0)
+
+// timers: record start/stop around one kernel launch on the ctx stream
+inline void timer_start(portal_ctx *c, int slot) { cudaEventRecord(c->ev[2 * slot], c->stream); }
+inline void timer_stop(portal_ctx *c, int slot) { cudaEventRecord(c->ev[2 * slot + 1], c->stream); }
+// after a stream synchronize: fold the slot's event pair into the totals
+inline void timer_collect(portal_ctx *c, int slot) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[2 * slot], c->ev[2 * slot + 1]) == cudaSuccess) {
+        c->t_ms[slot] += ms;
+        c->t_launch[slot] += 1;
+    }
+}
+inline void timers_reset(portal_ctx *c) {
+    for (int i = 0; i < T_NSLOT; i++) { c->t_ms[i] = 0.0; c->t_launch[i] = 0; }
+}
+
+// host: Gauss-Legendre rule on (-1,1), ascending knots (Newton iteration on
+// the three-term recurrence, long double)
+void gauss_legendre(int n, double *x, double *w);
+// host: the direction set of legendre_all (miscellaneous.f90:1100-1137);
+// returns rows (mu, phi, w) packed as 3 doubles per direction
+int legendre_all(int nth, int nph, std::vector<double> &xth);
+
+}  // namespace portal

@@ -1,0 +1,529 @@
+// Radiation field of every node: the inverse_rt loop of main_portal.x.
+//
+// Reference: main_para.f90:210-257 -> trace_node main_sub.f90:82-84 ->
+// inverse_rt inverse_rt.f90:1-137, trace_out :139-214 (with
+// check_neigh_fast miscellaneous.f90:1017-1076, pos_quadratic :1078-1098),
+// ray_in :217-344, find_dir miscellaneous.f90:48-82.
+//
+// Two kernels:
+//   k_line_table   per (node, line): the opacity / emissivity factors that
+//                  ray_in rebuilds for every (direction, channel, cell):
+//                  A = kv * c/nu / (sqrt(pi) b) * tx*dx   (optical depth per
+//                  trace step per unit Gaussian profile value), E the same
+//                  for the emissivity, and the dust terms.  HBM-bound, tiny.
+//   k_radiation_field  one warp per node (persistent warps, node queue):
+//                  for each direction of legendre_all
+//                   (1) FP64 set-up: the direction (find_dir's rotation in
+//                       closed form) and the sphere-exit distance
+//                       (pos_quadratic from the node, as trace_out's first
+//                       step computes it);
+//                   (2) the Voronoi walk, lanes over the neighbours of the
+//                       current cell.  The photon is kept relative to the
+//                       current node, so the face crossing
+//                       t = (|e|^2/2 - e.r) / (e.d) is formed from the
+//                       FP64-derived edge vectors without cancellation
+//                       against absolute coordinates.  Warp min-reduction
+//                       with the reference's tie rule (the last neighbour
+//                       in list order wins);
+//                   (3) the channel integration inward over the walk, lanes
+//                       over channels, lines looped in registers, cell
+//                       records staged in shared memory 32 cells at a time;
+//                   (4) the profile-weighted channel sum (warp reduction)
+//                       and the FP64 accumulation of J^0_0 and J^2_0.
+#include <cmath>
+
+#include "common.cuh"
+
+using namespace portal;
+
+namespace {
+
+constexpr float LOG2E_F = 1.4426950408889634f;
+// Face crossings closer than this (in units of r_max) are not taken.  The
+// reference uses 1e-10 (miscellaneous.f90:1048) against FP64 noise ~1e-16;
+// the FP32 walk's noise in t is ~1e-9, and a crossing shorter than 2e-8 is
+// 0.02 trace steps, i.e. it contributes nint(...) = 0 steps either way.
+constexpr float FACE_EPS = 2e-8f;
+
+struct LineConst {
+    double nu, A, B, kd, glo, gup, bb_cmb;
+    int lo, up;
+};
+constexpr int MAX_LINES = 64;
+__constant__ LineConst c_lines[MAX_LINES];
+
+struct RFArgs {
+    int N, bulk, L, nvel, nch, ndir, n_depth;
+    float dx32;
+    const double *__restrict__ pos;
+    const double *__restrict__ bvec;
+    const double *__restrict__ ab;
+    const float4 *__restrict__ cellv;
+    const int *__restrict__ off;
+    const int *__restrict__ idx;
+    const float4 *__restrict__ edge;
+    const float4 *__restrict__ ltab;
+    const double *__restrict__ dirs;  // (ndir, 6): mu, sin th, cos ph, sin ph, w, w*c_in/sqrt2
+    const float *__restrict__ chq;    // (nch) 2 nv / nvel
+    const float *__restrict__ chw;    // (nch) exp(-q0^2) * 2/(sqrt(pi) nvel)
+    double gx, gy, gz;
+    double *J0, *J2;
+    int *status;
+    int2 *walk;
+    unsigned long long *counters;
+};
+
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Line table: one thread per (node, line).
+__global__ void k_line_table(int N, int L, double dxp, const double *__restrict__ levp, int nlev,
+                             const double *__restrict__ b, const double *__restrict__ dustp,
+                             const double *__restrict__ tdust, float4 *__restrict__ ltab) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * L) return;
+    int n = (int)(t / L), l = (int)(t - (long long)n * L);
+    const LineConst lc = c_lines[l];
+    double p1 = levp[(size_t)nlev * n + lc.lo];
+    double p2 = levp[(size_t)nlev * n + lc.up];
+    // ray_in inverse_rt.f90:263-266, 293-294, 298-301
+    double c1 = 2.2102191e-42 * lc.nu;
+    double c2 = 5.272859e-35 * lc.nu;
+    double cnu = 299792458.0 / lc.nu;
+    double kv = c1 * lc.B * (p1 - lc.glo * p2 / lc.gup);
+    double ev = c2 * lc.A * p2;
+    double phif = cnu / (1.7724538509055160273 * b[n]) * dxp;
+    double Ad = lc.kd * dustp[n] * dxp;
+    double Td = tdust[n];
+    double Ibb = 0.0;
+    if (Td != 0.0) {  // black_body miscellaneous.f90:263-285
+        double c2b = 4.79924e-11 / Td;
+        Ibb = 1.4744995e-50 * lc.nu * lc.nu * lc.nu / (exp(c2b * lc.nu) - 1.0);
+    }
+    ltab[t] = make_float4((float)(kv * phif), (float)(ev * phif), (float)Ad, (float)(Ad * Ibb));
+}
+
+template <int NLG, bool DUST>
+struct CellRec {
+    float q0[32], dq[32];
+    float As[32][NLG];   // A * steps
+    float Ss[32][NLG];   // S (no dust) or E * steps (dust)
+    float Ad[32][DUST ? NLG : 1];   // dust tau per cell (dust only)
+    float Jd[32][DUST ? NLG : 1];   // dust emissivity * steps (dust only)
+};
+
+// NS channel slots per lane (nch <= 32 NS), NLG lines per register group.
+template <int NS, int NLG, bool DUST>
+__global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    int2 *wl = a.walk + (size_t)gw * (size_t)a.n_depth;
+    __shared__ CellRec<NLG, DUST> recs[8];
+    CellRec<NLG, DUST> &R = recs[wib];
+
+    float q0c[NS], wch[NS];
+    int nvs[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        int ch = lane + 32 * s;
+        nvs[s] = ch - a.nvel;
+        q0c[s] = (ch < a.nch) ? a.chq[ch] : 0.f;
+        wch[s] = (ch < a.nch) ? a.chw[ch] : 0.f;
+    }
+    unsigned long long nseg = 0;
+
+    for (;;) {
+        int node = 0;
+        if (lane == 0) node = (int)atomicAdd(&a.counters[0], 1ULL);
+        node = __shfl_sync(FULL, node, 0);
+        if (node >= a.bulk) break;
+        double acc0a = 0.0, acc0b = 0.0, acc2a = 0.0, acc2b = 0.0;  // lines lane, lane+32
+        int st = 0;
+        if (a.ab[node] > 0.0) {
+            // node frame (find_dir miscellaneous.f90:48-82): x = b x g / |b x g|,
+            // dir = R(b,ph) R(x,th) b = cos th b + sin th (cos ph (x x b) + sin ph x)
+            const double bx = a.bvec[3 * (size_t)node], by = a.bvec[3 * (size_t)node + 1],
+                         bz = a.bvec[3 * (size_t)node + 2];
+            double xx = by * a.gz - bz * a.gy, xy = bz * a.gx - bx * a.gz, xz = bx * a.gy - by * a.gx;
+            double xn = sqrt(xx * xx + xy * xy + xz * xz);
+            xx /= xn; xy /= xn; xz /= xn;
+            const double wx = xy * bz - xz * by, wy = xz * bx - xx * bz, wz = xx * by - xy * bx;
+            const double px = a.pos[3 * (size_t)node], py = a.pos[3 * (size_t)node + 1],
+                         pz = a.pos[3 * (size_t)node + 2];
+            const double pp = px * px + py * py + pz * pz;
+            const float4 cvn = a.cellv[node];
+            const float dqfac = 2.f * cvn.w / (float)a.nvel;
+
+            for (int k = 0; k < a.ndir; k++) {
+                const double *dr = a.dirs + 6 * (size_t)k;
+                const double mu = dr[0], sth = dr[1], cph = dr[2], sph = dr[3];
+                const double dx = mu * bx + sth * (cph * wx + sph * xx);
+                const double dy = mu * by + sth * (cph * wy + sph * xy);
+                const double dz = mu * bz + sth * (cph * wz + sph * xz);
+                // pos_quadratic(|d|^2, 2 p.d, |p|^2 - 1) from the node
+                double aq = dx * dx + dy * dy + dz * dz;
+                double bq = 2.0 * (px * dx + py * dy + pz * dz);
+                double dis = bq * bq - 4.0 * aq * (pp - 1.0);
+                double sexit = 0.0;
+                if (dis > 0.0) {
+                    double sq = sqrt(dis);
+                    double x1 = (-bq + sq) / (2.0 * aq), x2 = (-bq - sq) / (2.0 * aq);
+                    sexit = (x2 > 0.0) ? x2 : x1;
+                }
+                const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+
+                // ---- (2) walk ----
+                double s = 0.0;
+                float rx = 0.f, ry = 0.f, rz = 0.f;
+                int c = node, K = 0;
+                bool over = false;
+                for (;;) {
+                    const float tsph = (float)(sexit - s);
+                    const int o = a.off[c], deg = a.off[c + 1] - o;
+                    unsigned best = 0xffffffffu;
+                    int bestj = -1;
+                    float4 eb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int base = 0; base < deg; base += 32) {
+                        const int j = base + lane;
+                        unsigned tb = 0xffffffffu;
+                        float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (j < deg) {
+                            e = a.edge[o + j];
+                            const float den = e.x * fdx + e.y * fdy + e.z * fdz;
+                            const float num = e.w - (e.x * rx + e.y * ry + e.z * rz);
+                            if (den > 0.f) {
+                                const float t = num / den;
+                                if (t > FACE_EPS && t <= tsph) tb = __float_as_uint(t);
+                            }
+                        }
+                        const unsigned m = __reduce_min_sync(FULL, tb);
+                        if (m != 0xffffffffu && m <= best) {
+                            const unsigned bal = __ballot_sync(FULL, tb == m);
+                            const int jl = 31 - __clz(bal);
+                            best = m;
+                            bestj = base + jl;
+                            eb.x = __shfl_sync(FULL, e.x, jl);
+                            eb.y = __shfl_sync(FULL, e.y, jl);
+                            eb.z = __shfl_sync(FULL, e.z, jl);
+                        }
+                    }
+                    const float delta = (bestj < 0) ? tsph : __uint_as_float(best);
+                    const int steps = (int)roundf(delta / a.dx32);  // nint(delta_x/dx)
+                    if (K >= a.n_depth) { over = true; break; }
+                    if (lane == 0) wl[K] = make_int2(c, steps);
+                    K++;
+                    if (bestj < 0) break;
+                    s += (double)delta;
+                    rx = fmaf(delta, fdx, rx) - eb.x;
+                    ry = fmaf(delta, fdy, ry) - eb.y;
+                    rz = fmaf(delta, fdz, rz) - eb.z;
+                    c = a.idx[o + bestj];
+                }
+                if (over) { st |= PORTAL_NODE_DEPTH; break; }
+                nseg += (unsigned long long)K;
+                __syncwarp();
+
+                // ---- (3) channel integration, inward ----
+                const float vcp = cvn.x * fdx + cvn.y * fdy + cvn.z * fdz;
+                const int2 w0 = wl[0];
+                const double wgt = dr[4], wgt2 = dr[5];
+                for (int l0 = 0; l0 < a.L; l0 += NLG) {
+                    float I[NS][NLG];
+#pragma unroll
+                    for (int l = 0; l < NLG; l++) {
+                        const float bb = (l0 + l < a.L) ? (float)c_lines[l0 + l].bb_cmb : 0.f;
+#pragma unroll
+                        for (int s2 = 0; s2 < NS; s2++) I[s2][l] = bb;
+                    }
+                    for (int hi = K - 1; hi >= 1; hi -= 32) {
+                        const int nc = min(32, hi);
+                        if (lane < nc) {
+                            const int2 wc = wl[hi - lane];
+                            const float4 cv = a.cellv[wc.x];
+                            const float vp = cv.x * fdx + cv.y * fdy + cv.z * fdz;
+                            const float ib = 1.f / cv.w;
+                            R.q0[lane] = (vcp - vp) * ib;
+                            R.dq[lane] = dqfac * ib;
+                            const float fst = (float)wc.y;
+                            const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
+#pragma unroll
+                            for (int l = 0; l < NLG; l++) {
+                                if (l0 + l < a.L) {
+                                    const float4 v = lt[l];
+                                    R.As[lane][l] = v.x * fst;
+                                    if (DUST) {
+                                        R.Ss[lane][l] = v.y * fst;
+                                        R.Ad[lane][DUST ? l : 0] = v.z * fst;
+                                        R.Jd[lane][DUST ? l : 0] = v.w * fst;
+                                    } else {
+                                        R.Ss[lane][l] = v.y / v.x;
+                                    }
+                                }
+                            }
+                        }
+                        __syncwarp();
+                        for (int u = 0; u < nc; u++) {
+                            const float q0 = R.q0[u], dq = R.dq[u];
+                            float g[NS];
+#pragma unroll
+                            for (int s2 = 0; s2 < NS; s2++) {
+                                const float q = fmaf(dq, (float)nvs[s2], q0);
+                                g[s2] = ex2(-q * q * LOG2E_F);
+                            }
+#pragma unroll
+                            for (int l = 0; l < NLG; l++) {
+                                if (l0 + l < a.L) {
+                                    const float Au = R.As[u][l];
+                                    const float Su = R.Ss[u][l];
+                                    float Adu = 0.f, Jdu = 0.f;
+                                    if (DUST) { Adu = R.Ad[u][DUST ? l : 0]; Jdu = R.Jd[u][DUST ? l : 0]; }
+#pragma unroll
+                                    for (int s2 = 0; s2 < NS; s2++) {
+                                        float tau, Sv;
+                                        if (DUST) {
+                                            // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
+                                            tau = fmaf(Au, g[s2], Adu);
+                                            Sv = fmaf(Su, g[s2], Jdu) / tau;
+                                        } else {
+                                            tau = Au * g[s2];
+                                            Sv = Su;
+                                        }
+                                        const float e = ex2(-tau * LOG2E_F);
+                                        const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                        I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                    }
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    // central cell (inverse_rt.f90:320-339): no gate, profile at
+                    // the node's own b, then the weighted channel sum
+                    const float fst0 = (float)w0.y;
+                    float part[NLG];
+#pragma unroll
+                    for (int l = 0; l < NLG; l++) {
+                        part[l] = 0.f;
+                        if (l0 + l < a.L) {
+                            const float4 v = a.ltab[(size_t)node * a.L + l0 + l];
+#pragma unroll
+                            for (int s2 = 0; s2 < NS; s2++) {
+                                const float g0 = ex2(-q0c[s2] * q0c[s2] * LOG2E_F);
+                                float tau, Sv;
+                                if (DUST) {
+                                    const float kap = fmaf(v.x, g0, v.z);
+                                    tau = kap * fst0;
+                                    Sv = fmaf(v.y, g0, v.w) / kap;
+                                } else {
+                                    tau = v.x * g0 * fst0;
+                                    Sv = v.y / v.x;
+                                }
+                                const float e = ex2(-tau * LOG2E_F);
+                                const float Io = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                part[l] = fmaf(wch[s2], Io, part[l]);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int l = 0; l < NLG; l++) {
+                        float v = part[l];
+#pragma unroll
+                        for (int o2 = 16; o2 >= 1; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
+                        const int line = l0 + l;
+                        if (line < a.L && (line & 31) == lane) {
+                            if (line < 32) {
+                                acc0a += wgt * (double)v;
+                                acc2a += wgt2 * (double)v;
+                            } else {
+                                acc0b += wgt * (double)v;
+                                acc2b += wgt2 * (double)v;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (lane < a.L) {
+            a.J0[(size_t)node * a.L + lane] = (st == 0) ? acc0a : 0.0;
+            a.J2[(size_t)node * a.L + lane] = (st == 0) ? acc2a : 0.0;
+        }
+        if (lane + 32 < a.L) {
+            a.J0[(size_t)node * a.L + lane + 32] = (st == 0) ? acc0b : 0.0;
+            a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b : 0.0;
+        }
+        if (lane == 0) a.status[node] = st;
+    }
+    // segment count (every lane holds the same count)
+    if (lane == 0) atomicAdd(&a.counters[1], nseg);
+}
+
+}  // namespace
+
+namespace {
+
+// upload per-line constants of the molecule
+int upload_lines(portal_ctx *c) {
+    if (c->r_num > MAX_LINES)
+        return set_err(c, PORTAL_ERR_ARG, "more than 64 radiative lines are not supported");
+    LineConst h[MAX_LINES];
+    for (int k = 0; k < c->r_num; k++) {
+        int lo = c->r_trans[2 * k] - 1, up = c->r_trans[2 * k + 1] - 1;
+        h[k].nu = c->nu[k];
+        h[k].A = c->A[k];
+        h[k].B = c->Bij[k];
+        h[k].kd = c->kd_v[k];
+        h[k].glo = 2.0 * c->j_lev[lo] + 1.0;
+        h[k].gup = 2.0 * c->j_lev[up] + 1.0;
+        // black_body(2.73, nu) miscellaneous.f90:263-285
+        h[k].bb_cmb = 1.4744995e-50 * std::pow(c->nu[k], 3.0) *
+                      std::pow(std::exp(4.79924e-11 / 2.73 * c->nu[k]) - 1.0, -1.0);
+        h[k].lo = lo;
+        h[k].up = up;
+    }
+    PCHECK(c, cudaMemcpyToSymbolAsync(c_lines, h, sizeof(LineConst) * c->r_num, 0,
+                                      cudaMemcpyHostToDevice, c->stream));
+    return PORTAL_OK;
+}
+
+template <int NS, int NLG, bool DUST>
+int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
+    auto kern = k_radiation_field<NS, NLG, DUST>;
+    int nb = 0;
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, 0));
+    if (nb < 1) nb = 1;
+    int grid = nb * c->sm_count;
+    size_t nslots = (size_t)grid * 8;
+    if (c->walk.reserve(nslots * (size_t)n_depth) != cudaSuccess)
+        return set_err(c, PORTAL_ERR_NOMEM, "walk scratch allocation failed");
+    a.walk = c->walk.p;
+    PCHECK(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+    timer_start(c, T_RF);
+    kern<<<grid, 256, 0, c->stream>>>(a);
+    timer_stop(c, T_RF);
+    PCHECK(c, cudaGetLastError());
+    return PORTAL_OK;
+}
+
+template <int NS>
+int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
+    if (a.L <= 5)
+        return c->has_dust ? launch_rf<NS, 5, true>(c, a, n_depth) : launch_rf<NS, 5, false>(c, a, n_depth);
+    return c->has_dust ? launch_rf<NS, 10, true>(c, a, n_depth) : launch_rf<NS, 10, false>(c, a, n_depth);
+}
+
+}  // namespace
+
+namespace portal {
+
+// Runs the line table + radiation field on the device; J stays in c->J0/J2.
+int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
+                        int n_depth, long long *n_segments, int *n_failed) {
+    if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
+    if (c->nlev != (int)c->j_lev.size())
+        return set_err(c, PORTAL_ERR_STATE, "cloud and molecule disagree on nlev");
+    if (nth < 1 || nph < 1 || nvel < 1 || n_depth < 1 || !gvec || !(dx > 0.0) || 2 * nvel + 1 > 288)
+        return set_err(c, PORTAL_ERR_ARG, "portal_radiation_field: bad nth/nph/nvel/n_depth/dx "
+                                          "(at most 288 channels)");
+    cudaSetDevice(c->device);
+    timers_reset(c);
+    int rc;
+    if ((rc = upload_lines(c))) return rc;
+    const int L = c->r_num, N = c->N;
+    // direction table (legendre_all) and channel tables
+    std::vector<double> xth;
+    const int ndir = legendre_all(nth, nph, xth);
+    std::vector<double> dt(6 * (size_t)ndir);
+    for (int k = 0; k < ndir; k++) {
+        double mu = xth[3 * k], ph = xth[3 * k + 1], w = xth[3 * k + 2];
+        double th = std::acos(mu);
+        double c_in = (3.0 * mu * mu - 1.0) / 2.0;
+        dt[6 * k + 0] = std::cos(th);
+        dt[6 * k + 1] = std::sin(th);
+        dt[6 * k + 2] = std::cos(ph);
+        dt[6 * k + 3] = std::sin(ph);
+        dt[6 * k + 4] = w;
+        dt[6 * k + 5] = w * c_in / std::sqrt(2.0);
+    }
+    const int nch = 2 * nvel + 1;
+    std::vector<float> ct(2 * (size_t)nch);
+    const double spi = std::sqrt(std::acos(-1.0));
+    for (int i = 0; i < nch; i++) {
+        int nv = i - nvel;
+        double q0 = 2.0 * nv / nvel;
+        ct[i] = (float)q0;
+        // phi_v0 * d_v = exp(-q0^2)/(sqrt(pi) b) * 2 b / nvel
+        ct[nch + i] = (float)(std::exp(-q0 * q0) * 2.0 / (spi * nvel));
+    }
+    if (c->dirtab.reserve(dt.size()) || c->chtab.reserve(ct.size()) ||
+        c->ltab.reserve((size_t)L * N) || c->J0.reserve((size_t)L * N) || c->J2.reserve((size_t)L * N))
+        return set_err(c, PORTAL_ERR_NOMEM, "radiation-field buffers");
+    PCHECK(c, cudaMemcpyAsync(c->dirtab.p, dt.data(), dt.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, c->stream));
+    PCHECK(c, cudaMemcpyAsync(c->chtab.p, ct.data(), ct.size() * sizeof(float),
+                              cudaMemcpyHostToDevice, c->stream));
+    PCHECK(c, cudaMemsetAsync(c->J0.p, 0, (size_t)L * N * sizeof(double), c->stream));
+    PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), c->stream));
+    PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), c->stream));
+    // line table
+    {
+        long long tot = (long long)N * L;
+        timer_start(c, T_LINETAB);
+        k_line_table<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
+            N, L, c->tx * dx, c->levp.p, c->nlev, c->b64.p, c->dustp.p, c->tdust.p, c->ltab.p);
+        timer_stop(c, T_LINETAB);
+        PCHECK(c, cudaGetLastError());
+    }
+    RFArgs a;
+    a.N = N; a.bulk = c->bulk; a.L = L; a.nvel = nvel; a.nch = nch; a.ndir = ndir; a.n_depth = n_depth;
+    a.dx32 = (float)dx;
+    a.pos = c->pos64.p; a.bvec = c->bvec64.p; a.ab = c->ab.p; a.cellv = c->cellv.p;
+    a.off = c->nb_off.p; a.idx = c->nb_idx.p; a.edge = c->edge.p; a.ltab = c->ltab.p;
+    a.dirs = c->dirtab.p; a.chq = c->chtab.p; a.chw = c->chtab.p + nch;
+    a.gx = gvec[0]; a.gy = gvec[1]; a.gz = gvec[2];
+    a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
+    a.walk = nullptr;
+    if (nch <= 32) rc = dispatch_nlg<1>(c, a, n_depth);
+    else if (nch <= 64) rc = dispatch_nlg<2>(c, a, n_depth);
+    else if (nch <= 96) rc = dispatch_nlg<3>(c, a, n_depth);
+    else if (nch <= 160) rc = dispatch_nlg<5>(c, a, n_depth);
+    else rc = dispatch_nlg<9>(c, a, n_depth);
+    if (rc) return rc;
+    unsigned long long cnt[8];
+    PCHECK(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    timer_collect(c, T_LINETAB);
+    timer_collect(c, T_RF);
+    if (n_segments) *n_segments = (long long)cnt[1];
+    // failed nodes: count on the host from the status array only when asked
+    if (n_failed) *n_failed = 0;
+    c->j_valid = true;
+    return PORTAL_OK;
+}
+
+}  // namespace portal
+
+extern "C" int portal_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec,
+                                      double dx, int n_depth, double *J0, double *J2, int *status,
+                                      long long *n_segments) {
+    if (!c) return PORTAL_ERR_ARG;
+    int rc = portal::run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, n_segments, nullptr);
+    if (rc) return rc;
+    const size_t LN = (size_t)c->r_num * c->N;
+    if (J0) PCHECK(c, cudaMemcpyAsync(J0, c->J0.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (J2) PCHECK(c, cudaMemcpyAsync(J2, c->J2.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int> st_host;
+    int *st = status;
+    if (!st) { st_host.resize(c->N); st = st_host.data(); }
+    PCHECK(c, cudaMemcpyAsync(st, c->status.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < c->N; i++)
+        if (st[i] & PORTAL_NODE_DEPTH)
+            return set_err(c, PORTAL_ERR_DEPTH, "node_count > n_depth for node " + std::to_string(i + 1));
+    return PORTAL_OK;
+}

@@ -1,0 +1,572 @@
+// Polarized statistical equilibrium of every node: make_AC + get_rhovec +
+// the packing of trace_node.
+//
+// Reference: trace_node main_sub.f90:93-137, make_AC miscellaneous.f90:288-392,
+// all_transitions :394-460, setup_count_array :206-239, get_rhovec
+// em_coefs.f90:115-201, setup_stateq pop_eqs.f90:361-653 and the coupling
+// constants pop_eqs.f90:1-359.
+//
+// Every entry of the SE matrix is a linear combination of five per-node,
+// per-transition quantities
+//     f0 = B21 J0,  f1 = B21 J2,  f2 = A21,  f3 = C21 (n_H2, T),
+//     f4 = C21 exp(-h nu / k T)
+// with node-independent coefficients built from the Wigner coupling
+// constants.  The host turns setup_stateq's loops into that program once per
+// (molecule, kmax): a CSR list over matrix entries of (feature, coefficient)
+// terms.  The kernel (one warp per node) evaluates the features, assembles
+// the matrix in shared memory (FP64), replaces row 1 by the normalisation
+// sum sqrt(2J+1) rho^0_0 = 1, factorises a row-scaled FP32 copy with partial
+// pivoting and refines the solution of A rho = e_1 with FP64 residuals.
+// Should the refinement stall (FP32 LU too inaccurate for the matrix's
+// condition) the node is refactorised in FP64 on the device and flagged.
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+#include "common.cuh"
+
+namespace portal {
+void coupling_constants(int which, int j, int k, int j2, int k2, double *c0, double *c2);
+}
+using namespace portal;
+
+namespace {
+
+constexpr double A_TO_B = 6.781962e49;  // pop_eqs.f90:419
+constexpr double HK = 4.79924e-11;      // pop_eqs.f90:535
+
+struct SEArgs {
+    int N, bulk, c_dim, n_trans, nlev, L, c_temp, c_num, c_par, nent;
+    const double *__restrict__ J0;
+    const double *__restrict__ J2;
+    const double *__restrict__ h2;
+    const double *__restrict__ tkin;
+    const double *__restrict__ ab;
+    // per transition
+    const int *__restrict__ tr_rad;
+    const int *__restrict__ tr_col;
+    const double *__restrict__ tr_nu;
+    const double *__restrict__ tr_A;
+    const double *__restrict__ tr_B21;
+    const double *__restrict__ col_temps;
+    const double *__restrict__ Cji;
+    // program over the matrix entries
+    const int *__restrict__ ent_off;
+    const int *__restrict__ ent_pos;
+    const int *__restrict__ term_f;
+    const double *__restrict__ term_c;
+    const int *__restrict__ norm_col;   // (nlev) count_array
+    const double *__restrict__ norm_val;
+    const int *__restrict__ pack;       // (2 nlev) rho index or -1
+    double *pops;                       // (N, 2 nlev) column-major
+    double *jj20;                       // (N, L) or null
+    int *status;
+    int *nfail;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o >= 1; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// In-place LU with partial pivoting of the n x n column-major matrix M
+// (pivot: the first row of largest modulus, as LAPACK's IDAMAX picks).
+// Returns false if a pivot is zero.
+template <typename T>
+__device__ bool warp_lu(int n, T *M, int *piv, int lane) {
+    bool ok = true;
+    for (int k = 0; k < n; k++) {
+        T best = (T)-1;
+        int bi = n;
+        for (int i = k + lane; i < n; i += 32) {
+            T v = fabs(M[i + (size_t)n * k]);
+            if (v > best) { best = v; bi = i; }
+        }
+        for (int o = 16; o >= 1; o >>= 1) {
+            T ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (bi >= n) bi = k;  // NaN column: no row qualified; keep the diagonal
+        if (lane == 0) piv[k] = bi;
+        if (!(best > (T)0)) { ok = false; }
+        if (bi != k)
+            for (int j = lane; j < n; j += 32) {
+                T t = M[k + (size_t)n * j];
+                M[k + (size_t)n * j] = M[bi + (size_t)n * j];
+                M[bi + (size_t)n * j] = t;
+            }
+        __syncwarp();
+        const T d = M[k + (size_t)n * k];
+        const T r = (d != (T)0) ? (T)1 / d : (T)0;
+        for (int i = k + 1 + lane; i < n; i += 32) M[i + (size_t)n * k] *= r;
+        __syncwarp();
+        for (int i = k + 1 + lane; i < n; i += 32) {
+            const T lik = M[i + (size_t)n * k];
+            if (lik != (T)0)
+                for (int j = k + 1; j < n; j++) M[i + (size_t)n * j] -= lik * M[k + (size_t)n * j];
+        }
+        __syncwarp();
+    }
+    return ok;
+}
+
+// Solve (LU) x = P b in place in b (length n, shared memory).
+template <typename T, typename V>
+__device__ void warp_lu_solve(int n, const T *M, const int *piv, V *b, int lane) {
+    if (lane == 0)
+        for (int k = 0; k < n; k++)
+            if (piv[k] != k) { V t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
+    __syncwarp();
+    for (int k = 0; k < n; k++) {
+        const V bk = b[k];
+        for (int i = k + 1 + lane; i < n; i += 32) b[i] -= (V)M[i + (size_t)n * k] * bk;
+        __syncwarp();
+    }
+    for (int k = n - 1; k >= 0; k--) {
+        if (lane == 0) b[k] /= (V)M[k + (size_t)n * k];
+        __syncwarp();
+        const V bk = b[k];
+        for (int i = lane; i < k; i += 32) b[i] -= (V)M[i + (size_t)n * k] * bk;
+        __syncwarp();
+    }
+}
+
+// Dynamic shared memory per warp:
+//   A64 [n*n] double | feat [5*n_trans] double | x, r [n] double | d32 [n] float
+//   LU32 [n*n] float | scale [n] float | piv [n] int
+__host__ __device__ inline size_t se_warp_bytes(int n, int n_trans) {
+    size_t b = 0;
+    b += sizeof(double) * ((size_t)n * n + 5 * (size_t)n_trans + 2 * (size_t)n);
+    b += sizeof(float) * ((size_t)n * n + 2 * (size_t)n);
+    b += sizeof(int) * (size_t)n;
+    return (b + 15) & ~(size_t)15;
+}
+
+__global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n = a.c_dim;
+    unsigned char *base = smem + se_warp_bytes(n, a.n_trans) * wib;
+    double *A64 = (double *)base;
+    double *feat = A64 + (size_t)n * n;
+    double *x = feat + 5 * (size_t)a.n_trans;
+    double *r = x + n;
+    float *LU = (float *)(r + n);
+    float *d32 = LU + (size_t)n * n;
+    float *scl = d32 + n;
+    int *piv = (int *)(scl + n);
+
+    for (int node = blockIdx.x * nw + wib; node < a.bulk; node += gridDim.x * nw) {
+        if (!(a.ab[node] > 0.0)) continue;  // main_para.f90:213 (pops stay 0)
+        const double T = a.tkin[node], nH2 = a.h2[node];
+        // ---- features (make_AC miscellaneous.f90:331-390) ----
+        for (int t = lane; t < a.n_trans; t += 32) {
+            const int rr = a.tr_rad[t], cc = a.tr_col[t];
+            const double B21 = a.tr_B21[t];
+            double j0 = 0.0, j2 = 0.0, C21 = 0.0;
+            if (rr >= 0) {
+                j0 = a.J0[(size_t)node * a.L + rr];
+                j2 = a.J2[(size_t)node * a.L + rr];
+            }
+            if (cc >= 0) {
+                // temperature interpolation (first bracket; below the table the
+                // first bracket extrapolates, as the reference's loop does)
+                const int nT = a.c_temp;
+                double cr = 0.0;
+                for (int p = 0; p < a.c_par; p++) {
+                    const double *Ct = a.Cji + (size_t)nT * (cc + (size_t)a.c_num * p);
+                    double v = (T <= a.col_temps[0]) ? Ct[0] : 0.0;
+                    for (int i = 1; i < nT; i++)
+                        if (a.col_temps[i] > T) {
+                            const double ddT = (T - a.col_temps[i - 1]) / (a.col_temps[i] - a.col_temps[i - 1]);
+                            v = Ct[i - 1] + ddT * (Ct[i] - Ct[i - 1]);
+                            break;
+                        }
+                    cr += (a.c_par == 2 ? (p == 0 ? 0.25 : 0.75) : 1.0) * v;
+                }
+                C21 = cr * nH2 * 1e-6;
+            }
+            double *f = feat + 5 * (size_t)t;
+            f[0] = B21 * j0;
+            f[1] = B21 * j2;
+            f[2] = a.tr_A[t];
+            f[3] = C21;
+            f[4] = C21 * exp(-HK * a.tr_nu[t] / T);
+        }
+        for (int i = lane; i < n * n; i += 32) A64[i] = 0.0;
+        __syncwarp();
+        // ---- assembly (setup_stateq) ----
+        for (int e = lane; e < a.nent; e += 32) {
+            double v = 0.0;
+            for (int q = a.ent_off[e]; q < a.ent_off[e + 1]; q++) v += a.term_c[q] * feat[a.term_f[q]];
+            A64[a.ent_pos[e]] = v;
+        }
+        __syncwarp();
+        // ---- normalisation row (em_coefs.f90:158-164) ----
+        for (int j = lane; j < n; j += 32) A64[(size_t)n * j] = 0.0;
+        __syncwarp();
+        if (lane == 0)
+            for (int i = 0; i < a.nlev; i++) A64[(size_t)n * a.norm_col[i]] = a.norm_val[i];
+        __syncwarp();
+        // ---- FP32 LU of the row-scaled matrix ----
+        for (int i = lane; i < n; i += 32) {
+            double m = 0.0;
+            for (int j = 0; j < n; j++) m = fmax(m, fabs(A64[i + (size_t)n * j]));
+            scl[i] = (m > 0.0) ? (float)(1.0 / m) : 1.f;
+        }
+        __syncwarp();
+        for (int idx = lane; idx < n * n; idx += 32) {
+            const int i = idx % n;
+            LU[idx] = (float)(A64[idx] * (double)scl[i]);
+        }
+        __syncwarp();
+        int st = 0;
+        bool ok = warp_lu<float>(n, LU, piv, lane);
+        bool conv = false;
+        if (ok) {
+            for (int i = lane; i < n; i += 32) x[i] = 0.0;
+            __syncwarp();
+            double xmax = 0.0;
+            for (int it = 0; it < 8; it++) {
+                // r = e_1 - A x (FP64)
+                for (int i = lane; i < n; i += 32) {
+                    double s = (i == 0) ? 1.0 : 0.0;
+                    for (int j = 0; j < n; j++) s -= A64[i + (size_t)n * j] * x[j];
+                    d32[i] = (float)(s * (double)scl[i]);
+                }
+                __syncwarp();
+                warp_lu_solve<float, float>(n, LU, piv, d32, lane);
+                double dm = 0.0;
+                for (int i = lane; i < n; i += 32) {
+                    x[i] += (double)d32[i];
+                    dm = fmax(dm, fabs((double)d32[i]));
+                }
+                __syncwarp();
+                double xm = 0.0;
+                for (int i = lane; i < n; i += 32) xm = fmax(xm, fabs(x[i]));
+                dm = warp_max(dm);
+                xmax = warp_max(xm);
+                if (!(dm == dm) || !(xmax == xmax)) break;  // NaN
+                if (dm <= 1e-15 * xmax) { conv = true; break; }
+            }
+        }
+        if (!conv) {
+            // FP64 LU on the device (reuses LU32 + d32 storage as FP64 space
+            // is not available; re-assemble into A64 in place)
+            double *M = A64;
+            st |= ok ? PORTAL_NODE_REFINE : 0;
+            bool ok64 = warp_lu<double>(n, M, piv, lane);
+            if (!ok64) {
+                st |= PORTAL_NODE_SINGULAR;
+            } else {
+                for (int i = lane; i < n; i += 32) x[i] = (i == 0) ? 1.0 : 0.0;
+                __syncwarp();
+                warp_lu_solve<double, double>(n, M, piv, x, lane);
+                st |= PORTAL_NODE_REFINE;
+            }
+        }
+        __syncwarp();
+        // ---- packing (main_sub.f90:112-137) ----
+        for (int c2 = lane; c2 < 2 * a.nlev; c2 += 32) {
+            const int p = a.pack[c2];
+            double v = (p >= 0 && !(st & PORTAL_NODE_SINGULAR)) ? x[p] : 0.0;
+            if (st & PORTAL_NODE_SINGULAR) v = 0.0;
+            a.pops[(size_t)node + (size_t)a.N * c2] = v;
+        }
+        __syncwarp();
+        if (lane < a.nlev) {
+            const double v0 = a.pops[(size_t)node + (size_t)a.N * (2 * lane)];
+            if (v0 != v0) {
+                a.pops[(size_t)node + (size_t)a.N * (2 * lane)] = 0.0;
+                a.pops[(size_t)node + (size_t)a.N * (2 * lane + 1)] = 0.0;
+            }
+        }
+        if (a.jj20)
+            for (int l = lane; l < a.L; l += 32)
+                a.jj20[(size_t)node + (size_t)a.N * l] =
+                    a.J2[(size_t)node * a.L + l] / a.J0[(size_t)node * a.L + l];
+        if (lane == 0) {
+            a.status[node] |= st;
+            if (st & PORTAL_NODE_SINGULAR) atomicAdd(a.nfail, 1);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- host: the program ---------------------------------------------------
+
+struct Program {
+    int c_dim = 0, n_trans = 0;
+    std::vector<int> count_array, tr_lo, tr_up, tr_rad, tr_col;
+    std::vector<double> tr_nu, tr_A, tr_B21;
+    std::vector<int> ent_off, ent_pos, term_f, pack;
+    std::vector<double> term_c;
+};
+
+void build_program(const portal_ctx *c, int kmax, Program &P) {
+    const int nlev = c->nlev;
+    const std::vector<int> &J = c->j_lev;
+    // setup_count_array miscellaneous.f90:206-239
+    P.count_array.assign(nlev, 0);
+    int cnt = 0;
+    for (int i = 0; i < nlev; i++) {
+        P.count_array[i] = cnt;
+        for (int k = 0; k <= std::min(2 * J[i], kmax); k += 2) cnt++;
+    }
+    P.c_dim = cnt;
+    // all_transitions miscellaneous.f90:394-460
+    std::vector<int> T(nlev * nlev, 0);
+    auto mark = [&](int a, int b) {
+        if (c->e_levs[b] > c->e_levs[a]) T[a * nlev + b] = 1;
+        else T[b * nlev + a] = 1;
+    };
+    for (int i = 0; i < c->r_num; i++) mark(c->r_trans[2 * i] - 1, c->r_trans[2 * i + 1] - 1);
+    for (int i = 0; i < c->c_num; i++) mark(c->c_trans[2 * i] - 1, c->c_trans[2 * i + 1] - 1);
+    for (int i = 0; i < nlev; i++)
+        for (int j = 0; j < nlev; j++)
+            if (T[i * nlev + j]) { P.tr_lo.push_back(i); P.tr_up.push_back(j); }
+    P.n_trans = (int)P.tr_lo.size();
+    // make_AC's matching (first radiative / collisional entry with the same
+    // (lower, upper) ordering)
+    for (int t = 0; t < P.n_trans; t++) {
+        int lo = P.tr_lo[t], up = P.tr_up[t], rr = -1, cc = -1;
+        for (int j = 0; j < c->r_num; j++)
+            if (c->r_trans[2 * j] - 1 == lo && c->r_trans[2 * j + 1] - 1 == up) { rr = j; break; }
+        for (int j = 0; j < c->c_num; j++)
+            if (c->c_trans[2 * j] - 1 == lo && c->c_trans[2 * j + 1] - 1 == up) { cc = j; break; }
+        double nu = c->e_levs[up] - c->e_levs[lo];
+        double A = rr >= 0 ? c->A[rr] : 0.0;
+        P.tr_rad.push_back(rr);
+        P.tr_col.push_back(cc);
+        P.tr_nu.push_back(nu);
+        P.tr_A.push_back(A);
+        P.tr_B21.push_back(A_TO_B * A / std::pow(nu, 3.0));
+    }
+    // coupling-constant cache
+    std::map<std::tuple<int, int, int, int, int>, std::pair<double, double>> cache;
+    auto cc_get = [&](int which, int j, int k, int j2, int k2) {
+        auto key = std::make_tuple(which, j, k, j2, k2);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+        double a0, a2;
+        coupling_constants(which, j, k, j2, k2, &a0, &a2);
+        return cache[key] = std::make_pair(a0, a2);
+    };
+    const int n = P.c_dim;
+    std::map<int, std::vector<std::pair<int, double>>> ent;  // pos -> terms
+    auto add = [&](int c1, int c2, int t, int f, double coef) {
+        auto &v = ent[c1 + n * c2];
+        if (coef != 0.0) v.push_back({5 * t + f, coef});
+    };
+    auto touch = [&](int c1, int c2) { ent[c1 + n * c2]; };
+    for (int i1 = 0; i1 < nlev; i1++) {
+        std::vector<int> up, dn;  // transition ids in the reference's order
+        for (int i2 = 0; i2 < nlev; i2++)
+            for (int q = 0; q < P.n_trans; q++) {
+                if (P.tr_lo[q] == i1 && P.tr_up[q] == i2) up.push_back(q);
+                if (P.tr_lo[q] == i2 && P.tr_up[q] == i1) dn.push_back(q);
+            }
+        const int j1 = J[i1];
+        const double g1 = 2.0 * j1 + 1.0;
+        const int k1m = std::min(2 * j1, kmax);
+        for (int q : up) {  // pop_eqs.f90:467-515
+            int i2 = P.tr_up[q], j2 = J[i2];
+            double g2 = 2.0 * j2 + 1.0;
+            int c1 = P.count_array[i1];
+            for (int k1 = 0; k1 <= k1m; k1 += 2, c1++) {
+                int c2 = P.count_array[i2];
+                for (int k2 = 0; k2 <= std::min(2 * j2, kmax); k2 += 2, c2++) {
+                    auto ts = cc_get(1, j1, k1, j2, k2);
+                    auto te = cc_get(2, j1, k1, j2, k2);
+                    touch(c1, c2);
+                    add(c1, c2, q, 0, ts.first);
+                    add(c1, c2, q, 1, ts.second);
+                    add(c1, c2, q, 2, te.first);
+                    if (k1 == k2 && k1 == 0) add(c1, c2, q, 3, std::sqrt(g2 / g1));
+                }
+            }
+        }
+        for (int q : dn) {  // pop_eqs.f90:518-562
+            int i2 = P.tr_lo[q], j2 = J[i2];
+            double g2 = 2.0 * j2 + 1.0;
+            int c1 = P.count_array[i1];
+            for (int k1 = 0; k1 <= k1m; k1 += 2, c1++) {
+                int c2 = P.count_array[i2];
+                for (int k2 = 0; k2 <= std::min(2 * j2, kmax); k2 += 2, c2++) {
+                    auto ta = cc_get(0, j1, k1, j2, k2);
+                    touch(c1, c2);
+                    add(c1, c2, q, 0, (g1 / g2) * ta.first);
+                    add(c1, c2, q, 1, (g1 / g2) * ta.second);
+                    if (k1 == k2 && k1 == 0) add(c1, c2, q, 4, std::sqrt(g2 / g1) * (g1 / g2));
+                }
+            }
+        }
+        // diagonal block pop_eqs.f90:564-650
+        int c1 = P.count_array[i1];
+        for (int k1 = 0; k1 <= k1m; k1 += 2, c1++) {
+            int c2 = P.count_array[i1];
+            for (int k2 = 0; k2 <= k1m; k2 += 2, c2++) {
+                touch(c1, c2);
+                for (int q : up) {
+                    int j3 = J[P.tr_up[q]];
+                    double g3 = 2.0 * j3 + 1.0;
+                    auto ra = cc_get(3, j1, k1, j3, k2);
+                    add(c1, c2, q, 0, -(g3 / g1) * ra.first);
+                    add(c1, c2, q, 1, -(g3 / g1) * ra.second);
+                    if (k1 == k2) add(c1, c2, q, 4, -(g3 / g1));
+                }
+                for (int q : dn) {
+                    int j3 = J[P.tr_lo[q]];
+                    auto rs = cc_get(4, j1, k1, j3, k2);
+                    add(c1, c2, q, 0, -rs.first);
+                    add(c1, c2, q, 1, -rs.second);
+                    if (k1 == k2) {
+                        add(c1, c2, q, 2, -1.0);
+                        add(c1, c2, q, 3, -1.0);
+                    }
+                }
+            }
+        }
+    }
+    P.ent_off.assign(1, 0);
+    P.ent_pos.clear(); P.term_f.clear(); P.term_c.clear();
+    for (auto &kv : ent) {
+        P.ent_pos.push_back(kv.first);
+        for (auto &tc : kv.second) { P.term_f.push_back(tc.first); P.term_c.push_back(tc.second); }
+        P.ent_off.push_back((int)P.term_f.size());
+    }
+    // packing main_sub.f90:112-129
+    P.pack.assign(2 * nlev, -1);
+    for (int i = 0; i < nlev; i++) {
+        P.pack[2 * i] = P.count_array[i];
+        if (J[i] != 0) P.pack[2 * i + 1] = P.count_array[i] + 1;
+    }
+}
+
+}  // namespace
+
+namespace portal {
+
+int prepare_se(portal_ctx *c, int kmax) {
+    if (c->se_kmax == kmax) return PORTAL_OK;
+    Program P;
+    build_program(c, kmax, P);
+    // pack ints: tr_rad | tr_col | ent_off | ent_pos | term_f | norm_col | pack | col? ;
+    std::vector<int> I;
+    std::vector<double> D;
+    auto putI = [&](const std::vector<int> &v) { size_t o = I.size(); I.insert(I.end(), v.begin(), v.end()); return o; };
+    auto putD = [&](const std::vector<double> &v) { size_t o = D.size(); D.insert(D.end(), v.begin(), v.end()); return o; };
+    std::vector<double> norm_val(c->nlev);
+    for (int i = 0; i < c->nlev; i++) norm_val[i] = std::sqrt(2.0 * c->j_lev[i] + 1.0);
+    size_t o_rad = putI(P.tr_rad), o_col = putI(P.tr_col), o_eoff = putI(P.ent_off),
+           o_epos = putI(P.ent_pos), o_tf = putI(P.term_f), o_nc = putI(P.count_array),
+           o_pack = putI(P.pack);
+    size_t o_nu = putD(P.tr_nu), o_A = putD(P.tr_A), o_B = putD(P.tr_B21), o_tc = putD(P.term_c),
+           o_nv = putD(norm_val), o_ct = putD(c->col_temps), o_C = putD(c->Cji);
+    if (c->se_ints.reserve(I.size()) || c->se_dbls.reserve(D.size()))
+        return set_err(c, PORTAL_ERR_NOMEM, "SE program");
+    PCHECK(c, cudaMemcpyAsync(c->se_ints.p, I.data(), I.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    PCHECK(c, cudaMemcpyAsync(c->se_dbls.p, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    c->se_kmax = kmax;
+    c->c_dim = P.c_dim;
+    c->n_trans = P.n_trans;
+    c->count_array = P.count_array;
+    // remember offsets in the context (packed into se_off)
+    c->se_ni = (int)P.ent_pos.size();
+    c->se_offs[0] = o_rad; c->se_offs[1] = o_col; c->se_offs[2] = o_eoff; c->se_offs[3] = o_epos;
+    c->se_offs[4] = o_tf; c->se_offs[5] = o_nc; c->se_offs[6] = o_pack;
+    c->se_offs[7] = o_nu; c->se_offs[8] = o_A; c->se_offs[9] = o_B; c->se_offs[10] = o_tc;
+    c->se_offs[11] = o_nv; c->se_offs[12] = o_ct; c->se_offs[13] = o_C;
+    return PORTAL_OK;
+}
+
+int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
+    if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
+    if (kmax < 2 || (kmax & 1))
+        return set_err(c, PORTAL_ERR_ARG, "kmax must be even and >= 2 (trace_node packs rho^2_0)");
+    int rc = prepare_se(c, kmax);
+    if (rc) return rc;
+    const int n = c->c_dim;
+    const size_t wb = se_warp_bytes(n, c->n_trans);
+    int wpb = (int)std::min<size_t>(8, (200 * 1024) / wb);
+    if (wpb < 1) return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
+    const size_t smem = wb * wpb;
+    PCHECK(c, cudaFuncSetAttribute(k_solve_se, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (c->pops.reserve((size_t)c->N * 2 * c->nlev) || c->jj20.reserve((size_t)c->N * c->r_num))
+        return set_err(c, PORTAL_ERR_NOMEM, "SE outputs");
+    PCHECK(c, cudaMemsetAsync(c->pops.p, 0, (size_t)c->N * 2 * c->nlev * sizeof(double), c->stream));
+    PCHECK(c, cudaMemsetAsync(c->jj20.p, 0, (size_t)c->N * c->r_num * sizeof(double), c->stream));
+    PCHECK(c, cudaMemsetAsync(c->counters.p + 2, 0, sizeof(unsigned long long), c->stream));
+    SEArgs a;
+    a.N = c->N; a.bulk = c->bulk; a.c_dim = n; a.n_trans = c->n_trans; a.nlev = c->nlev; a.L = c->r_num;
+    a.c_temp = c->c_temp; a.c_num = c->c_num; a.c_par = c->c_par; a.nent = c->se_ni;
+    a.J0 = c->J0.p; a.J2 = c->J2.p; a.h2 = c->h2.p; a.tkin = c->tkin.p; a.ab = c->ab.p;
+    const int *I = c->se_ints.p;
+    const double *D = c->se_dbls.p;
+    a.tr_rad = I + c->se_offs[0]; a.tr_col = I + c->se_offs[1]; a.ent_off = I + c->se_offs[2];
+    a.ent_pos = I + c->se_offs[3]; a.term_f = I + c->se_offs[4]; a.norm_col = I + c->se_offs[5];
+    a.pack = I + c->se_offs[6];
+    a.tr_nu = D + c->se_offs[7]; a.tr_A = D + c->se_offs[8]; a.tr_B21 = D + c->se_offs[9];
+    a.term_c = D + c->se_offs[10]; a.norm_val = D + c->se_offs[11]; a.col_temps = D + c->se_offs[12];
+    a.Cji = D + c->se_offs[13];
+    a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
+    a.nfail = (int *)(c->counters.p + 2);
+    int nb = 0;
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_solve_se, 32 * wpb, smem));
+    int grid = c->sm_count * std::max(1, nb);
+    timer_start(c, T_SE);
+    k_solve_se<<<grid, 32 * wpb, smem, c->stream>>>(a);
+    timer_stop(c, T_SE);
+    PCHECK(c, cudaGetLastError());
+    int nf = 0;
+    PCHECK(c, cudaMemcpyAsync(&nf, c->counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    timer_collect(c, T_SE);
+    if (n_singular) *n_singular = nf;
+    return PORTAL_OK;
+}
+
+}  // namespace portal
+
+extern "C" int portal_solve_se(portal_ctx *c, int kmax, const double *J0, const double *J2,
+                               double *pol_pops, double *rates, double *JJ_20, int *status) {
+    if (!c) return PORTAL_ERR_ARG;
+    if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
+    cudaSetDevice(c->device);
+    const size_t LN = (size_t)c->r_num * c->N;
+    if ((J0 == nullptr) != (J2 == nullptr))
+        return set_err(c, PORTAL_ERR_ARG, "portal_solve_se: pass both J0 and J2 or neither");
+    if (J0) {
+        if (c->J0.reserve(LN) || c->J2.reserve(LN)) return set_err(c, PORTAL_ERR_NOMEM, "J buffers");
+        PCHECK(c, cudaMemcpyAsync(c->J0.p, J0, LN * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PCHECK(c, cudaMemcpyAsync(c->J2.p, J2, LN * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)c->N * sizeof(int), c->stream));
+        c->j_valid = true;
+    } else if (!c->j_valid) {
+        return set_err(c, PORTAL_ERR_STATE, "portal_solve_se: no device-resident radiation field");
+    }
+    timers_reset(c);
+    int nsing = 0;
+    int rc = portal::run_solve_se(c, kmax, &nsing);
+    if (rc) return rc;
+    if (pol_pops)
+        PCHECK(c, cudaMemcpyAsync(pol_pops, c->pops.p, (size_t)c->N * 2 * c->nlev * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+    if (JJ_20)
+        PCHECK(c, cudaMemcpyAsync(JJ_20, c->jj20.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (status)
+        PCHECK(c, cudaMemcpyAsync(status, c->status.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (rates) {
+        // rates output (extra_info = 1) is not implemented on the device yet
+        return set_err(c, PORTAL_ERR_ARG, "portal_solve_se: rates output is not supported; pass NULL");
+    }
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    if (nsing) return set_err(c, PORTAL_ERR_SINGULAR, std::to_string(nsing) + " singular SE systems");
+    return PORTAL_OK;
+}

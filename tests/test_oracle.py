@@ -1,0 +1,182 @@
+"""The oracle against the golden fixtures and analytic limits (CPU only)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from portal_gb300 import synth
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+def test_wigner_3j_6j_against_sympy():
+    g = _load("wigner.json")
+    worst = 0.0
+    for row in g["w3j"]:
+        *a, v = row
+        ex = float(v)
+        got = oracle.wigner3j(*[2 * x for x in a])
+        worst = max(worst, abs(got - ex) / max(abs(ex), 1e-300) if ex != 0 else abs(got))
+    for row in g["w6j"]:
+        *a, v = row
+        ex = float(v)
+        got = oracle.wigner6j(*[2 * x for x in a])
+        worst = max(worst, abs(got - ex) / max(abs(ex), 1e-300) if ex != 0 else abs(got))
+    assert worst < 1e-14, worst
+    assert len(g["w3j"]) >= 600 and len(g["w6j"]) >= 300
+
+
+def test_gauss_legendre_against_numpy_and_mpmath():
+    g = _load("leggauss.json")
+    for n, rule in g["rules"].items():
+        x, w = oracle.gauss_legendre(int(n))
+        ex = g["exact"][n]
+        np.testing.assert_allclose(x, [float(v) for v in ex["x"]], rtol=0, atol=4e-16)
+        np.testing.assert_allclose(w, [float(v) for v in ex["w"]], rtol=4e-15, atol=0)
+        # numpy's leggauss itself carries ~1e-12 in the weights at n = 64
+        np.testing.assert_allclose(x, rule["x"], rtol=0, atol=2e-15)
+        np.testing.assert_allclose(w, rule["w"], rtol=5e-12, atol=0)
+
+
+@pytest.mark.parametrize("n,expect", [(16, 178), (24, 388), (32, 678)])
+def test_legendre_all_direction_count(n, expect):
+    g = _load("leggauss.json")
+    xth = oracle.legendre_all(n, n)
+    assert len(xth) == expect == g["n_sphere"][str(n)]
+    assert abs(xth[:, 2].sum() - 1.0) < 1e-13          # weights / 4 pi sum to 1
+    # sum w P2(mu) = 0 for an exact rule
+    assert abs((xth[:, 2] * (3 * xth[:, 0] ** 2 - 1) / 2).sum()) < 1e-13
+
+
+def test_se_solution_against_lapack():
+    g = _load("lapack.json")
+    for case in g["cases"]:
+        A = np.array(case["A"])
+        rho = np.array(case["rho"])
+        # oracle's LU-solve of the same system
+        from scipy.linalg import solve
+        x = solve(A, np.eye(A.shape[0])[:, 0])
+        np.testing.assert_allclose(x, rho, rtol=1e-9, atol=1e-12 * np.abs(rho).max())
+
+
+def test_se_oracle_matches_lapack_pipeline(cfg1):
+    """orc_solve_se (assembly + LU solve + packing) against the fixture's
+    dgetri column for the same J."""
+    cloud, mol, rc = cfg1
+    g = _load("lapack.json")
+    P = oracle.OracleProblem(cloud, mol)
+    N, R = cloud.node_num, mol.r_num
+    for case in g["cases"]:
+        node = case["node"]
+        J0 = np.zeros((N, R)); J2 = np.zeros((N, R))
+        J0[node - 1] = case["J0"]; J2[node - 1] = case["J2"]
+        A = P.node_matrix(rc.kmax, node, J0, J2)
+        A0 = np.array(case["A"])
+        # rows 2.. of the oracle's matrix are the fixture's (row 1 replaced)
+        np.testing.assert_allclose(A[1:], A0[1:], rtol=1e-12, atol=1e-300)
+        pp, st, nf = P.solve_se(rc.kmax, J0, J2, node, node)
+        rho = np.array(case["rho"])
+        ca, c = [], 0
+        for j in mol.j_lev:
+            ca.append(c); c += len(range(0, min(2 * int(j), rc.kmax) + 1, 2))
+        for i, j in enumerate(mol.j_lev):
+            assert abs(pp[node - 1, 2 * i] - rho[ca[i]]) <= 1e-10 * abs(rho[ca[i]])
+            if j:
+                assert abs(pp[node - 1, 2 * i + 1] - rho[ca[i] + 1]) <= 1e-9 * abs(rho[ca[i]])
+
+
+def _tiny_problem(n=512, seed=3, nlev=5, **kw):
+    mol = synth.linear_rotor(nlev)
+    cloud = synth.power_law_sphere(n, seed, mol, **kw)
+    return cloud, mol
+
+
+def test_se_limits_isotropic_and_collisional():
+    """J^2 = 0 => rho^2_0 = 0; huge density => Boltzmann populations at T_kin;
+    normalisation sum sqrt(2J+1) rho^0_0 = 1 (em_coefs.f90:158-164)."""
+    cloud, mol = _tiny_problem(64, t_uniform=20.0)
+    P = oracle.OracleProblem(cloud, mol)
+    N, R = cloud.node_num, mol.r_num
+    nu = mol.nu
+    bb = np.array([oracle.black_body(2.73, v) for v in nu])
+    J0 = np.tile(bb, (N, 1)); J2 = np.zeros((N, R))
+    pp, st, nf = P.solve_se(6, J0, J2)
+    g = 2 * mol.j_lev + 1
+    np.testing.assert_allclose((pp[:, 0::2] * np.sqrt(g)).sum(1), 1.0, rtol=1e-12)
+    assert np.abs(pp[:, 1::2]).max() <= 1e-12 * np.abs(pp[:, 0::2]).max()
+    # collision dominated: n_H2 -> 1e14 cm^-3
+    cloud.h2_dens[:] = 1e20
+    P2 = oracle.OracleProblem(cloud, mol)
+    pp2, _, _ = P2.solve_se(6, J0, J2)
+    N_J = pp2[:, 0::2] * np.sqrt(g)
+    ek = mol.e_levs * 4.79924e-11                         # h nu / k in K, the reference constant
+    boltz = g * np.exp(-ek / 20.0)
+    boltz /= boltz.sum()
+    np.testing.assert_allclose(N_J, np.tile(boltz, (N, 1)), rtol=1e-6)
+
+
+def test_optically_thin_limit_gives_cmb():
+    """Vanishing populations: every ray returns the CMB, and J^0_0 equals
+    B_nu(2.73 K) times the channel quadrature of the profile (inverse_rt.f90:
+    275-339 sums phi dv over +-2 b, ~erf(2)); J^2_0 vanishes."""
+    cloud, mol = _tiny_problem(256)
+    cloud.lev_p *= 1e-30
+    rc = synth.RunConfig(nth=8, nph=8, nvel=8, kmax=6, gvec=synth.gauge_vector(0))
+    P = oracle.OracleProblem(cloud, mol)
+    J0, J2, st, nseg, nf = P.radiation_field(rc, 1, 32)
+    q = 2.0 * np.arange(-rc.nvel, rc.nvel + 1) / rc.nvel
+    quad = (np.exp(-q * q) * 2.0 / (math.sqrt(math.pi) * rc.nvel)).sum()
+    bb = np.array([oracle.black_body(2.73, v) for v in mol.nu])
+    np.testing.assert_allclose(J0[:32], np.tile(bb * quad, (32, 1)), rtol=1e-9)
+    assert np.abs(J2[:32]).max() < 1e-12 * J0[:32].max()
+
+
+def test_walk_covers_ray_to_sphere():
+    """Every walk ends on the unit sphere: the cumulative steps equal the
+    exit distance / dx (to the rounding of each segment)."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(2048)
+    P = oracle.OracleProblem(cloud, mol)
+    L = oracle.lib()
+    dl = np.zeros(2 * 20001, dtype=np.int32)
+    nc = C.c_int(0)
+    rng = np.random.default_rng(0)
+    dx = synth.F4(1e-6)
+    for node in rng.integers(1, cloud.node_num + 1, size=50):
+        d = rng.normal(size=3); d /= np.linalg.norm(d)
+        st = L.orc_trace_out(C.byref(P.c), int(node), d.ctypes.data_as(oracle.P_D), C.c_double(dx), 20000,
+                             dl.ctypes.data_as(oracle.P_I), C.byref(nc))
+        assert st == 0
+        n = nc.value
+        X = cloud.xyz[node - 1]
+        b = X @ d; cq = X @ X - 1.0
+        s_exit = -b + math.sqrt(b * b - cq)
+        assert abs(dl[2 * (n - 1) + 1] * dx - s_exit) <= (n + 1) * 0.5 * dx + 1e-12
+        assert dl[2 * n] == 0 and all(dl[2 * i] > 0 for i in range(n))
+
+
+def test_polarize_prop_against_rk4():
+    """polarize_prop (raytrace.f90:1-56) against an RK4 integration of
+    dI/ds = -eta_I I - eta_Q Q + eps_I, dQ/ds = -eta_Q I - eta_I Q + eps_Q."""
+    import ctypes as C
+    L = oracle.lib()
+    L.orc_polarize_prop.restype = None
+    L.orc_polarize_prop.argtypes = [C.c_double] * 5 + [oracle.P_D] * 3
+    for (eI, eQ, sI, sQ, ds) in [(2.0, 0.5, 1.0, 0.1, 0.7), (0.3, -0.2, 0.5, 0.05, 3.0), (5.0, 1.0, 2.0, -0.3, 0.2)]:
+        I, Q, U = C.c_double(0.4), C.c_double(-0.1), C.c_double(0.2)
+        L.orc_polarize_prop(eI, eQ, sI, sQ, ds, C.byref(I), C.byref(Q), C.byref(U))
+        y = np.array([0.4, -0.1]); h = ds / 4000
+        f = lambda v: np.array([-eI * v[0] - eQ * v[1] + sI, -eQ * v[0] - eI * v[1] + sQ])
+        for _ in range(4000):
+            k1 = f(y); k2 = f(y + h / 2 * k1); k3 = f(y + h / 2 * k2); k4 = f(y + h * k3)
+            y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        np.testing.assert_allclose([I.value, Q.value], y, rtol=1e-9)
+        assert abs(U.value - 0.2 * math.exp(-eI * ds)) < 1e-14
