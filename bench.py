@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Throughput of main_portal.x's node loop on GB300.
+
+One step = one pass of the hot path over the whole cloud: the radiation field
+of every node (line table + fused Voronoi walk / channel integration) and the
+polarized statistical-equilibrium solve of every node, i.e. the OpenMP loop
+main_para.f90:210-257 of the reference.  Workload: the power-law sphere with
+262,144 points (seed 1), a 10-level linear rotor (9 lines), 24x24 directions
+(388 rays per node), 129 velocity channels, kmax = 6 (34 x 34 SE systems).
+
+  value    ray-segments/s over all ranks, cloud resident in HBM, kernel work
+           timed with CUDA events on the library's stream, L2 flushed between
+           steps;
+  e2e      the same metric through the C ABI from pinned host buffers: every
+           step uploads the cloud (portal_set_cloud), runs the node loop and
+           reads pol_pops back;
+  cpu_baseline  the FP64 oracle port (OpenMP over nodes like the reference)
+           on this host's cores, on a bounded sample of the same nodes.
+
+--impl reference times that CPU port alone on the same workload.
+Multi-GPU: every rank runs its own replica of the workload (weak scaling);
+the ranks only meet for a barrier and the max of the step times.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-converged SE (1e-6 rel) warm-start vs plain; ray-segments/s; HBM GB/s"
+UNIT = "ray-segments/s"
+
+
+def workload_config(cloud, mol, rc, n_points):
+    return {
+        "workload": "power-law sphere, %d points (seed 1), %d-level linear rotor (%d lines), "
+                    "%dx%d directions, %d channels, kmax %d" % (n_points, mol.nlev, mol.r_num, rc.nth,
+                                                                 rc.nph, 2 * rc.nvel + 1, rc.kmax),
+        "points": int(n_points), "levels": int(mol.nlev), "lines": int(mol.r_num),
+        "directions": rc.nth, "channels": 2 * rc.nvel + 1, "kmax": rc.kmax,
+        "step": "radiation field + polarized SE solve of every node (main_portal.x node loop)",
+        "l2": "flushed between timed steps (256 MiB write)",
+    }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_segment():
+    """DRAM bytes per ray segment of the radiation-field kernel, from the ncu
+    summary committed under profiles/ (None when absent)."""
+    p = os.path.join(ROOT, "profiles", "radiation_field_cfg2.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_segment:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); smax = max(smax, float(r[2]))
+                for i, n in enumerate(names):
+                    if r[5 + i].strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def sample_nodes_for(seconds, per_node_s, n_total):
+    return int(max(16, min(n_total, seconds / max(per_node_s, 1e-6))))
+
+
+def cpu_port_rate(cloud, mol, rc, target_s, repeats=1):
+    """Oracle port on this host's cores over a contiguous node range (node
+    order is random in radius, so a range is a random sample)."""
+    import oracle
+    P = oracle.OracleProblem(cloud, mol)
+    nthreads = os.cpu_count() or 1
+    t = time.perf_counter()
+    _, _, _, nseg, _ = P.radiation_field(rc, 1, nthreads, nthreads)
+    per_node = (time.perf_counter() - t) / nthreads
+    n = sample_nodes_for(target_s, per_node / nthreads, cloud.bulk_node_num)
+    rates = []
+    for r in range(repeats):
+        lo = 1 + (r * n) % max(1, cloud.bulk_node_num - n)
+        t = time.perf_counter()
+        J0, J2, _, nseg, _ = P.radiation_field(rc, lo, lo + n - 1, nthreads)
+        P.solve_se(rc.kmax, J0, J2, lo, lo + n - 1, nthreads)
+        dt = time.perf_counter() - t
+        rates.append((nseg / dt, dt, n, nseg))
+    return rates, nthreads
+
+
+def build_workload(n_points):
+    from portal_gb300 import synth
+    return synth.config_cloud("cfg2", n_points=n_points)
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    cloud, mol, rc = build_workload(args.points)
+    cfg = workload_config(cloud, mol, rc, cloud.node_num)
+    for _ in range(args.warmup):
+        pass  # the CPU port has no warm-up state; each step is cold by construction
+    rates, cores = cpu_port_rate(cloud, mol, rc, args.cpu_seconds, repeats=args.steps)
+    vals = [r[0] for r in rates]
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.median([r[1] for r in rates]) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d consecutive nodes of %d per step, all their rays + SE" %
+                                       (rates[0][2], cloud.bulk_node_num)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import portal_gb300 as pg
+    from portal_gb300 import build as pbuild
+
+    pbuild.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    cloud, mol, rc = build_workload(args.points)
+    N, nlev = cloud.node_num, mol.nlev
+    stream = torch.cuda.Stream()
+    ctx = pg.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_molecule(mol)
+
+    # reference-layout host arrays in pinned memory (what a Fortran caller passes)
+    def pinned(a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        t = torch.empty(a.shape, dtype=torch.float64 if dtype == np.float64 else torch.int32, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+    temp = np.stack([cloud.t_kin, cloud.t_dust], axis=1)
+    host = dict(xyz=pinned(cloud.xyz, np.float64), vel=pinned(cloud.vel, np.float64),
+                b_all=pinned(cloud.b_all, np.float64), temp_all=pinned(temp, np.float64),
+                dust_p=pinned(cloud.dust_p, np.float64), h2_dens=pinned(cloud.h2_dens, np.float64),
+                ab_all=pinned(cloud.ab_all, np.float64), lev_p=pinned(cloud.lev_p, np.float64),
+                bvec=pinned(cloud.bvec, np.float64), del_ne=pinned(cloud.del_ne(), np.int32),
+                del_num_ne=pinned(cloud.del_num_ne(), np.int32))
+    h2d = sum(int(v.nbytes) for v in host.values())
+    pops_host = pinned(np.zeros((2 * nlev, N)), np.float64)
+    d2h = int(pops_host.nbytes) + 4 * N
+
+    def upload():
+        ctx.set_cloud_arrays(N, cloud.bulk_node_num, nlev, host["xyz"], host["vel"], host["b_all"],
+                             host["temp_all"], host["dust_p"], host["h2_dens"], host["ab_all"], host["lev_p"],
+                             host["bvec"], host["del_ne"], host["del_num_ne"], cloud.tx)
+
+    upload()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def step():
+        _, _, _, nseg = ctx.radiation_field(rc, fetch=False)
+        kt_rf = ctx.kernel_times()
+        ctx.solve_se(rc.kmax, fetch=False)
+        kt_se = ctx.kernel_times()
+        return nseg, kt_rf, kt_se
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    clocks.start()
+    times, rf_ms, launches, nseg_tot = [], [], 0, 0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        nseg, kt_rf, kt_se = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        rf_ms.append(kt_rf["radiation_field"][0])
+        launches += kt_rf["line_table"][1] + kt_rf["radiation_field"][1] + kt_se["solve_se"][1]
+        nseg_tot += nseg
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_total_ms = sum(times)
+    if dist:
+        tt = torch.tensor([t_total_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total_ms = float(tt.item())
+        ns = torch.tensor([nseg_tot], dtype=torch.float64)
+        dist.all_reduce(ns, op=dist.ReduceOp.SUM)
+        nseg_all = float(ns.item())
+    else:
+        nseg_all = float(nseg_tot)
+    value = nseg_all / (t_total_ms * 1e-3)
+    nseg_step = nseg_tot / args.steps
+
+    # ---- end to end through the C ABI from pinned host memory ----
+    e2e_times = []
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        upload()
+        ctx.radiation_field(rc, fetch=False)
+        ctx.solve_se(rc.kmax, out=pops_host)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = statistics.median(e2e_times)
+    if dist:
+        ev = torch.tensor([t_e2e], dtype=torch.float64)
+        dist.all_reduce(ev, op=dist.ReduceOp.MAX)
+        t_e2e = float(ev.item())
+    e2e_val = nseg_step * world / t_e2e
+
+    # ---- roofline of the dominant kernel (radiation field) ----
+    deg = float(np.diff(cloud.nb_off).mean())
+    b_seg = 4 + deg * (4 + 12) + 12 + 4 + 4 + 4 + 4 * nlev
+    rf_launch_ms = statistics.median(rf_ms)
+    achieved = b_seg * nseg_step / (rf_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    tps = traffic_per_segment()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (tps * nseg_step) if tps else None,
+            "kernel": "k_radiation_field", "algorithmic_bytes_per_segment": b_seg,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "launch_ms": rf_launch_ms, "segments_per_launch": nseg_step}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 ray integration, f32 LU + f64 refinement",
+            "data": "synthetic", "config": workload_config(cloud, mol, rc, N),
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rates, cores = cpu_port_rate(cloud, mol, rc, args.cpu_seconds, repeats=1)
+        line["cpu_baseline"] = {"value": rates[0][0], "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "%d consecutive nodes of %d (all their rays + SE), %.1f s" %
+                                          (rates[0][2], cloud.bulk_node_num, rates[0][1])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--points", type=int, default=262144)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+    return gpu_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -124,6 +124,12 @@ int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const do
 int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J2,
                     double *pol_pops, double *rates, double *JJ_20, int *status);
 
+/* Run this context's work on the caller's CUDA stream (a cudaStream_t
+ * passed as void*), or on the context's own stream when NULL.  Lets a caller
+ * order the library's kernels with its own work and time them with its own
+ * events.  No reference counterpart (the reference has no device). */
+int portal_set_stream(portal_ctx *ctx, void *cuda_stream);
+
 /* Kernel timing of the last call (CUDA events on the context's stream):
  * times_ms[0] line-table kernel, [1] radiation-field kernel, [2] SE kernel,
  * [3] emission-coefficient kernel, [4] image walk kernel, [5] image

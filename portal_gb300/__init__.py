@@ -30,7 +30,7 @@ KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_w
 EXPORTS = (
     "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
     "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
-    "portal_radiation_field", "portal_solve_se", "portal_last_kernel_times",
+    "portal_radiation_field", "portal_solve_se", "portal_last_kernel_times", "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
 )
 
@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
                                          P_D, P_D, P_I, C.POINTER(C.c_longlong)]
     L.portal_solve_se.argtypes = [C.c_void_p, C.c_int, P_D, P_D, P_D, P_D, P_D, P_I]
     L.portal_last_kernel_times.argtypes = [C.c_void_p, P_D, P_I, C.c_int]
+    L.portal_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     L.portal_wigner3j.restype = C.c_double
     L.portal_wigner3j.argtypes = [C.c_int] * 6
     L.portal_wigner6j.restype = C.c_double
@@ -148,6 +149,15 @@ class Context:
                                            float(cloud.tx)))
         self.N = N
 
+    def set_cloud_arrays(self, N, bulk, nlev, xyz, vel, b_all, temp_all, dust_p, h2_dens, ab_all, lev_p,
+                         bvec, del_ne, del_num_ne, tx):
+        """portal_set_cloud with the reference-layout arrays as given (no
+        copies: float64 / int32 C-contiguous arrays, e.g. in pinned memory)."""
+        self._check(lib().portal_set_cloud(self._h, N, bulk, nlev, _p(xyz), _p(vel), _p(b_all), _p(temp_all),
+                                           _p(dust_p), _p(h2_dens), _p(ab_all), _p(lev_p), _p(bvec),
+                                           del_ne.shape[0], _p(del_ne, P_I), _p(del_num_ne, P_I), float(tx)))
+        self.N = N
+
     def set_populations(self, lev_p):
         self._check(lib().portal_set_populations(self._h, _p(_f64(lev_p))))
 
@@ -164,8 +174,13 @@ class Context:
                                                  rc.n_depth, _p(J0), _p(J2), _p(st, P_I), C.byref(nseg)))
         return J0, J2, st, int(nseg.value)
 
-    def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False):
-        """pol_pops as (N, 2*nlev) (reference pol_pops(node,:)), status."""
+    def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False, out=None):
+        """pol_pops as (N, 2*nlev) (reference pol_pops(node,:)), status.
+        out: a float64 (2*nlev, N) C-contiguous buffer (the reference's
+        pol_pops(N, 2*nlev) memory) to receive the result without a copy."""
+        if out is not None:
+            self._check(lib().portal_solve_se(self._h, kmax, None, None, _p(out), None, None, None))
+            return out, None
         pp = np.zeros((2 * self.nlev, self.N)) if fetch else None      # Fortran (N, 2 nlev)
         jj = np.zeros((self.r_num, self.N)) if jj20 else None
         st = np.zeros(self.N, dtype=np.int32) if fetch else None
@@ -176,6 +191,10 @@ class Context:
         if jj20:
             out = out + (jj.T.copy(),)
         return out
+
+    def set_stream(self, stream_ptr: int | None):
+        """Run on a caller-owned cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(lib().portal_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
     def kernel_times(self):
         t = np.zeros(len(KERNEL_SLOTS))

@@ -48,7 +48,8 @@ enum TimerSlot { T_LINETAB = 0, T_RF = 1, T_SE = 2, T_EMCOEF = 3, T_IMWALK = 4, 
 struct portal_ctx {
     int device = 0;
     int sm_count = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // the stream all work runs on
+    cudaStream_t own_stream = nullptr;   // created by portal_create
     std::string err;
 
     // ---- molecule (host copies, FP64) ----

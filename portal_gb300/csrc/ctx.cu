@@ -64,8 +64,9 @@ extern "C" int portal_create(portal_ctx **out, int device) {
     portal_ctx *c = new portal_ctx();
     c->device = device;
     c->sm_count = prop.multiProcessorCount;
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); delete c; return PORTAL_ERR_CUDA; }
+    c->stream = c->own_stream;
     for (int i = 0; i < 2 * T_NSLOT; i++) cudaEventCreate(&c->ev[i]);
     c->ev_ready = true;
     if (c->counters.reserve(8) != cudaSuccess) { delete c; return PORTAL_ERR_NOMEM; }
@@ -79,7 +80,7 @@ extern "C" int portal_destroy(portal_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->ev_ready)
         for (int i = 0; i < 2 * T_NSLOT; i++) cudaEventDestroy(c->ev[i]);
-    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;  // DevBuf destructors free device memory
     return PORTAL_OK;
 }
@@ -248,6 +249,14 @@ extern "C" int portal_set_populations(portal_ctx *c, const double *lev_p) {
                               cudaMemcpyHostToDevice, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
     c->j_valid = false;
+    return PORTAL_OK;
+}
+
+extern "C" int portal_set_stream(portal_ctx *c, void *stream) {
+    if (!c) return PORTAL_ERR_ARG;
+    cudaSetDevice(c->device);
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
     return PORTAL_OK;
 }
 

@@ -11,26 +11,28 @@
 //                  A = kv * c/nu / (sqrt(pi) b) * tx*dx   (optical depth per
 //                  trace step per unit Gaussian profile value), E the same
 //                  for the emissivity, and the dust terms.  HBM-bound, tiny.
-//   k_radiation_field  one warp per node (persistent warps, node queue):
-//                  for each direction of legendre_all
-//                   (1) FP64 set-up: the direction (find_dir's rotation in
-//                       closed form) and the sphere-exit distance
-//                       (pos_quadratic from the node, as trace_out's first
-//                       step computes it);
-//                   (2) the Voronoi walk, lanes over the neighbours of the
-//                       current cell.  The photon is kept relative to the
+//   k_radiation_field  one warp per node (persistent warps, node queue);
+//                  the directions of legendre_all in batches of 32 rays:
+//                   (1) FP64 set-up, one lane per ray: the direction
+//                       (find_dir's rotation in closed form) and the
+//                       sphere-exit distance (pos_quadratic from the node,
+//                       as trace_out's first step computes it);
+//                   (2) the Voronoi walk, one lane per ray, 32 rays in
+//                       flight per warp.  The photon is kept relative to the
 //                       current node, so the face crossing
 //                       t = (|e|^2/2 - e.r) / (e.d) is formed from the
 //                       FP64-derived edge vectors without cancellation
-//                       against absolute coordinates.  Warp min-reduction
-//                       with the reference's tie rule (the last neighbour
-//                       in list order wins);
+//                       against absolute coordinates; the neighbour scan
+//                       keeps check_neigh_fast's sequential tie rule.  The
+//                       (cell, steps) list of each ray goes to a per-warp
+//                       scratch slice in global memory (L2-resident);
 //                   (3) the channel integration inward over the walk, lanes
 //                       over channels, lines looped in registers, cell
 //                       records staged in shared memory 32 cells at a time;
 //                   (4) the profile-weighted channel sum (warp reduction)
 //                       and the FP64 accumulation of J^0_0 and J^2_0.
 #include <cmath>
+#include <cstdlib>
 
 #include "common.cuh"
 
@@ -115,6 +117,14 @@ struct CellRec {
     float Jd[32][DUST ? NLG : 1];   // dust emissivity * steps (dust only)
 };
 
+// Per-warp shared state of the node being processed and its current batch of
+// (up to) 32 rays.
+struct RayBatch {
+    double frame[13];    // b(3), x(3), w(3), node position(3), |p|^2
+    float4 dir[32];      // (d_x, d_y, d_z, v_node . d) per ray
+    int K[32];           // segments per ray (-1: n_depth overflow)
+};
+
 // NS channel slots per lane (nch <= 32 NS), NLG lines per register group.
 template <int NS, int NLG, bool DUST>
 __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
@@ -122,21 +132,13 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
-    int2 *wl = a.walk + (size_t)gw * (size_t)a.n_depth;
+    int2 *const wbase = a.walk + (size_t)gw * 32 * (size_t)a.n_depth;
     __shared__ CellRec<NLG, DUST> recs[8];
+    __shared__ RayBatch rbs[8];
     CellRec<NLG, DUST> &R = recs[wib];
+    RayBatch &B = rbs[wib];
 
-    float q0c[NS], wch[NS];
-    int nvs[NS];
-#pragma unroll
-    for (int s = 0; s < NS; s++) {
-        int ch = lane + 32 * s;
-        nvs[s] = ch - a.nvel;
-        q0c[s] = (ch < a.nch) ? a.chq[ch] : 0.f;
-        wch[s] = (ch < a.nch) ? a.chw[ch] : 0.f;
-    }
     unsigned long long nseg = 0;
-
     for (;;) {
         int node = 0;
         if (lane == 0) node = (int)atomicAdd(&a.counters[0], 1ULL);
@@ -145,203 +147,213 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
         double acc0a = 0.0, acc0b = 0.0, acc2a = 0.0, acc2b = 0.0;  // lines lane, lane+32
         int st = 0;
         if (a.ab[node] > 0.0) {
-            // node frame (find_dir miscellaneous.f90:48-82): x = b x g / |b x g|,
-            // dir = R(b,ph) R(x,th) b = cos th b + sin th (cos ph (x x b) + sin ph x)
-            const double bx = a.bvec[3 * (size_t)node], by = a.bvec[3 * (size_t)node + 1],
-                         bz = a.bvec[3 * (size_t)node + 2];
-            double xx = by * a.gz - bz * a.gy, xy = bz * a.gx - bx * a.gz, xz = bx * a.gy - by * a.gx;
-            double xn = sqrt(xx * xx + xy * xy + xz * xz);
-            xx /= xn; xy /= xn; xz /= xn;
-            const double wx = xy * bz - xz * by, wy = xz * bx - xx * bz, wz = xx * by - xy * bx;
-            const double px = a.pos[3 * (size_t)node], py = a.pos[3 * (size_t)node + 1],
-                         pz = a.pos[3 * (size_t)node + 2];
-            const double pp = px * px + py * py + pz * pz;
+            if (lane == 0) {
+                // node frame (find_dir miscellaneous.f90:48-82): x = b x g / |b x g|,
+                // dir = R(b,ph) R(x,th) b = cos th b + sin th (cos ph (x x b) + sin ph x)
+                const double bx = a.bvec[3 * (size_t)node], by = a.bvec[3 * (size_t)node + 1],
+                             bz = a.bvec[3 * (size_t)node + 2];
+                double xx = by * a.gz - bz * a.gy, xy = bz * a.gx - bx * a.gz, xz = bx * a.gy - by * a.gx;
+                const double xn = sqrt(xx * xx + xy * xy + xz * xz);
+                xx /= xn; xy /= xn; xz /= xn;
+                const double px = a.pos[3 * (size_t)node], py = a.pos[3 * (size_t)node + 1],
+                             pz = a.pos[3 * (size_t)node + 2];
+                double *f = B.frame;
+                f[0] = bx; f[1] = by; f[2] = bz; f[3] = xx; f[4] = xy; f[5] = xz;
+                f[6] = xy * bz - xz * by; f[7] = xz * bx - xx * bz; f[8] = xx * by - xy * bx;
+                f[9] = px; f[10] = py; f[11] = pz; f[12] = px * px + py * py + pz * pz;
+            }
+            __syncwarp();
             const float4 cvn = a.cellv[node];
             const float dqfac = 2.f * cvn.w / (float)a.nvel;
 
-            for (int k = 0; k < a.ndir; k++) {
-                const double *dr = a.dirs + 6 * (size_t)k;
-                const double mu = dr[0], sth = dr[1], cph = dr[2], sph = dr[3];
-                const double dx = mu * bx + sth * (cph * wx + sph * xx);
-                const double dy = mu * by + sth * (cph * wy + sph * xy);
-                const double dz = mu * bz + sth * (cph * wz + sph * xz);
-                // pos_quadratic(|d|^2, 2 p.d, |p|^2 - 1) from the node
-                double aq = dx * dx + dy * dy + dz * dz;
-                double bq = 2.0 * (px * dx + py * dy + pz * dz);
-                double dis = bq * bq - 4.0 * aq * (pp - 1.0);
-                double sexit = 0.0;
-                if (dis > 0.0) {
-                    double sq = sqrt(dis);
-                    double x1 = (-bq + sq) / (2.0 * aq), x2 = (-bq - sq) / (2.0 * aq);
-                    sexit = (x2 > 0.0) ? x2 : x1;
-                }
-                const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
-
-                // ---- (2) walk ----
-                double s = 0.0;
-                float rx = 0.f, ry = 0.f, rz = 0.f;
-                int c = node, K = 0;
+            for (int k0 = 0; k0 < a.ndir && st == 0; k0 += 32) {
+                const int nr = min(32, a.ndir - k0);
+                // ---- (1)+(2) set-up and walk, one lane per ray ----
+                int K = 0;
                 bool over = false;
-                for (;;) {
-                    const float tsph = (float)(sexit - s);
-                    const int o = a.off[c], deg = a.off[c + 1] - o;
-                    unsigned best = 0xffffffffu;
-                    int bestj = -1;
-                    float4 eb = make_float4(0.f, 0.f, 0.f, 0.f);
-                    for (int base = 0; base < deg; base += 32) {
-                        const int j = base + lane;
-                        unsigned tb = 0xffffffffu;
-                        float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (j < deg) {
-                            e = a.edge[o + j];
+                if (lane < nr) {
+                    const double *dr = a.dirs + 6 * (size_t)(k0 + lane);
+                    const double *f = B.frame;
+                    const double mu = dr[0], sth = dr[1], cph = dr[2], sph = dr[3];
+                    const double dx = mu * f[0] + sth * (cph * f[6] + sph * f[3]);
+                    const double dy = mu * f[1] + sth * (cph * f[7] + sph * f[4]);
+                    const double dz = mu * f[2] + sth * (cph * f[8] + sph * f[5]);
+                    // pos_quadratic(|d|^2, 2 p.d, |p|^2 - 1) from the node
+                    const double aq = dx * dx + dy * dy + dz * dz;
+                    const double bq = 2.0 * (f[9] * dx + f[10] * dy + f[11] * dz);
+                    const double dis = bq * bq - 4.0 * aq * (f[12] - 1.0);
+                    double sexit = 0.0;
+                    if (dis > 0.0) {
+                        const double sq = sqrt(dis);
+                        const double x1 = (-bq + sq) / (2.0 * aq), x2 = (-bq - sq) / (2.0 * aq);
+                        sexit = (x2 > 0.0) ? x2 : x1;
+                    }
+                    const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+                    B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
+                    int2 *wl = wbase + (size_t)lane * a.n_depth;
+                    double s = 0.0;
+                    float rx = 0.f, ry = 0.f, rz = 0.f;
+                    int c = node;
+                    for (;;) {
+                        const float tsph = (float)(sexit - s);
+                        const int o = a.off[c], deg = a.off[c + 1] - o;
+                        // check_neigh_fast's scan: best starts at the sphere exit, a
+                        // neighbour replaces it when FACE_EPS < t <= best (so among equal
+                        // t the later neighbour wins).  t = num/den compared by cross
+                        // multiplication (den > 0).
+                        float bnum = tsph, bden = 1.f;
+                        int bj = -1;
+                        for (int j = 0; j < deg; j++) {
+                            const float4 e = a.edge[o + j];
                             const float den = e.x * fdx + e.y * fdy + e.z * fdz;
                             const float num = e.w - (e.x * rx + e.y * ry + e.z * rz);
-                            if (den > 0.f) {
-                                const float t = num / den;
-                                if (t > FACE_EPS && t <= tsph) tb = __float_as_uint(t);
+                            if (den > 0.f && num > FACE_EPS * den && num * bden <= bnum * den) {
+                                bnum = num;
+                                bden = den;
+                                bj = j;
                             }
                         }
-                        const unsigned m = __reduce_min_sync(FULL, tb);
-                        if (m != 0xffffffffu && m <= best) {
-                            const unsigned bal = __ballot_sync(FULL, tb == m);
-                            const int jl = 31 - __clz(bal);
-                            best = m;
-                            bestj = base + jl;
-                            eb.x = __shfl_sync(FULL, e.x, jl);
-                            eb.y = __shfl_sync(FULL, e.y, jl);
-                            eb.z = __shfl_sync(FULL, e.z, jl);
-                        }
+                        const float delta = (bj < 0) ? tsph : bnum / bden;
+                        if (K >= a.n_depth) { over = true; break; }
+                        wl[K] = make_int2(c, (int)roundf(delta / a.dx32));  // nint(delta_x/dx)
+                        K++;
+                        if (bj < 0) break;
+                        const float4 e = a.edge[o + bj];
+                        s += (double)delta;
+                        rx = fmaf(delta, fdx, rx) - e.x;
+                        ry = fmaf(delta, fdy, ry) - e.y;
+                        rz = fmaf(delta, fdz, rz) - e.z;
+                        c = a.idx[o + bj];
                     }
-                    const float delta = (bestj < 0) ? tsph : __uint_as_float(best);
-                    const int steps = (int)roundf(delta / a.dx32);  // nint(delta_x/dx)
-                    if (K >= a.n_depth) { over = true; break; }
-                    if (lane == 0) wl[K] = make_int2(c, steps);
-                    K++;
-                    if (bestj < 0) break;
-                    s += (double)delta;
-                    rx = fmaf(delta, fdx, rx) - eb.x;
-                    ry = fmaf(delta, fdy, ry) - eb.y;
-                    rz = fmaf(delta, fdz, rz) - eb.z;
-                    c = a.idx[o + bestj];
                 }
-                if (over) { st |= PORTAL_NODE_DEPTH; break; }
-                nseg += (unsigned long long)K;
+                B.K[lane] = over ? -1 : K;
+                if (__any_sync(FULL, over)) { st |= PORTAL_NODE_DEPTH; break; }
                 __syncwarp();
 
-                // ---- (3) channel integration, inward ----
-                const float vcp = cvn.x * fdx + cvn.y * fdy + cvn.z * fdz;
-                const int2 w0 = wl[0];
-                const double wgt = dr[4], wgt2 = dr[5];
-                for (int l0 = 0; l0 < a.L; l0 += NLG) {
-                    float I[NS][NLG];
+                // ---- (3)+(4) channel integration of each ray of the batch ----
+                for (int rr = 0; rr < nr; rr++) {
+                    const int Kr = B.K[rr];
+                    const int2 *wl = wbase + (size_t)rr * a.n_depth;
+                    const float4 d4 = B.dir[rr];
+                    const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
+                    const double wgt = dr[4], wgt2 = dr[5];
+                    nseg += (unsigned long long)Kr;
+                    const int2 w0 = wl[0];
+                    for (int l0 = 0; l0 < a.L; l0 += NLG) {
+                        float I[NS][NLG];
 #pragma unroll
-                    for (int l = 0; l < NLG; l++) {
-                        const float bb = (l0 + l < a.L) ? (float)c_lines[l0 + l].bb_cmb : 0.f;
+                        for (int l = 0; l < NLG; l++) {
+                            const float bb = (l0 + l < a.L) ? (float)c_lines[l0 + l].bb_cmb : 0.f;
 #pragma unroll
-                        for (int s2 = 0; s2 < NS; s2++) I[s2][l] = bb;
-                    }
-                    for (int hi = K - 1; hi >= 1; hi -= 32) {
-                        const int nc = min(32, hi);
-                        if (lane < nc) {
-                            const int2 wc = wl[hi - lane];
-                            const float4 cv = a.cellv[wc.x];
-                            const float vp = cv.x * fdx + cv.y * fdy + cv.z * fdz;
-                            const float ib = 1.f / cv.w;
-                            R.q0[lane] = (vcp - vp) * ib;
-                            R.dq[lane] = dqfac * ib;
-                            const float fst = (float)wc.y;
-                            const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
+                            for (int s2 = 0; s2 < NS; s2++) I[s2][l] = bb;
+                        }
+                        for (int hi = Kr - 1; hi >= 1; hi -= 32) {
+                            const int nc = min(32, hi);
+                            __syncwarp();
+                            if (lane < nc) {
+                                const int2 wc = wl[hi - lane];
+                                const float4 cv = a.cellv[wc.x];
+                                const float vp = cv.x * d4.x + cv.y * d4.y + cv.z * d4.z;
+                                const float ib = 1.f / cv.w;
+                                R.q0[lane] = (d4.w - vp) * ib;
+                                R.dq[lane] = dqfac * ib;
+                                const float fst = (float)wc.y;
+                                const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
 #pragma unroll
-                            for (int l = 0; l < NLG; l++) {
-                                if (l0 + l < a.L) {
-                                    const float4 v = lt[l];
-                                    R.As[lane][l] = v.x * fst;
-                                    if (DUST) {
-                                        R.Ss[lane][l] = v.y * fst;
-                                        R.Ad[lane][DUST ? l : 0] = v.z * fst;
-                                        R.Jd[lane][DUST ? l : 0] = v.w * fst;
-                                    } else {
-                                        R.Ss[lane][l] = v.y / v.x;
+                                for (int l = 0; l < NLG; l++) {
+                                    if (l0 + l < a.L) {
+                                        const float4 v = lt[l];
+                                        R.As[lane][l] = v.x * fst;
+                                        if (DUST) {
+                                            R.Ss[lane][l] = v.y * fst;
+                                            R.Ad[lane][DUST ? l : 0] = v.z * fst;
+                                            R.Jd[lane][DUST ? l : 0] = v.w * fst;
+                                        } else {
+                                            R.Ss[lane][l] = v.y / v.x;
+                                        }
+                                    }
+                                }
+                            }
+                            __syncwarp();
+                            for (int u = 0; u < nc; u++) {
+                                const float q0 = R.q0[u], dq = R.dq[u];
+                                float g[NS];
+#pragma unroll
+                                for (int s2 = 0; s2 < NS; s2++) {
+                                    const float q = fmaf(dq, (float)(lane + 32 * s2 - a.nvel), q0);
+                                    g[s2] = ex2(-q * q * LOG2E_F);
+                                }
+#pragma unroll
+                                for (int l = 0; l < NLG; l++) {
+                                    if (l0 + l < a.L) {
+                                        const float Au = R.As[u][l];
+                                        const float Su = R.Ss[u][l];
+                                        float Adu = 0.f, Jdu = 0.f;
+                                        if (DUST) { Adu = R.Ad[u][DUST ? l : 0]; Jdu = R.Jd[u][DUST ? l : 0]; }
+#pragma unroll
+                                        for (int s2 = 0; s2 < NS; s2++) {
+                                            float tau, Sv;
+                                            if (DUST) {
+                                                // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
+                                                tau = fmaf(Au, g[s2], Adu);
+                                                Sv = fmaf(Su, g[s2], Jdu) / tau;
+                                            } else {
+                                                tau = Au * g[s2];
+                                                Sv = Su;
+                                            }
+                                            const float e = ex2(-tau * LOG2E_F);
+                                            const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                            I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                        }
                                     }
                                 }
                             }
                         }
-                        __syncwarp();
-                        for (int u = 0; u < nc; u++) {
-                            const float q0 = R.q0[u], dq = R.dq[u];
-                            float g[NS];
+                        // central cell (inverse_rt.f90:320-339): no gate, profile at
+                        // the node's own b, then the weighted channel sum
+                        const float fst0 = (float)w0.y;
+                        float part[NLG];
 #pragma unroll
-                            for (int s2 = 0; s2 < NS; s2++) {
-                                const float q = fmaf(dq, (float)nvs[s2], q0);
-                                g[s2] = ex2(-q * q * LOG2E_F);
-                            }
+                        for (int l = 0; l < NLG; l++) {
+                            part[l] = 0.f;
+                            if (l0 + l < a.L) {
+                                const float4 v = a.ltab[(size_t)node * a.L + l0 + l];
 #pragma unroll
-                            for (int l = 0; l < NLG; l++) {
-                                if (l0 + l < a.L) {
-                                    const float Au = R.As[u][l];
-                                    const float Su = R.Ss[u][l];
-                                    float Adu = 0.f, Jdu = 0.f;
-                                    if (DUST) { Adu = R.Ad[u][DUST ? l : 0]; Jdu = R.Jd[u][DUST ? l : 0]; }
-#pragma unroll
-                                    for (int s2 = 0; s2 < NS; s2++) {
+                                for (int s2 = 0; s2 < NS; s2++) {
+                                    const int ch = lane + 32 * s2;
+                                    if (ch < a.nch) {
+                                        const float q0c = a.chq[ch];
+                                        const float g0 = ex2(-q0c * q0c * LOG2E_F);
                                         float tau, Sv;
                                         if (DUST) {
-                                            // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
-                                            tau = fmaf(Au, g[s2], Adu);
-                                            Sv = fmaf(Su, g[s2], Jdu) / tau;
+                                            const float kap = fmaf(v.x, g0, v.z);
+                                            tau = kap * fst0;
+                                            Sv = fmaf(v.y, g0, v.w) / kap;
                                         } else {
-                                            tau = Au * g[s2];
-                                            Sv = Su;
+                                            tau = v.x * g0 * fst0;
+                                            Sv = v.y / v.x;
                                         }
                                         const float e = ex2(-tau * LOG2E_F);
-                                        const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
-                                        I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                        const float Io = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                        part[l] = fmaf(a.chw[ch], Io, part[l]);
                                     }
                                 }
                             }
                         }
-                        __syncwarp();
-                    }
-                    // central cell (inverse_rt.f90:320-339): no gate, profile at
-                    // the node's own b, then the weighted channel sum
-                    const float fst0 = (float)w0.y;
-                    float part[NLG];
 #pragma unroll
-                    for (int l = 0; l < NLG; l++) {
-                        part[l] = 0.f;
-                        if (l0 + l < a.L) {
-                            const float4 v = a.ltab[(size_t)node * a.L + l0 + l];
+                        for (int l = 0; l < NLG; l++) {
+                            float v = part[l];
 #pragma unroll
-                            for (int s2 = 0; s2 < NS; s2++) {
-                                const float g0 = ex2(-q0c[s2] * q0c[s2] * LOG2E_F);
-                                float tau, Sv;
-                                if (DUST) {
-                                    const float kap = fmaf(v.x, g0, v.z);
-                                    tau = kap * fst0;
-                                    Sv = fmaf(v.y, g0, v.w) / kap;
+                            for (int o2 = 16; o2 >= 1; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
+                            const int line = l0 + l;
+                            if (line < a.L && (line & 31) == lane) {
+                                if (line < 32) {
+                                    acc0a += wgt * (double)v;
+                                    acc2a += wgt2 * (double)v;
                                 } else {
-                                    tau = v.x * g0 * fst0;
-                                    Sv = v.y / v.x;
+                                    acc0b += wgt * (double)v;
+                                    acc2b += wgt2 * (double)v;
                                 }
-                                const float e = ex2(-tau * LOG2E_F);
-                                const float Io = fmaf(I[s2][l], e, Sv * (1.f - e));
-                                part[l] = fmaf(wch[s2], Io, part[l]);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int l = 0; l < NLG; l++) {
-                        float v = part[l];
-#pragma unroll
-                        for (int o2 = 16; o2 >= 1; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
-                        const int line = l0 + l;
-                        if (line < a.L && (line & 31) == lane) {
-                            if (line < 32) {
-                                acc0a += wgt * (double)v;
-                                acc2a += wgt2 * (double)v;
-                            } else {
-                                acc0b += wgt * (double)v;
-                                acc2b += wgt2 * (double)v;
                             }
                         }
                     }
@@ -358,6 +370,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
             a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b : 0.0;
         }
         if (lane == 0) a.status[node] = st;
+        __syncwarp();
     }
     // segment count (every lane holds the same count)
     if (lane == 0) atomicAdd(&a.counters[1], nseg);
@@ -399,7 +412,7 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     if (nb < 1) nb = 1;
     int grid = nb * c->sm_count;
     size_t nslots = (size_t)grid * 8;
-    if (c->walk.reserve(nslots * (size_t)n_depth) != cudaSuccess)
+    if (c->walk.reserve(nslots * 32 * (size_t)n_depth) != cudaSuccess)
         return set_err(c, PORTAL_ERR_NOMEM, "walk scratch allocation failed");
     a.walk = c->walk.p;
     PCHECK(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
@@ -410,9 +423,20 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     return PORTAL_OK;
 }
 
+// Line-group width: lines whose intensities one lane keeps in registers at
+// once.  5 keeps the kernel under 128 registers (two 256-thread blocks per
+// SM); 10 saves one Gaussian-profile evaluation per cell for 6..10 lines.
+// PORTAL_RF_LINE_GROUP=5|10 overrides the choice.
+inline int line_group(int L) {
+    const char *e = getenv("PORTAL_RF_LINE_GROUP");
+    if (e && (atoi(e) == 5 || atoi(e) == 10)) return atoi(e);
+    (void)L;
+    return 5;
+}
+
 template <int NS>
 int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
-    if (a.L <= 5)
+    if (line_group(a.L) == 5)
         return c->has_dust ? launch_rf<NS, 5, true>(c, a, n_depth) : launch_rf<NS, 5, false>(c, a, n_depth);
     return c->has_dust ? launch_rf<NS, 10, true>(c, a, n_depth) : launch_rf<NS, 10, false>(c, a, n_depth);
 }

@@ -231,8 +231,8 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
         if (ok) {
             for (int i = lane; i < n; i += 32) x[i] = 0.0;
             __syncwarp();
-            double xmax = 0.0;
-            for (int it = 0; it < 8; it++) {
+            double xmax = 0.0, dprev = 1e300;
+            for (int it = 0; it < 10; it++) {
                 // r = e_1 - A x (FP64)
                 for (int i = lane; i < n; i += 32) {
                     double s = (i == 0) ? 1.0 : 0.0;
@@ -252,7 +252,11 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
                 dm = warp_max(dm);
                 xmax = warp_max(xm);
                 if (!(dm == dm) || !(xmax == xmax)) break;  // NaN
-                if (dm <= 1e-15 * xmax) { conv = true; break; }
+                // converged: the correction is at the level FP64 residuals can
+                // resolve (~cond(SA) * eps), or it stopped shrinking there
+                if (dm <= 2e-14 * xmax) { conv = true; break; }
+                if (it >= 2 && dm <= 1e-12 * xmax && dm > 0.5 * dprev) { conv = true; break; }
+                dprev = dm;
             }
         }
         if (!conv) {

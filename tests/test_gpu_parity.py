@@ -1,0 +1,182 @@
+"""CUDA path (through the C ABI) against the FP64 oracle on the same seeded
+inputs.
+
+Stated tolerances (FP32 ray integration with an FP32 Voronoi walk, FP32 LU +
+FP64 refinement for the SE):
+  J^0_0       per (node, line) relative error: max 2e-4, 99.9th pct 2e-6,
+              median 2e-7
+  J^2_0       per (node, line) |dJ^2_0| / J^0_0: max 5e-5
+  rho (same J) relative 1e-10 (FP64 solve quality)
+  rho (chain)  rho^0_0 relative 2e-4, |d rho^2_0| / rho^0_0 2e-5
+  segments    equal to 1e-4 (near-degenerate Voronoi crossings may differ)
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+J0_MAX, J0_P999, J0_MED, J2_MAX = 2e-4, 2e-6, 2e-7, 5e-5
+
+
+@pytest.fixture(scope="module")
+def ctx(built_lib):
+    import portal_gb300 as pg
+    c = pg.Context(0)
+    yield c
+    c.close()
+
+
+def _rf(ctx, cloud, mol, rc):
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    return ctx.radiation_field(rc)
+
+
+def _check_J(J0, J2, oJ0, oJ2, mask=None):
+    if mask is not None:
+        J0, J2, oJ0, oJ2 = J0[mask], J2[mask], oJ0[mask], oJ2[mask]
+    r0 = np.abs(J0 - oJ0) / np.abs(oJ0)
+    r2 = np.abs(J2 - oJ2) / np.abs(oJ0)
+    assert np.isfinite(J0).all() and np.isfinite(J2).all()
+    assert r0.max() < J0_MAX, r0.max()
+    assert np.quantile(r0, 0.999) < J0_P999, np.quantile(r0, 0.999)
+    assert np.median(r0) < J0_MED, np.median(r0)
+    assert r2.max() < J2_MAX, r2.max()
+
+
+def test_radiation_field_cfg1(ctx, cfg1, cfg1_oracle):
+    cloud, mol, rc = cfg1
+    J0, J2, st, nseg = _rf(ctx, cloud, mol, rc)
+    assert not st.any()
+    assert abs(nseg - cfg1_oracle["nseg"]) <= 1e-4 * cfg1_oracle["nseg"]
+    _check_J(J0, J2, cfg1_oracle["J0"], cfg1_oracle["J2"])
+
+
+def test_solve_se_same_J_cfg1(ctx, cfg1, cfg1_oracle):
+    import portal_gb300 as pg
+    cloud, mol, rc = cfg1
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    pops, st = ctx.solve_se(rc.kmax, cfg1_oracle["J0"], cfg1_oracle["J2"])
+    assert not (st & pg.NODE_SINGULAR).any()
+    opp = cfg1_oracle["P"].solve_se(rc.kmax, cfg1_oracle["J0"], cfg1_oracle["J2"])[0]
+    scale = np.abs(opp[:, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pops[:, 0::2] - opp[:, 0::2]) / np.abs(opp[:, 0::2])).max() < 1e-10
+    assert (np.abs(pops[:, 1::2] - opp[:, 1::2]) / scale).max() < 1e-10
+    g = np.sqrt(2 * mol.j_lev + 1)
+    np.testing.assert_allclose((pops[:, 0::2] * g).sum(1), 1.0, rtol=1e-12)
+
+
+def test_node_loop_chain_cfg1(ctx, cfg1, cfg1_oracle):
+    """Device-resident chain radiation field -> SE against oracle -> oracle."""
+    cloud, mol, rc = cfg1
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    ctx.radiation_field(rc, fetch=False)
+    pops, st = ctx.solve_se(rc.kmax)
+    opp = cfg1_oracle["pops"]
+    assert (np.abs(pops[:, 0::2] - opp[:, 0::2]) / np.abs(opp[:, 0::2])).max() < 2e-4
+    scale = np.abs(opp[:, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pops[:, 1::2] - opp[:, 1::2]) / scale).max() < 2e-5
+
+
+def test_deterministic(ctx, cfg1):
+    cloud, mol, rc = cfg1
+    a = _rf(ctx, cloud, mol, rc)
+    b = ctx.radiation_field(rc)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[3] == b[3]
+
+
+def _small(n=2048, nlev=5, seed=5, **kw):
+    from portal_gb300 import synth
+    mol = synth.linear_rotor(nlev)
+    cloud = synth.power_law_sphere(n, seed, mol, **kw)
+    rc = synth.RunConfig(nth=8, nph=8, nvel=16, kmax=6, gvec=synth.gauge_vector(seed))
+    return cloud, mol, rc
+
+
+def test_n_depth_overflow_is_reported(ctx):
+    import portal_gb300 as pg
+    cloud, mol, rc = _small()
+    rc.n_depth = 3
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    with pytest.raises(pg.PortalError) as e:
+        ctx.radiation_field(rc)
+    assert e.value.code == -4
+
+
+def test_skipped_and_surface_nodes(ctx):
+    """ab_all <= 0 nodes (main_para.f90:213) and nodes beyond bulk_node_num
+    get J = 0 and pol_pops = 0, as in the reference."""
+    import oracle
+    cloud, mol, rc = _small()
+    cloud.ab_all[[3, 10, 77]] = 0.0
+    cloud.bulk_node_num = cloud.node_num - 100
+    J0, J2, st, _ = _rf(ctx, cloud, mol, rc)
+    pops, _ = ctx.solve_se(rc.kmax)
+    for n in (3, 10, 77):
+        assert (J0[n] == 0).all() and (pops[n] == 0).all()
+    assert (J0[cloud.bulk_node_num:] == 0).all() and (pops[cloud.bulk_node_num:] == 0).all()
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc, 1, 200)
+    m = np.ones(200, bool); m[[3, 10, 77]] = False
+    _check_J(J0[:200], J2[:200], oJ0[:200], oJ2[:200], mask=m)
+
+
+def test_neighbour_lists_longer_than_a_warp(ctx):
+    """Padding every neighbour list with non-adjacent nodes (beyond 32
+    entries) leaves the Voronoi walk unchanged: the padded faces are never the
+    nearest exit.  Checked against the oracle on the same padded lists."""
+    import oracle
+    cloud, mol, rc = _small(1024)
+    N = cloud.node_num
+    rng = np.random.default_rng(1)
+    off, idx = cloud.nb_off, cloud.nb_idx
+    new_off, new_idx = [0], []
+    for i in range(N):
+        own = set(idx[off[i]:off[i + 1]].tolist()) | {i}
+        extra = [int(x) for x in rng.choice(N, 40, replace=False) if int(x) not in own][:24]
+        lst = sorted(set(idx[off[i]:off[i + 1]].tolist()) | set(extra))
+        new_idx += lst
+        new_off.append(len(new_idx))
+    cloud.nb_off = np.array(new_off, dtype=np.int64)
+    cloud.nb_idx = np.array(new_idx, dtype=np.int32)
+    assert np.diff(cloud.nb_off).max() > 32
+    J0, J2, st, nseg = _rf(ctx, cloud, mol, rc)
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, onseg, _ = P.radiation_field(rc, 1, 128)
+    _check_J(J0[:128], J2[:128], oJ0[:128], oJ2[:128])
+
+
+def test_dust_path(ctx):
+    """Dust on (gas-to-dust ratio set): the dust branch of ray_in
+    (inverse_rt.f90:298-311) against the oracle."""
+    import oracle
+    from portal_gb300 import synth
+    cloud, mol, rc = _small(1024)
+    cloud.dust_p[:] = cloud.h2_dens * synth.F4(2.32e-27) / 100.0
+    J0, J2, st, _ = _rf(ctx, cloud, mol, rc)
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc, 1, 128)
+    _check_J(J0[:128], J2[:128], oJ0[:128], oJ2[:128])
+
+
+def test_cfg2_shape_subset():
+    """The 10-level / 24x24 / 129-channel shape on a 16,384-point cloud:
+    first 64 nodes against the oracle."""
+    import oracle
+    import portal_gb300 as pg
+    from portal_gb300 import synth
+    cloud, mol, rc = synth.config_cloud("cfg2", n_points=16384)
+    with pg.Context(0) as c:
+        c.set_molecule(mol)
+        c.set_cloud(cloud)
+        J0, J2, st, nseg = c.radiation_field(rc)
+        pops, st2 = c.solve_se(rc.kmax)
+    assert not st.any()
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc, 1, 64)
+    _check_J(J0[:64], J2[:64], oJ0[:64], oJ2[:64])
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2, 1, 64)
+    assert (np.abs(pops[:64, 0::2] - opp[:64, 0::2]) / np.abs(opp[:64, 0::2])).max() < 2e-4
