@@ -136,10 +136,12 @@ def cpu_port_rate(cloud, mol, rc, target_s, repeats=1):
     import oracle
     P = oracle.OracleProblem(cloud, mol)
     nthreads = os.cpu_count() or 1
+    # calibration: 2 nodes per thread; per_node = wall time per node at full
+    # thread count
     t = time.perf_counter()
-    _, _, _, nseg, _ = P.radiation_field(rc, 1, nthreads, nthreads)
-    per_node = (time.perf_counter() - t) / nthreads
-    n = sample_nodes_for(target_s, per_node / nthreads, cloud.bulk_node_num)
+    _, _, _, nseg, _ = P.radiation_field(rc, 1, 2 * nthreads, nthreads)
+    per_node = (time.perf_counter() - t) / (2 * nthreads)
+    n = sample_nodes_for(target_s, per_node, cloud.bulk_node_num)
     rates = []
     for r in range(repeats):
         lo = 1 + (r * n) % max(1, cloud.bulk_node_num - n)
@@ -151,15 +153,17 @@ def cpu_port_rate(cloud, mol, rc, target_s, repeats=1):
     return rates, nthreads
 
 
-def build_workload(n_points):
+def build_workload(n_points, n_depth=10000):
     from portal_gb300 import synth
-    return synth.config_cloud("cfg2", n_points=n_points)
+    cloud, mol, rc = synth.config_cloud("cfg2", n_points=n_points)
+    rc.n_depth = n_depth
+    return cloud, mol, rc
 
 
 def reference_arm(args, rank, world):
     if rank != 0:
         return 0
-    cloud, mol, rc = build_workload(args.points)
+    cloud, mol, rc = build_workload(args.points, args.n_depth)
     cfg = workload_config(cloud, mol, rc, cloud.node_num)
     for _ in range(args.warmup):
         pass  # the CPU port has no warm-up state; each step is cold by construction
@@ -189,7 +193,7 @@ def gpu_arm(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    cloud, mol, rc = build_workload(args.points)
+    cloud, mol, rc = build_workload(args.points, args.n_depth)
     N, nlev = cloud.node_num, mol.nlev
     stream = torch.cuda.Stream()
     ctx = pg.Context(local_rank)
@@ -325,6 +329,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-depth", type=int, default=10000,
+                    help="walk length limit (main_portal.x's n_depth); smaller values shrink the walk scratch")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))

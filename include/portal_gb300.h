@@ -124,6 +124,31 @@ int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const do
 int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J2,
                     double *pol_pops, double *rates, double *JJ_20, int *status);
 
+/* Stokes image of one inclination: the pixel mode of finish_portal.x
+ * (para_finish.f90:352-448) -- rotate_all_save (miscellaneous.f90:844-907),
+ * the population read-back (para_finish.f90:222-240), comp_emcoefs
+ * (em_coefs.f90:1-113) per bulk node and line, trace_out_raytrace
+ * (raytrace.f90:58-177) per pixel and ray_in_raytrace (:179-323) per pixel,
+ * line and channel.  star_mod = 0 only.
+ *   pol_pops(N, 2*nlev) as main_portal.x wrote it, or NULL for the
+ *   device-resident result of portal_solve_se;
+ *   lines l1(nlines), l2(nlines) 1-based levels (at most 16 lines; as in
+ *   the reference every line takes the frequency of the last pair,
+ *   para_finish.f90:173-175); th_inc, ph_az inclination and azimuth
+ *   (radians); channels v = i*dvel + v0, i = -nvel..nvel; pixels
+ *   (2*im_pix+1)^2 over +-im_size (< 1/sqrt(2), so that every start point
+ *   lies inside the unit sphere); alpha the dust polarisation efficiency
+ *   (0.15 in para_finish.f90:78); dx the march step (REAL*4 1E-4 there).
+ * Outputs (any may be NULL), each (2*im_pix+1, 2*im_pix+1, 2*nvel+1,
+ * nlines) column-major, unscaled intensities (para_finish.f90 multiplies
+ * I, Q, U by I_to_T = 3.255e39/nu0^2 when it writes them): I, Q, U, tau
+ * and the dust I, Q, U, tau; status(pixels) 0 or PORTAL_NODE_DEPTH. */
+int portal_image(portal_ctx *ctx, const double *pol_pops, int nlines, const int *l1, const int *l2,
+                 double th_inc, double ph_az, int nvel, double dvel, double v0, int im_pix,
+                 double im_size, double alpha, double dx, int n_depth_rt, float *I, float *Q,
+                 float *U, float *tau, float *dust_I, float *dust_Q, float *dust_U,
+                 float *dust_tau, int *status);
+
 /* Run this context's work on the caller's CUDA stream (a cudaStream_t
  * passed as void*), or on the context's own stream when NULL.  Lets a caller
  * order the library's kernels with its own work and time them with its own

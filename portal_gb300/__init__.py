@@ -30,7 +30,8 @@ KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_w
 EXPORTS = (
     "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
     "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
-    "portal_radiation_field", "portal_solve_se", "portal_last_kernel_times", "portal_set_stream",
+    "portal_radiation_field", "portal_solve_se", "portal_image", "portal_last_kernel_times",
+    "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
 )
 
@@ -67,6 +68,9 @@ def lib() -> C.CDLL:
     L.portal_solve_se.argtypes = [C.c_void_p, C.c_int, P_D, P_D, P_D, P_D, P_D, P_I]
     L.portal_last_kernel_times.argtypes = [C.c_void_p, P_D, P_I, C.c_int]
     L.portal_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    P_F = C.POINTER(C.c_float)
+    L.portal_image.argtypes = [C.c_void_p, P_D, C.c_int, P_I, P_I, C.c_double, C.c_double, C.c_int, C.c_double,
+                               C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int] + [P_F] * 8 + [P_I]
     L.portal_wigner3j.restype = C.c_double
     L.portal_wigner3j.argtypes = [C.c_int] * 6
     L.portal_wigner6j.restype = C.c_double
@@ -191,6 +195,25 @@ class Context:
         if jj20:
             out = out + (jj.T.copy(),)
         return out
+
+    def image(self, l1, l2, th_inc, ph_az, nvel, dvel, v0, im_pix, im_size, alpha=0.15,
+              dx=float(np.float32(1e-4)), n_depth_rt=10000, pol_pops=None, quantities=8):
+        """Stokes cubes of one inclination.  Returns an (8, nlines, nchan,
+        npx(y), npx(x)) float32 array (I, Q, U, tau, dust I, Q, U, tau; the
+        memory of eight Fortran (npx, npx, nchan, nlines) arrays) and the
+        per-pixel status.  pol_pops: (N, 2*nlev) or None for the result of the
+        last solve_se."""
+        l1 = _i32(l1); l2 = _i32(l2)
+        nl, npx, nch = len(l1), 2 * im_pix + 1, 2 * nvel + 1
+        out = np.zeros((8, nl, nch, npx, npx), dtype=np.float32)
+        st = np.zeros(npx * npx, dtype=np.int32)
+        pp = None if pol_pops is None else np.ascontiguousarray(np.asarray(pol_pops, dtype=np.float64).T)
+        P_F = C.POINTER(C.c_float)
+        ptrs = [out[q].ctypes.data_as(P_F) if q < quantities else None for q in range(8)]
+        self._check(lib().portal_image(self._h, _p(pp), nl, _p(l1, P_I), _p(l2, P_I), float(th_inc), float(ph_az),
+                                       nvel, float(dvel), float(v0), im_pix, float(im_size), float(alpha), float(dx),
+                                       n_depth_rt, *ptrs, _p(st, P_I)))
+        return out, st
 
     def set_stream(self, stream_ptr: int | None):
         """Run on a caller-owned cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""

@@ -64,6 +64,7 @@ struct portal_ctx {
     double tx = 0.0;
     portal::DevBuf<double> pos64;     // (3,N) FP64 positions
     portal::DevBuf<double> bvec64;    // (3,N)
+    portal::DevBuf<double> vel64;     // (3,N) FP64 velocities (image rotation)
     portal::DevBuf<float4> cellv;     // (vx,vy,vz,b) per node
     portal::DevBuf<int> nb_off;       // N+1
     portal::DevBuf<int> nb_idx;       // nnz, 0-based

@@ -219,19 +219,18 @@ extern "C" int portal_set_cloud(portal_ctx *c, int N, int bulk, int nlev, const 
     PCHECK(c, cudaMemcpyAsync(c->nb_off.p, off.data(), (N + 1) * sizeof(int),
                               cudaMemcpyHostToDevice, c->stream));
     DevBuf<int> dne;
-    DevBuf<double> dvel;
-    if (dne.reserve((size_t)N * maxne) || dvel.reserve(3 * (size_t)N))
+    if (dne.reserve((size_t)N * maxne) || c->vel64.reserve(3 * (size_t)N))
         return set_err(c, PORTAL_ERR_NOMEM, "portal_set_cloud: staging allocation failed");
     PCHECK(c, cudaMemcpyAsync(dne.p, del_ne, (size_t)N * maxne * sizeof(int),
                               cudaMemcpyHostToDevice, c->stream));
-    PCHECK(c, cudaMemcpyAsync(dvel.p, vel_all, 3 * (size_t)N * sizeof(double),
+    PCHECK(c, cudaMemcpyAsync(c->vel64.p, vel_all, 3 * (size_t)N * sizeof(double),
                               cudaMemcpyHostToDevice, c->stream));
     long long tot = (long long)N * maxne;
     k_build_edges<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(N, maxne, dne.p, c->nb_off.p,
                                                                       c->pos64.p, c->nb_idx.p,
                                                                       c->edge.p);
     PCHECK(c, cudaGetLastError());
-    k_cellv<<<(N + 255) / 256, 256, 0, c->stream>>>(N, dvel.p, c->b64.p, c->cellv.p);
+    k_cellv<<<(N + 255) / 256, 256, 0, c->stream>>>(N, c->vel64.p, c->b64.p, c->cellv.p);
     PCHECK(c, cudaGetLastError());
     PCHECK(c, cudaStreamSynchronize(c->stream));  // staging buffers die at scope end
     c->N = N; c->bulk = bulk; c->nnz = nnz; c->maxdeg = maxdeg; c->tx = tx;
