@@ -149,6 +149,45 @@ int portal_image(portal_ctx *ctx, const double *pol_pops, int nlines, const int 
                  float *U, float *tau, float *dust_I, float *dust_Q, float *dust_U,
                  float *dust_tau, int *status);
 
+/* Radiation field for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference.  It serves callers that must not call
+ * cudaMalloc: a host whose device memory is owned by its own pool (e.g. CUDA
+ * Fortran device arrays, a framework that hands out pre-sized buffers), or
+ * code that may not allocate between simulation steps.  It computes what
+ * portal_radiation_field computes, needs no context, and allocates nothing:
+ *   - every input is a DEVICE pointer to the reference-layout array that
+ *     portal_set_cloud takes from the host (xyz(3,N), vel_all(3,N), b_all(N),
+ *     temp_all(2,N), dust_p(N), ab_all(N), lev_p(nlev,N), bvec_all(3,N),
+ *     del_ne(N,maxne), del_num_ne(N)); the molecule's line data
+ *     (j_lev, r_trans(2,r_num), t_Aji, nu, t_Bij, kd_v) and gvec are HOST
+ *     pointers;
+ *   - J0(r_num,N), J2(r_num,N) and status(N) (or NULL) are DEVICE outputs;
+ *   - its only scratch is a fixed 64 MiB array inside the library image,
+ *     held on every GPU that loads the library until the process exits.
+ * The call is asynchronous on cuda_stream (a cudaStream_t, NULL = legacy
+ * default stream): synchronise before reading the outputs.  Every call
+ * shares the one scratch array (and the line constants), so calls that
+ * overlap on the GPU race; serialise them.  The first call on each device
+ * looks up the scratch array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.
+ * Limits (PORTAL_ERR_ARG beyond them; portal_radiation_field_static_limits
+ * reports them): n_depth <= 857 cells per ray, r_num <= 64 lines,
+ * 2*nvel+1 <= 288 channels, nth*nph <= 8192 directions.  Walk overflow is
+ * reported per node in status (PORTAL_NODE_DEPTH) with J = 0 there. */
+int portal_radiation_field_static(void *cuda_stream, int node_num, int bulk_node_num, int nlev,
+                                  const double *xyz, const double *vel_all, const double *b_all,
+                                  const double *temp_all, const double *dust_p, const double *ab_all,
+                                  const double *lev_p, const double *bvec_all, int maxne,
+                                  const int *del_ne, const int *del_num_ne, double tx,
+                                  const int *j_lev, int r_num, const int *r_trans,
+                                  const double *t_Aji, const double *nu, const double *t_Bij,
+                                  const double *kd_v, int nth, int nph, int nvel, const double *gvec,
+                                  double dx, int n_depth, double *J0, double *J2, int *status);
+/* The size limits of portal_radiation_field_static (any pointer may be NULL). */
+void portal_radiation_field_static_limits(int *max_n_depth, int *max_lines, int *max_channels,
+                                          int *max_directions, long long *scratch_bytes);
+
 /* Run this context's work on the caller's CUDA stream (a cudaStream_t
  * passed as void*), or on the context's own stream when NULL.  Lets a caller
  * order the library's kernels with its own work and time them with its own

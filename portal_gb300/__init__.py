@@ -33,6 +33,7 @@ EXPORTS = (
     "portal_radiation_field", "portal_solve_se", "portal_image", "portal_last_kernel_times",
     "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
+    "portal_radiation_field_static", "portal_radiation_field_static_limits",
 )
 
 _lib = None
@@ -77,6 +78,13 @@ def lib() -> C.CDLL:
     L.portal_wigner6j.argtypes = [C.c_int] * 6
     L.portal_coupling_constant.restype = None
     L.portal_coupling_constant.argtypes = [C.c_int] * 5 + [P_D, P_D]
+    # the allocation-free entry point takes raw device addresses
+    V = C.c_void_p
+    L.portal_radiation_field_static.argtypes = (
+        [V, C.c_int, C.c_int, C.c_int] + [V] * 8 + [C.c_int, V, V, C.c_double] +
+        [P_I, C.c_int, P_I, P_D, P_D, P_D, P_D, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int] + [V] * 3)
+    L.portal_radiation_field_static_limits.restype = None
+    L.portal_radiation_field_static_limits.argtypes = [P_I, P_I, P_I, P_I, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
