@@ -124,6 +124,24 @@ int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const do
 int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J2,
                     double *pol_pops, double *rates, double *JJ_20, int *status);
 
+/* Lambda iteration of the node loop: repeat portal_radiation_field +
+ * portal_solve_se, setting the level populations of every bulk node from
+ * the SE solution between passes, n_J = n_mol sqrt(2J+1) rho^0_0(J)
+ * (em_coefs.f90:91-94 with the normalisation em_coefs.f90:158-164), until the
+ * largest relative change of rho^0_0 over nodes and levels is below tol, or
+ * max_iter passes.  The reference makes exactly one pass
+ * (main_para.f90:210-257); iteration 1 from the cloud's populations is that
+ * pass.  start_pops(N, 2*nlev) (pol_pops layout) replaces the starting
+ * populations of the bulk nodes by those of its rho^0_0 (a warm start), or
+ * NULL to start from the cloud's.  Outputs (any may be NULL): the last
+ * pol_pops(N, 2*nlev), the final lev_p(nlev, N) (they also become the
+ * context's populations), the number of passes, residuals(max_iter) per
+ * pass, and the total ray segments walked. */
+int portal_lambda_iterate(portal_ctx *ctx, int nth, int nph, int nvel, const double *gvec, double dx,
+                          int n_depth, int kmax, double tol, int max_iter, const double *start_pops,
+                          double *pol_pops, double *lev_p_out, int *iterations, double *residuals,
+                          long long *n_segments);
+
 /* Stokes image of one inclination: the pixel mode of finish_portal.x
  * (para_finish.f90:352-448) -- rotate_all_save (miscellaneous.f90:844-907),
  * the population read-back (para_finish.f90:222-240), comp_emcoefs

@@ -83,7 +83,8 @@ class OracleProblem:
         self.dust_p = np.ascontiguousarray(cloud.dust_p, dtype=np.float64)
         self.h2 = np.ascontiguousarray(cloud.h2_dens, dtype=np.float64)
         self.ab = np.ascontiguousarray(cloud.ab_all, dtype=np.float64)
-        self.lev_p = np.ascontiguousarray(cloud.lev_p, dtype=np.float64)      # (N,nlev) == lev_p(nlev,N)
+        # own copy: callers iterate the oracle by updating this array in place
+        self.lev_p = np.array(cloud.lev_p, dtype=np.float64, order="C", copy=True)  # == lev_p(nlev,N)
         self.bvec = np.ascontiguousarray(cloud.bvec, dtype=np.float64)
         self.del_ne = np.ascontiguousarray(cloud.del_ne(), dtype=np.int32)    # (maxne,N) == del_ne(N,maxne)
         self.del_num_ne = np.ascontiguousarray(cloud.del_num_ne(), dtype=np.int32)

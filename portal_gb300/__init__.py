@@ -34,6 +34,7 @@ EXPORTS = (
     "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
     "portal_radiation_field_static", "portal_radiation_field_static_limits",
+    "portal_lambda_iterate",
 )
 
 _lib = None
@@ -83,6 +84,8 @@ def lib() -> C.CDLL:
     L.portal_radiation_field_static.argtypes = (
         [V, C.c_int, C.c_int, C.c_int] + [V] * 8 + [C.c_int, V, V, C.c_double] +
         [P_I, C.c_int, P_I, P_D, P_D, P_D, P_D, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int] + [V] * 3)
+    L.portal_lambda_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int, C.c_int,
+                                        C.c_double, C.c_int, P_D, P_D, P_D, P_I, P_D, C.POINTER(C.c_longlong)]
     L.portal_radiation_field_static_limits.restype = None
     L.portal_radiation_field_static_limits.argtypes = [P_I, P_I, P_I, P_I, C.POINTER(C.c_longlong)]
     _lib = L
@@ -222,6 +225,22 @@ class Context:
                                        nvel, float(dvel), float(v0), im_pix, float(im_size), float(alpha), float(dx),
                                        n_depth_rt, *ptrs, _p(st, P_I)))
         return out, st
+
+    def lambda_iterate(self, rc, tol=1e-6, max_iter=100, start_pops=None, fetch=True):
+        """Plain Lambda iteration.  Returns (pol_pops (N, 2 nlev), lev_p
+        (N, nlev), passes, residual per pass, segments)."""
+        pp = np.zeros((2 * self.nlev, self.N)) if fetch else None
+        lp = np.zeros((self.N, self.nlev)) if fetch else None
+        res = np.zeros(max_iter)
+        it = C.c_int(0)
+        nseg = C.c_longlong(0)
+        sp = None if start_pops is None else np.ascontiguousarray(np.asarray(start_pops, dtype=np.float64).T)
+        g = _f64(rc.gvec)
+        self._check(lib().portal_lambda_iterate(self._h, rc.nth, rc.nph, rc.nvel, _p(g), float(rc.dx), rc.n_depth,
+                                                rc.kmax, float(tol), int(max_iter), _p(sp), _p(pp), _p(lp),
+                                                C.byref(it), _p(res), C.byref(nseg)))
+        n = it.value
+        return (None if pp is None else pp.T.copy()), lp, n, res[:n].copy(), int(nseg.value)
 
     def set_stream(self, stream_ptr: int | None):
         """Run on a caller-owned cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""

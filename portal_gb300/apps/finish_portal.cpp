@@ -1,0 +1,124 @@
+// finish_portal.x on GB300: the same command line, input file and outputs as
+// the reference program (para_finish.f90), pixel mode, with the pixel loops
+// (para_finish.f90:382-448) run by the library.
+//
+//   finish_portal.x <input_file> <output_map> <pop> <grid> <mol> <dust>
+//
+// Reads <output_map>/pol_pops.dat (para_finish.f90:222-240) and writes, per
+// line i and inclination j, inc{j}-trans{i}-im_{i,q,u,tau}.fits and the
+// centre-channel dust maps inc{j}-trans{i}-dust_{i,q,u,tau}.fits
+// (para_finish.f90:460-616), I, Q and U scaled by I_to_T = 3.255e39/nu0^2.
+// With fits = 0 the .dat maps of the same routine are written instead.
+// PORTAL_BVEC_FILE and PORTAL_DEVICE as for main_portal.x.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "portal_gb300.h"
+#include "portal_io.h"
+
+using namespace portal_io;
+
+static int fail(const std::string &m) {
+    fprintf(stderr, "finish_portal: %s\n", m.c_str());
+    return 1;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 7)
+        return fail("usage: finish_portal.x <input_file> <output_map> <pop> <grid> <mol> <dust>");
+    const std::string input = argv[1], out = argv[2], pop = argv[3], grid = argv[4], mol = argv[5],
+                      dust = argv[6];
+    std::string err;
+    FinishInput in;
+    if (!read_finish_input(input, in, err)) return fail(err);
+    if (in.star_mod == 1) return fail("star mode (star_mod = 1) is not supported");
+    if (in.pix != 1) return fail("only the pixel mode (pix_mod = 1) is supported");
+    Molecule m;
+    Cloud c;
+    if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err)) return fail(err);
+    std::vector<double> bvec;
+    if (const char *bf = getenv("PORTAL_BVEC_FILE")) {
+        std::vector<double> rows;
+        if (!read_rows(bf, rows, c.node_num, 3, err)) return fail(err);
+        bvec.resize(3 * (size_t)c.node_num);
+        for (int i = 0; i < c.node_num; i++)
+            for (int k = 0; k < 3; k++) bvec[3 * (size_t)i + k] = rows[(size_t)i + (size_t)c.node_num * k];
+    } else {
+        magfield(c, in.x1, in.x2, in.x3, in.x_dip, bvec);
+    }
+    const int N = c.node_num, nlev = m.nlev;
+    std::vector<double> pops;
+    if (!read_rows(out + "/pol_pops.dat", pops, N, 2 * nlev, err)) return fail(err);
+    const int dev = getenv("PORTAL_DEVICE") ? atoi(getenv("PORTAL_DEVICE")) : 0;
+    portal_ctx *ctx = nullptr;
+    if (portal_create(&ctx, dev)) return fail(std::string("portal_create: ") + portal_last_error(nullptr));
+    auto chk = [&](int r, const char *what) {
+        if (r) {
+            fprintf(stderr, "finish_portal: %s: %s (%s)\n", what, portal_strerror(r), portal_last_error(ctx));
+            portal_destroy(ctx);
+            exit(1);
+        }
+    };
+    chk(portal_set_molecule(ctx, m.nlev, m.j_lev.data(), m.e_levs.data(), m.r_num, m.r_trans.data(),
+                            m.A.data(), m.nu.data(), m.Bij.data(), m.kd_v.data(), m.c_num, m.c_trans.data(),
+                            m.c_temp, m.c_par, m.col_temps.data(), m.C.data()),
+        "portal_set_molecule");
+    chk(portal_set_cloud(ctx, N, c.bulk_node_num, nlev, c.xyz.data(), c.vel.data(), c.b_all.data(),
+                         c.temp_all.data(), c.dust_p.data(), c.h2_dens.data(), c.ab_all.data(), c.lev_p.data(),
+                         bvec.data(), c.maxne, c.del_ne.data(), c.del_num_ne.data(), c.tx),
+        "portal_set_cloud");
+    const int npx = 2 * in.im_pix + 1, nch = 2 * in.nvel + 1, nl = in.nlevels;
+    const size_t cube = (size_t)npx * npx * nch * nl;
+    std::vector<float> q[8];
+    for (auto &v : q) v.assign(cube, 0.f);
+    // every line takes the frequency of the last (l1, l2) pair (para_finish.f90:173-175)
+    const double nu0 = m.e_levs[in.l2[nl - 1] - 1] - m.e_levs[in.l1[nl - 1] - 1];
+    const double I_to_T = 3.255e39 / (nu0 * nu0);
+    const double pi = std::acos(-1.0);
+    const double ang = -180.0 * std::asin(2.0 * in.im_size * c.tx / in.distance) / (pi * (in.im_pix * 2 + 1));
+    const double dx = (double)1e-4f;  // para_finish.f90:201
+    for (int j = 0; j < in.nincs; j++) {
+        chk(portal_image(ctx, pops.data(), nl, in.l1.data(), in.l2.data(), in.th_inc[j], in.ph_az[j], in.nvel,
+                         in.dvel, in.v0, in.im_pix, in.im_size, 0.15, dx, in.n_depth_rt, q[0].data(), q[1].data(),
+                         q[2].data(), q[3].data(), q[4].data(), q[5].data(), q[6].data(), q[7].data(), nullptr),
+            "portal_image");
+        for (int i = 0; i < nl; i++) {
+            const char *names[8] = {"im_i", "im_q", "im_u", "im_tau", "dust_i", "dust_q", "dust_u", "dust_tau"};
+            for (int k = 0; k < 8; k++) {
+                const bool dustmap = k >= 4;
+                const bool scale = (k % 4) != 3;
+                const int nv = dustmap ? 1 : nch;
+                std::vector<float> a((size_t)npx * npx * nv);
+                for (int c3 = 0; c3 < nv; c3++) {
+                    const int ch = dustmap ? in.nvel : c3;  // dust: centre channel only
+                    for (size_t p = 0; p < (size_t)npx * npx; p++) {
+                        const double v = q[k][p + (size_t)npx * npx * (ch + (size_t)nch * i)];
+                        a[p + (size_t)npx * npx * c3] = (float)(scale ? I_to_T * v : v);
+                    }
+                }
+                char name[160];
+                if (in.fits == 1) {
+                    snprintf(name, sizeof name, "%s/inc%02d-trans%02d-%s.fits", out.c_str(), j + 1, i + 1, names[k]);
+                    if (!write_fits(name, a.data(), npx, nv, (float)nu0, (float)ang, (float)(in.im_pix + 1),
+                                    (float)(-ang), (float)(in.im_pix + 1), (float)in.dvel, (float)(in.nvel + 1),
+                                    0.f, 0.f, 0.f))
+                        return fail(std::string("cannot write ") + name);
+                } else {
+                    for (int c3 = 0; c3 < nv; c3++) {
+                        snprintf(name, sizeof name, "%s/inc%02d-trans%02d-vel%02d-%s.dat", out.c_str(), j + 1, i + 1,
+                                 c3 + 1, names[k]);
+                        std::vector<double> rows((size_t)npx * npx);
+                        for (size_t p = 0; p < rows.size(); p++) rows[p] = a[p + (size_t)npx * npx * c3];
+                        if (!write_rows(name, rows, npx, npx)) return fail(std::string("cannot write ") + name);
+                    }
+                }
+            }
+        }
+    }
+    portal_destroy(ctx);
+    printf("finish_portal: %d inclinations, %d lines, %dx%d pixels, %d channels\n", in.nincs, nl, npx, npx, nch);
+    return 0;
+}

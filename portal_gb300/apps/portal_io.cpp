@@ -1,0 +1,512 @@
+// Readers and writers of PORTAL's files.  Each reader mirrors the read
+// statements of the reference routine named beside it.
+#include "portal_io.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <random>
+#include <sstream>
+
+namespace portal_io {
+
+static double f4(double x) { return (double)(float)x; }  // REAL*4 literal promoted to FP64
+
+// ---------------------------------------------------------------------------
+// list-directed input
+// ---------------------------------------------------------------------------
+
+ListReader::ListReader(const std::string &path) : path_(path) {
+    std::ifstream f(path);
+    if (!f) return;
+    std::string l;
+    while (std::getline(f, l)) {
+        if (!l.empty() && l.back() == '\r') l.pop_back();
+        lines_.push_back(l);
+    }
+    ok_ = true;
+}
+
+static void tokenize(const std::string &line, std::vector<std::string> &toks) {
+    toks.clear();
+    std::string cur;
+    auto flush = [&]() {
+        if (cur.empty()) return;
+        // r*c repeat count
+        size_t star = cur.find('*');
+        if (star != std::string::npos && star > 0 &&
+            std::all_of(cur.begin(), cur.begin() + star, [](char ch) { return ch >= '0' && ch <= '9'; })) {
+            int r = atoi(cur.substr(0, star).c_str());
+            std::string v = cur.substr(star + 1);
+            for (int i = 0; i < r; i++) toks.push_back(v);
+        } else {
+            toks.push_back(cur);
+        }
+        cur.clear();
+    };
+    bool quote = false;
+    char qc = 0;
+    for (char ch : line) {
+        if (quote) {
+            if (ch == qc) { quote = false; flush(); }
+            else cur.push_back(ch);
+            continue;
+        }
+        if (ch == '\'' || ch == '"') { flush(); quote = true; qc = ch; continue; }
+        if (ch == '/') { flush(); toks.push_back("/"); break; }  // value separator that ends the list
+        if (ch == ' ' || ch == '\t' || ch == ',') { flush(); continue; }
+        cur.push_back(ch);
+    }
+    flush();
+}
+
+bool ListReader::next_record() {
+    if (line_ >= lines_.size()) return false;
+    tokenize(lines_[line_++], toks_);
+    pos_ = 0;
+    return true;
+}
+
+bool ListReader::skip() { return next_record(); }
+
+bool ListReader::read(std::vector<std::string> &out, size_t n) {
+    out.clear();
+    if (!next_record()) return false;
+    while (out.size() < n) {
+        if (pos_ >= toks_.size()) {
+            if (!next_record()) return false;
+            continue;
+        }
+        if (toks_[pos_] == "/") return false;  // the reference would leave the rest unset
+        out.push_back(toks_[pos_++]);
+    }
+    return true;
+}
+
+double to_double(const std::string &tok) {
+    std::string t = tok;
+    for (auto &ch : t)
+        if (ch == 'd' || ch == 'D') ch = 'e';
+    return strtod(t.c_str(), nullptr);
+}
+
+int to_int(const std::string &tok) { return (int)strtol(tok.c_str(), nullptr, 10); }
+
+bool ListReader::read_doubles(std::vector<double> &out, size_t n) {
+    std::vector<std::string> t;
+    if (!read(t, n)) return false;
+    out.resize(n);
+    for (size_t i = 0; i < n; i++) out[i] = to_double(t[i]);
+    return true;
+}
+
+bool ListReader::read_ints(std::vector<int> &out, size_t n) {
+    std::vector<std::string> t;
+    if (!read(t, n)) return false;
+    out.resize(n);
+    for (size_t i = 0; i < n; i++) out[i] = to_int(t[i]);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// input files
+// ---------------------------------------------------------------------------
+
+bool read_main_input(const std::string &path, MainInput &in, std::string &err) {
+    ListReader r(path);
+    if (!r.ok()) { err = "cannot open " + path; return false; }
+    std::vector<std::string> t;
+    // main_para.f90:74-79 (the line holding dust_ii_gas is read as x1, and
+    // x2, x3, x_dip then continue on the field line, as list-directed input does)
+    if (!r.skip() || !r.read(t, 6)) { err = path + ": star line"; return false; }
+    in.star_mod = to_int(t[0]); in.T_star = to_double(t[1]); in.R_star = to_double(t[2]);
+    for (int k = 0; k < 3; k++) in.XYZ_star[k] = to_double(t[3 + k]);
+    if (!r.read(t, 3)) { err = path + ": nth nph nvel"; return false; }
+    in.nth = to_int(t[0]); in.nph = to_int(t[1]); in.nvel = to_int(t[2]);
+    if (!r.read(t, 4)) { err = path + ": field line"; return false; }
+    in.x1 = to_double(t[0]); in.x2 = to_double(t[1]); in.x3 = to_double(t[2]); in.x_dip = to_double(t[3]);
+    if (!r.read(t, 2)) { err = path + ": kmax extra_info"; return false; }
+    in.kmax = to_int(t[0]); in.extra_info = to_int(t[1]);
+    if (!r.read(t, 2)) { err = path + ": max_ne_temp n_depth"; return false; }
+    in.max_ne_temp = to_int(t[0]); in.n_depth = to_int(t[1]);
+    return true;
+}
+
+bool read_finish_input(const std::string &path, FinishInput &in, std::string &err) {
+    ListReader r(path);
+    if (!r.ok()) { err = "cannot open " + path; return false; }
+    std::vector<std::string> t;
+    std::vector<int> vi;
+    std::vector<double> vd;
+    // para_finish.f90:89-121
+    if (!r.skip() || !r.read(t, 1)) { err = path + ": nlevels"; return false; }
+    in.nlevels = to_int(t[0]);
+    if (in.nlevels < 1) { err = path + ": nlevels < 1"; return false; }
+    if (!r.read_ints(in.l1, in.nlevels) || !r.read_ints(in.l2, in.nlevels)) { err = path + ": l1/l2"; return false; }
+    if (!r.skip() || !r.read(t, 1)) { err = path + ": nincs"; return false; }
+    in.nincs = to_int(t[0]);
+    if (in.nincs < 1) { err = path + ": nincs < 1"; return false; }
+    if (!r.read_doubles(in.th_inc, in.nincs) || !r.read_doubles(in.ph_az, in.nincs)) { err = path + ": angles"; return false; }
+    if (!r.skip() || !r.read(t, 3)) { err = path + ": nvel dvel v0"; return false; }
+    in.nvel = to_int(t[0]); in.dvel = to_double(t[1]); in.v0 = to_double(t[2]);
+    if (!r.skip() || !r.read(t, 6)) { err = path + ": star line"; return false; }
+    in.star_mod = to_int(t[0]); in.T_star = to_double(t[1]); in.R_star = to_double(t[2]);
+    for (int k = 0; k < 3; k++) in.XYZ_star[k] = to_double(t[3 + k]);
+    if (!r.read(t, 4)) { err = path + ": field line"; return false; }
+    in.x1 = to_double(t[0]); in.x2 = to_double(t[1]); in.x3 = to_double(t[2]); in.x_dip = to_double(t[3]);
+    if (!r.read(t, 2)) { err = path + ": kmax extra_info"; return false; }
+    in.kmax = to_int(t[0]); in.extra_info = to_int(t[1]);
+    if (!r.read(t, 3)) { err = path + ": pix im_pix im_size"; return false; }
+    in.pix = to_int(t[0]); in.im_pix = to_int(t[1]); in.im_size = to_double(t[2]);
+    if (!r.read(t, 2)) { err = path + ": fits distance"; return false; }
+    in.fits = to_int(t[0]); in.distance = to_double(t[1]);
+    if (!r.read(t, 2)) { err = path + ": max_ne_temp n_depth_rt"; return false; }
+    in.max_ne_temp = to_int(t[0]); in.n_depth_rt = to_int(t[1]);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// LIME / LAMDA / dust
+// ---------------------------------------------------------------------------
+
+bool read_lime(const std::string &pop, const std::string &grid, const std::string &mol,
+               const std::string &dust, double dust_ii_gas, int max_ne_temp, Molecule &m, Cloud &c,
+               std::string &err) {
+    (void)dust_ii_gas;  // the per-node gas-to-dust column of the .pop is what eat_lime uses
+    std::vector<std::string> t;
+    std::vector<double> vd;
+    // ---- grid.vtk: points (eat_lime_dim eat_lime.f90:21-34, :124-136) ----
+    ListReader g(grid);
+    if (!g.ok()) { err = "cannot open " + grid; return false; }
+    for (int k = 0; k < 4; k++) g.skip();
+    if (!g.read(t, 2)) { err = grid + ": POINTS line"; return false; }
+    const int N = to_int(t[1]);
+    if (N < 1) { err = grid + ": no points"; return false; }
+    c.node_num = N;
+    c.xyz.resize(3 * (size_t)N);
+    for (int i = 0; i < N; i++) {
+        if (!g.read_doubles(vd, 3)) { err = grid + ": point " + std::to_string(i + 1); return false; }
+        for (int k = 0; k < 3; k++) c.xyz[3 * (size_t)i + k] = vd[k];
+    }
+    g.skip();
+    if (!g.read(t, 2)) { err = grid + ": CELLS line"; return false; }
+    const int ntet = to_int(t[1]);
+    // adj_list_no_delaunay miscellaneous.f90:910-1015: each tetrahedron gives
+    // its vertices the other three; SortUnique then sorts and de-duplicates
+    std::vector<std::vector<int>> nb(N);
+    for (int q = 0; q < ntet; q++) {
+        std::vector<int> vi;
+        if (!g.read_ints(vi, 5)) { err = grid + ": cell " + std::to_string(q + 1); return false; }
+        int v[4];
+        for (int k = 0; k < 4; k++) {
+            v[k] = vi[1 + k] + 1;
+            if (v[k] < 1 || v[k] > N) { err = grid + ": cell vertex out of range"; return false; }
+        }
+        for (int k = 0; k < 4; k++)
+            for (int k2 = 0; k2 < 4; k2++)
+                if (k2 != k) nb[v[k] - 1].push_back(v[k2]);
+    }
+    int maxne = 0;
+    c.del_num_ne.assign(N, 0);
+    for (int i = 0; i < N; i++) {
+        if ((int)nb[i].size() > max_ne_temp) {  // miscellaneous.f90:1000-1004
+            err = "count_ne=" + std::to_string(nb[i].size()) + " while max_ne_temp=" +
+                  std::to_string(max_ne_temp) + "; adjust max_ne_temp parameter! Make it bigger.";
+            return false;
+        }
+        std::sort(nb[i].begin(), nb[i].end());
+        nb[i].erase(std::unique(nb[i].begin(), nb[i].end()), nb[i].end());
+        c.del_num_ne[i] = (int)nb[i].size();
+        maxne = std::max(maxne, c.del_num_ne[i]);
+    }
+    c.maxne = maxne;
+    c.del_ne.assign((size_t)N * maxne, 0);  // main_para.f90:124-128
+    for (int i = 0; i < N; i++)
+        for (size_t s = 0; s < nb[i].size(); s++) c.del_ne[(size_t)i + (size_t)N * s] = nb[i][s];
+
+    // ---- LAMDA (eat_lime_dim :38-62, eat_lime_no_delaunay :151-196) ----
+    ListReader f(mol);
+    if (!f.ok()) { err = "cannot open " + mol; return false; }
+    for (int k = 0; k < 3; k++) f.skip();
+    if (!f.read_doubles(vd, 1)) { err = mol + ": molecular weight"; return false; }
+    m.mass = vd[0];
+    f.skip();
+    if (!f.read(t, 1)) { err = mol + ": number of levels"; return false; }
+    m.nlev = to_int(t[0]);
+    f.skip();
+    m.e_levs.resize(m.nlev);
+    m.j_lev.resize(m.nlev);
+    for (int i = 0; i < m.nlev; i++) {
+        if (!f.read(t, 3)) { err = mol + ": level " + std::to_string(i + 1); return false; }
+        m.e_levs[i] = to_double(t[1]);
+        const double g1 = to_double(t[2]);
+        m.j_lev[i] = (int)std::lround((g1 - 1.0) / 2.0);  // nint
+    }
+    f.skip();
+    if (!f.read(t, 1)) { err = mol + ": number of radiative transitions"; return false; }
+    m.r_num = to_int(t[0]);
+    f.skip();
+    m.r_trans.resize(2 * (size_t)m.r_num);
+    m.A.resize(m.r_num);
+    m.nu.resize(m.r_num);
+    for (int i = 0; i < m.r_num; i++) {
+        if (!f.read(t, 5)) { err = mol + ": radiative transition " + std::to_string(i + 1); return false; }
+        m.r_trans[2 * i + 1] = to_int(t[1]);  // upper
+        m.r_trans[2 * i] = to_int(t[2]);      // lower
+        m.A[i] = to_double(t[3]);
+        m.nu[i] = to_double(t[4]);
+    }
+    f.skip();
+    if (!f.read(t, 1)) { err = mol + ": number of collision partners"; return false; }
+    m.c_par = to_int(t[0]);
+    if (m.c_par < 1 || m.c_par > 2) { err = mol + ": 1 or 2 collision partners"; return false; }
+    for (int k = 0; k < 3; k++) f.skip();
+    if (!f.read(t, 1)) { err = mol + ": number of collisional transitions"; return false; }
+    m.c_num = to_int(t[0]);
+    f.skip();
+    if (!f.read(t, 1)) { err = mol + ": number of collision temperatures"; return false; }
+    m.c_temp = to_int(t[0]);
+    f.skip();
+    if (!f.read_doubles(m.col_temps, m.c_temp)) { err = mol + ": collision temperatures"; return false; }
+    f.skip();
+    m.c_trans.resize(2 * (size_t)m.c_num);
+    m.C.assign((size_t)m.c_temp * m.c_num * m.c_par, 0.0);
+    for (int i = 0; i < m.c_num; i++) {
+        if (!f.read(t, 3 + (size_t)m.c_temp)) { err = mol + ": collisional transition " + std::to_string(i + 1); return false; }
+        m.c_trans[2 * i + 1] = to_int(t[1]);
+        m.c_trans[2 * i] = to_int(t[2]);
+        for (int k = 0; k < m.c_temp; k++) m.C[(size_t)k + (size_t)m.c_temp * i] = to_double(t[3 + k]);
+    }
+    if (m.c_par == 2) {
+        // eat_lime.f90:184-195: five records skipped, then the partner's
+        // temperature count is read as its transition count
+        for (int k = 0; k < 5; k++) f.skip();
+        if (!f.read(t, 1)) { err = mol + ": second partner"; return false; }
+        const int c2 = to_int(t[0]);
+        for (int k = 0; k < 3; k++) f.skip();
+        for (int i = 0; i < c2 && i < m.c_num; i++) {
+            if (!f.read(t, 3 + (size_t)m.c_temp)) { err = mol + ": second partner rates"; return false; }
+            for (int k = 0; k < m.c_temp; k++)
+                m.C[(size_t)k + (size_t)m.c_temp * (i + (size_t)m.c_num)] = to_double(t[3 + k]);
+        }
+    }
+    // ---- .pop rows (eat_lime.f90:207-224) ----
+    ListReader p(pop);
+    if (!p.ok()) { err = "cannot open " + pop; return false; }
+    p.skip();
+    const int nl = m.nlev;
+    c.nlev = nl;
+    c.vel.assign(3 * (size_t)N, 0.0);
+    c.h2_dens.assign(N, 1.0);
+    c.temp_all.assign(2 * (size_t)N, 0.0);
+    c.b_all.assign(N, 200.0);
+    c.ab_all.assign(N, 1e-3);
+    c.lev_p.assign((size_t)nl * N, 0.0);
+    std::vector<double> g2d(N, 0.0);
+    int bulk = 0;
+    while (bulk < N && p.read_doubles(vd, 13 + (size_t)nl)) {
+        const int i = bulk;
+        for (int k = 0; k < 3; k++) c.vel[3 * (size_t)i + k] = vd[3 + k];
+        c.h2_dens[i] = vd[6];
+        c.temp_all[2 * (size_t)i] = vd[7];
+        c.temp_all[2 * (size_t)i + 1] = vd[8];
+        c.b_all[i] = vd[9];
+        c.ab_all[i] = vd[10];
+        g2d[i] = vd[11];
+        for (int l = 0; l < nl; l++) c.lev_p[(size_t)nl * i + l] = vd[13 + l];
+        bulk++;
+    }
+    c.bulk_node_num = bulk;
+    // surface nodes (eat_lime.f90:227-245)
+    for (int j = bulk; j < N; j++) {
+        double sp = 1.0;
+        c.lev_p[(size_t)nl * j] = 1.0;
+        for (int k = 1; k < nl; k++) {
+            c.lev_p[(size_t)nl * j + k] = 1.0 * std::exp(-m.e_levs[k] * 0.527);
+            sp += c.lev_p[(size_t)nl * j + k];
+        }
+        for (int k = 0; k < nl; k++) c.lev_p[(size_t)nl * j + k] /= sp;
+    }
+    for (int j = 0; j < N; j++) {  // :250-263
+        const double b_therm = 2.0 * 8314.462 * c.temp_all[2 * (size_t)j] / m.mass;
+        c.b_all[j] = std::sqrt(c.b_all[j] * c.b_all[j] + b_therm);
+        for (int l = 0; l < nl; l++) c.lev_p[(size_t)nl * j + l] *= c.ab_all[j] * c.h2_dens[j];
+    }
+    double rmax = 0.0;  // :269-279
+    for (int i = 0; i < N; i++) {
+        const double *x = &c.xyz[3 * (size_t)i];
+        rmax = std::max(rmax, std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]));
+    }
+    for (auto &v : c.xyz) v /= rmax;
+    c.tx = rmax;
+    // ---- dust table (eat_lime.f90:285-298, dust_to_opacities miscellaneous.f90:643-700) ----
+    ListReader d(dust);
+    if (!d.ok()) { err = "cannot open " + dust; return false; }
+    const int n_dt = 67;
+    std::vector<double> lt(n_dt), lk(n_dt);
+    for (int i = 0; i < n_dt; i++) {
+        if (!d.read_doubles(vd, 2)) { err = dust + ": row " + std::to_string(i + 1); return false; }
+        lt[i] = std::log10(vd[0]);
+        lk[i] = std::log10(vd[1]);
+    }
+    m.kd_v.resize(m.r_num);
+    for (int i = 0; i < m.r_num; i++) {
+        const double nu_hz = m.nu[i] * f4(1e9);
+        const double mu0 = std::log10(f4(2.998e14) / nu_hz);
+        double kd_m = 0.0;
+        for (int j = 0; j < n_dt - 1; j++)
+            if (mu0 > lt[j] && mu0 < lt[j + 1]) {
+                const double res = (mu0 - lt[j]) / (lt[j + 1] - lt[j]);
+                kd_m = lk[j] + res * (lk[j + 1] - lk[j]);
+                break;
+            }
+        if (mu0 > lt[n_dt - 1]) {
+            const double res = (mu0 - lt[n_dt - 1]) / (lt[n_dt - 1] - lt[n_dt - 2]);
+            kd_m = lk[n_dt - 1] + res * (lk[n_dt - 1] - lk[n_dt - 2]);
+        }
+        m.kd_v[i] = std::pow(10.0, kd_m) * f4(1e-1);
+    }
+    c.dust_p.assign(N, 0.0);  // :302-311
+    for (int i = 0; i < N; i++)
+        if (g2d[i] != 0.0) c.dust_p[i] = c.h2_dens[i] * f4(2.32e-27) / g2d[i];
+    // ---- main_para.f90:119-120, :178-185 ----
+    for (auto &v : m.nu) v = f4(1e9) * v;
+    for (auto &v : m.e_levs) v = f4(29.9792458e9) * v;
+    m.Bij.resize(m.r_num);
+    for (int i = 0; i < m.r_num; i++) {
+        const double g1 = 2.0 * m.j_lev[m.r_trans[2 * i] - 1] + 1.0;
+        const double g2 = 2.0 * m.j_lev[m.r_trans[2 * i + 1] - 1] + 1.0;
+        m.Bij[i] = (g2 / g1) * m.A[i] * 1.6179542e57 / std::pow(m.nu[i], 3.0);
+    }
+    return true;
+}
+
+void magfield(const Cloud &c, double x1, double x2, double x3, double x_dip, std::vector<double> &bvec) {
+    const int N = c.node_num;
+    bvec.assign(3 * (size_t)N, 0.0);
+    auto nrm = [](const double *v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    for (int i = 0; i < N; i++) {
+        const double *x = &c.xyz[3 * (size_t)i];
+        double b[3];
+        if (x_dip != 0.0) {  // dipole_magfield miscellaneous.f90:553-595
+            double xv[3] = {x[0], x[1], x[2]};
+            const double n = nrm(xv);
+            for (auto &v : xv) v /= n;
+            b[0] = 3.0 * xv[0] * xv[2];
+            b[1] = 3.0 * xv[1] * xv[2];
+            b[2] = 3.0 * xv[2] * xv[2] - 1.0;
+        } else {  // global_magfield :597-641
+            double rad[3] = {x[0], x[1], x[2]}, tor[3] = {x[1], -x[0], 0.0};
+            double pol[3] = {x[2] * x[0], x[1] * x[2], -(x[1] * x[1] + x[0] * x[0])};
+            const double nr = nrm(rad), nt = nrm(tor), np = nrm(pol);
+            for (int k = 0; k < 3; k++) b[k] = x1 * rad[k] / nr + x2 * tor[k] / nt + x3 * pol[k] / np;
+        }
+        const double nb = nrm(b);
+        for (int k = 0; k < 3; k++) bvec[3 * (size_t)i + k] = b[k] / nb;
+    }
+}
+
+void gauge_vector(unsigned long long seed, double g[3]) {
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    for (int k = 0; k < 3; k++) g[k] = u(rng);
+    const double n = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    for (int k = 0; k < 3; k++) g[k] /= n;
+}
+
+bool write_rows(const std::string &path, const std::vector<double> &cm, int rows, int cols) {
+    FILE *f = fopen(path.c_str(), "w");
+    if (!f) return false;
+    for (int r = 0; r < rows; r++) {
+        for (int k = 0; k < cols; k++) fprintf(f, " %24.17E", cm[(size_t)r + (size_t)rows * k]);
+        fputc('\n', f);
+    }
+    return fclose(f) == 0;
+}
+
+bool read_rows(const std::string &path, std::vector<double> &cm, int rows, int cols, std::string &err) {
+    ListReader r(path);
+    if (!r.ok()) { err = "cannot open " + path; return false; }
+    cm.assign((size_t)rows * cols, 0.0);
+    std::vector<double> v;
+    for (int i = 0; i < rows; i++) {  // para_finish.f90:226-227
+        if (!r.read_doubles(v, cols)) { err = path + ": row " + std::to_string(i + 1); return false; }
+        for (int k = 0; k < cols; k++) cm[(size_t)i + (size_t)rows * k] = v[k];
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// FITS
+// ---------------------------------------------------------------------------
+
+static std::string card_log(const char *k, bool v) {
+    char b[81];
+    snprintf(b, sizeof b, "%-8s= %20s", k, v ? "T" : "F");
+    return b;
+}
+static std::string card_int(const char *k, long v) {
+    char b[81];
+    snprintf(b, sizeof b, "%-8s= %20ld", k, v);
+    return b;
+}
+static std::string card_e(const char *k, float v) {  // ftpkye with 8 decimals
+    char b[81];
+    snprintf(b, sizeof b, "%-8s= %20.8E", k, (double)v);
+    return b;
+}
+static std::string card_s(const char *k, const char *v) {
+    char q[72];
+    snprintf(q, sizeof q, "'%-8s'", v);
+    char b[81];
+    snprintf(b, sizeof b, "%-8s= %-20s", k, q);
+    return b;
+}
+
+bool write_fits(const std::string &path, const float *a, int npix, int nvel, float restfreq, float cdelt1,
+                float crpix1, float cdelt2, float crpix2, float cdelt3, float crpix3, float crval1,
+                float crval2, float crval3) {
+    std::vector<std::string> cards = {
+        card_log("SIMPLE", true), card_int("BITPIX", -32), card_int("NAXIS", 3),
+        card_int("NAXIS1", npix), card_int("NAXIS2", npix), card_int("NAXIS3", nvel),
+        card_log("EXTEND", true), card_s("OBJECT", "PORTAL"), card_e("EPOCH", 2.0e3f),
+        card_e("LONPOLE", 1.8e2f), card_e("EQUINOX", 2.0e3f), card_s("SPECSYS", "LSRK"),
+        card_e("RESTFREQ", restfreq), card_int("VELREF", 257), card_s("CTYPE1", "RA---SIN"),
+        card_e("CDELT1", cdelt1), card_e("CRPIX1", crpix1), card_e("CRVAL1", crval1),
+        card_s("CUNIT1", "DEG"), card_s("CTYPE2", "DEC--SIN"), card_e("CDELT2", cdelt2),
+        card_e("CRPIX2", crpix2), card_e("CRVAL2", crval2), card_s("CUNIT2", "DEG"),
+        card_s("CTYPE3", "VELO-LSR"), card_e("CDELT3", cdelt3), card_e("CRPIX3", crpix3),
+        card_e("CRVAL3", crval3), card_s("CUNIT3", "M/S"), card_e("BSCALE", 1.0f),
+        card_e("BZERO", 0.0f), card_s("BUNIT", "K"), "END"};
+    std::string hdr;
+    for (auto &c : cards) {
+        std::string x = c;
+        x.resize(80, ' ');
+        hdr += x;
+    }
+    hdr.resize((hdr.size() + 2879) / 2880 * 2880, ' ');
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    fwrite(hdr.data(), 1, hdr.size(), f);
+    const size_t n = (size_t)npix * npix * nvel;
+    std::vector<unsigned char> buf(n * 4);
+    for (size_t i = 0; i < n; i++) {
+        uint32_t u;
+        memcpy(&u, &a[i], 4);
+        buf[4 * i] = (unsigned char)(u >> 24);
+        buf[4 * i + 1] = (unsigned char)(u >> 16);
+        buf[4 * i + 2] = (unsigned char)(u >> 8);
+        buf[4 * i + 3] = (unsigned char)u;
+    }
+    fwrite(buf.data(), 1, buf.size(), f);
+    const size_t pad = (2880 - (buf.size() % 2880)) % 2880;
+    std::vector<unsigned char> z(pad, 0);
+    if (pad) fwrite(z.data(), 1, pad, f);
+    return fclose(f) == 0;
+}
+
+}  // namespace portal_io

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libportal_gb300.so")
-SOURCES = ["ctx.cu", "rf.cu", "rf_static.cu", "se.cu", "image.cu", "wigner.cpp"]
+SOURCES = ["ctx.cu", "rf.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "wigner.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -57,7 +57,30 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_apps()
     return LIB
+
+
+APPS = os.path.join(HERE, "apps")
+
+
+def build_apps() -> list:
+    """The drop-in executables main_portal.x and finish_portal.x (host C++
+    over the C ABI), linked against the library with an $ORIGIN rpath."""
+    outs = []
+    io_src = os.path.join(APPS, "portal_io.cpp")
+    for prog in ("main_portal", "finish_portal"):
+        src = os.path.join(APPS, prog + ".cpp")
+        exe = os.path.join(OUT, prog + ".x")
+        deps = [src, io_src, os.path.join(APPS, "portal_io.h"), LIB]
+        if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
+            cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                   "-I", APPS, src, io_src, "-o", exe, "-L", OUT, "-lportal_gb300", "-Wl,-rpath,$ORIGIN"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"{prog} build failed:\n{r.stderr}")
+        outs.append(exe)
+    return outs
 
 
 if __name__ == "__main__":

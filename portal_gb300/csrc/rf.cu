@@ -191,11 +191,13 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
                     int2 *wl = wbase + (size_t)lane * a.n_depth;
-                    double s = 0.0;
+                    // distance left to the sphere exit as an unevaluated float pair
+                    // (rh + rl), decremented exactly by each step
+                    float rh = (float)sexit, rl = (float)(sexit - (double)rh);
                     float rx = 0.f, ry = 0.f, rz = 0.f;
                     int c = node;
                     for (;;) {
-                        const float tsph = (float)(sexit - s);
+                        const float tsph = rh + rl;
                         const int o = a.off[c], deg = a.off[c + 1] - o;
                         // check_neigh_fast's scan: best starts at the sphere exit, a
                         // neighbour replaces it when FACE_EPS < t <= best (so among equal
@@ -219,7 +221,14 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                         K++;
                         if (bj < 0) break;
                         const float4 e = a.edge[o + bj];
-                        s += (double)delta;
+                        {   // (rh, rl) -= delta: two-sum, then renormalise
+                            const float t = rh - delta;
+                            const float bv = t - rh;
+                            const float err = (rh - (t - bv)) - (delta + bv);
+                            const float lo = rl + err;
+                            rh = t + lo;
+                            rl = lo - (rh - t);
+                        }
                         rx = fmaf(delta, fdx, rx) - e.x;
                         ry = fmaf(delta, fdy, ry) - e.y;
                         rz = fmaf(delta, fdz, rz) - e.z;
@@ -261,16 +270,31 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                 const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
 #pragma unroll
                                 for (int l = 0; l < NLG; l++) {
-                                    if (l0 + l < a.L) {
-                                        const float4 v = lt[l];
-                                        R.As[lane][l] = v.x * fst;
-                                        if (DUST) {
+                                    if (DUST) {
+                                        if (l0 + l < a.L) {
+                                            const float4 v = lt[l];
+                                            R.As[lane][l] = v.x * fst;
                                             R.Ss[lane][l] = v.y * fst;
                                             R.Ad[lane][DUST ? l : 0] = v.z * fst;
                                             R.Jd[lane][DUST ? l : 0] = v.w * fst;
-                                        } else {
-                                            R.Ss[lane][l] = v.y / v.x;
                                         }
+                                    } else {
+                                        // optical depth at unit profile in log2 units (ex2
+                                        // takes it as is) and the source function.  A cell
+                                        // line with kv <= 0 fails ray_in's gate tau > 1e-30
+                                        // in every channel (inverse_rt.f90:308), and so does
+                                        // a padding line of the last group: both get A = S
+                                        // = 0, which leaves I unchanged exactly (e = 1).
+                                        float As = 0.f, Ss = 0.f;
+                                        if (l0 + l < a.L) {
+                                            const float4 v = lt[l];
+                                            if (v.x > 0.f) {
+                                                As = v.x * fst * LOG2E_F;
+                                                Ss = v.y / v.x;
+                                            }
+                                        }
+                                        R.As[lane][l] = As;
+                                        R.Ss[lane][l] = Ss;
                                     }
                                 }
                             }
@@ -285,25 +309,33 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                 }
 #pragma unroll
                                 for (int l = 0; l < NLG; l++) {
-                                    if (l0 + l < a.L) {
-                                        const float Au = R.As[u][l];
-                                        const float Su = R.Ss[u][l];
-                                        float Adu = 0.f, Jdu = 0.f;
-                                        if (DUST) { Adu = R.Ad[u][DUST ? l : 0]; Jdu = R.Jd[u][DUST ? l : 0]; }
+                                    const float Au = R.As[u][l];
+                                    const float Su = R.Ss[u][l];
+                                    if (DUST) {
+                                        if (l0 + l < a.L) {
+                                            const float Adu = R.Ad[u][DUST ? l : 0], Jdu = R.Jd[u][DUST ? l : 0];
+#pragma unroll
+                                            for (int s2 = 0; s2 < NS; s2++) {
+                                                // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
+                                                const float tau = fmaf(Au, g[s2], Adu);
+                                                const float Sv = fmaf(Su, g[s2], Jdu) / tau;
+                                                const float e = ex2(-tau * LOG2E_F);
+                                                const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                                I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                            }
+                                        }
+                                    } else {
+                                        // ray_in's gate tau > 1e-30 (inverse_rt.f90:308) needs no
+                                        // test here: channels below it have ex2(-tau) == 1
+                                        // exactly (the rounding of ex2.approx for arguments above
+                                        // -2^-23), and I e + S (1 - e), formed as
+                                        // fma(I, e, fma(-S, e, S)), then leaves I unchanged;
+                                        // lines with kv <= 0 carry A = S = 0.  Branch-free, so
+                                        // the NS x NLG update chains of a cell interleave.
 #pragma unroll
                                         for (int s2 = 0; s2 < NS; s2++) {
-                                            float tau, Sv;
-                                            if (DUST) {
-                                                // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
-                                                tau = fmaf(Au, g[s2], Adu);
-                                                Sv = fmaf(Su, g[s2], Jdu) / tau;
-                                            } else {
-                                                tau = Au * g[s2];
-                                                Sv = Su;
-                                            }
-                                            const float e = ex2(-tau * LOG2E_F);
-                                            const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
-                                            I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                            const float e = ex2(-Au * g[s2]);
+                                            I[s2][l] = fmaf(I[s2][l], e, fmaf(-Su, e, Su));
                                         }
                                     }
                                 }
@@ -455,7 +487,6 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
         return set_err(c, PORTAL_ERR_ARG, "portal_radiation_field: bad nth/nph/nvel/n_depth/dx "
                                           "(at most 288 channels)");
     cudaSetDevice(c->device);
-    timers_reset(c);
     int rc;
     if ((rc = upload_lines(c))) return rc;
     const int L = c->r_num, N = c->N;
@@ -536,6 +567,7 @@ extern "C" int portal_radiation_field(portal_ctx *c, int nth, int nph, int nvel,
                                       double dx, int n_depth, double *J0, double *J2, int *status,
                                       long long *n_segments) {
     if (!c) return PORTAL_ERR_ARG;
+    timers_reset(c);
     int rc = portal::run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, n_segments, nullptr);
     if (rc) return rc;
     const size_t LN = (size_t)c->r_num * c->N;

@@ -1,0 +1,134 @@
+"""The drop-in executables main_portal.x / finish_portal.x: file parsing on the
+CPU (parse-only dump), and the whole file -> GPU -> file path on the GPU."""
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from portal_gb300 import lime, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MAIN = os.path.join(ROOT, "portal_gb300", "_build", "main_portal.x")
+FINISH = os.path.join(ROOT, "portal_gb300", "_build", "finish_portal.x")
+
+
+@pytest.fixture(scope="module")
+def case(tmp_path_factory, built_lib):
+    d = str(tmp_path_factory.mktemp("portal_case"))
+    mol = synth.linear_rotor(5)
+    cloud = synth.power_law_sphere(2000, 3, mol, keep_raw=True)
+    rc = synth.RunConfig(nth=8, nph=8, nvel=16, kmax=6, gvec=synth.gauge_vector(3))
+    paths = lime.write_case(d, cloud, mol)
+    lime.write_main_input(os.path.join(d, "pol.dat"), rc, extra_info=1)
+    return dict(d=d, mol=mol, cloud=cloud, rc=rc, paths=paths)
+
+
+def _run(exe, case, env_extra, input_name="pol.dat"):
+    p = case["paths"]
+    env = dict(os.environ, **env_extra)
+    return subprocess.run([exe, os.path.join(case["d"], input_name), case["d"], p["pop"], p["grid"], p["mol"],
+                           p["dust"]], env=env, capture_output=True, text=True, timeout=600)
+
+
+def _npy(d, name):
+    return np.load(os.path.join(d, name + ".npy"))
+
+
+def test_ingestion_matches_python_restatement(case):
+    """eat_lime_no_delaunay + main_para.f90:119-185 from the files (C++)
+    equal the same transforms applied in memory (Python)."""
+    dd = os.path.join(case["d"], "dump_b")
+    os.makedirs(dd, exist_ok=True)
+    r = _run(MAIN, case, dict(PORTAL_DUMP_INGESTED=dd, PORTAL_BVEC_FILE=case["paths"]["bvec"]))
+    assert r.returncode == 0, r.stderr
+    cloud, mol = case["cloud"], case["mol"]
+    np.testing.assert_array_equal(_npy(dd, "xyz"), cloud.xyz.ravel())
+    np.testing.assert_array_equal(_npy(dd, "vel"), cloud.vel.ravel())
+    np.testing.assert_array_equal(_npy(dd, "b_all"), cloud.b_all)
+    np.testing.assert_array_equal(_npy(dd, "lev_p"), cloud.lev_p.ravel())
+    np.testing.assert_array_equal(_npy(dd, "bvec"), cloud.bvec.ravel())
+    np.testing.assert_array_equal(_npy(dd, "del_ne"), cloud.del_ne().ravel())
+    np.testing.assert_array_equal(_npy(dd, "del_num_ne"), cloud.del_num_ne())
+    for name in ("e_levs", "nu", "A", "Bij", "kd_v"):
+        np.testing.assert_array_equal(_npy(dd, name), getattr(mol, name))
+    sc = _npy(dd, "scalars")
+    assert sc[0] == cloud.tx and int(sc[1]) == cloud.bulk_node_num and sc[3] == mol.mass
+
+
+def test_input_file_line_shift_is_reproduced(case):
+    """main_para.f90:77 reads x1..x_dip starting on the dust_ii_gas line of
+    the file run_portal.sh writes, so x1 = dust_ii_gas, x2 = b_rad,
+    x3 = b_tor, x_dip = b_pol (b_dip is never read): with the field line
+    "0 1 0 1.d0" the field is global_magfield(0.01, 0, 1)."""
+    dd = os.path.join(case["d"], "dump_g")
+    os.makedirs(dd, exist_ok=True)
+    r = _run(MAIN, case, dict(PORTAL_DUMP_INGESTED=dd))
+    assert r.returncode == 0, r.stderr
+    b = _npy(dd, "bvec").reshape(-1, 3)
+    x = case["cloud"].xyz
+    rad = x / np.linalg.norm(x, axis=1, keepdims=True)
+    pol = np.stack([x[:, 2] * x[:, 0], x[:, 1] * x[:, 2], -(x[:, 1] ** 2 + x[:, 0] ** 2)], axis=1)
+    pol /= np.linalg.norm(pol, axis=1, keepdims=True)
+    ref = 0.01 * rad + 1.0 * pol
+    ref /= np.linalg.norm(ref, axis=1, keepdims=True)
+    np.testing.assert_allclose(b, ref, rtol=0, atol=1e-14)
+
+
+def test_fits_writer_roundtrip(tmp_path, built_lib):
+    """writeimage's header keywords and big-endian float data
+    (fits_writing.f90:57-149), read back by the repo's own parser."""
+    import ctypes as C
+    cube = np.arange(5 * 7 * 7, dtype=np.float32).reshape(5, 7, 7) * 0.25
+    # exercise the C++ writer through finish_portal's FITS routine: a tiny
+    # shim library is not shipped, so write with Python in the same layout and
+    # parse it back; the C++ writer is exercised end to end in the GPU test
+    path = str(tmp_path / "x.fits")
+    cards = ["SIMPLE  =                    T", "BITPIX  =                  -32", "NAXIS   =                    3",
+             "NAXIS1  =                    7", "NAXIS2  =                    7", "NAXIS3  =                    5", "END"]
+    hdr = "".join(c.ljust(80) for c in cards)
+    hdr = hdr.ljust((len(hdr) + 2879) // 2880 * 2880)
+    data = cube.astype(">f4").tobytes()
+    with open(path, "wb") as f:
+        f.write(hdr.encode() + data + b"\0" * ((2880 - len(data) % 2880) % 2880))
+    h, d = lime.read_fits(path)
+    assert h["NAXIS3"] == "5" and np.array_equal(d, cube)
+
+
+@pytest.mark.gpu
+def test_main_and_finish_portal_end_to_end(case):
+    """main_portal.x then finish_portal.x on files equal the library calls on
+    the same cloud: pol_pops.dat to the last digit written, and the FITS
+    cubes to the I_to_T scaling."""
+    import portal_gb300 as pg
+    d, cloud, mol, rc = case["d"], case["cloud"], case["mol"], case["rc"]
+    env = dict(PORTAL_BVEC_FILE=case["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec))
+    r = _run(MAIN, case, env)
+    assert r.returncode == 0, r.stderr
+    pops_file = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        ctx.radiation_field(rc, fetch=False)
+        pops, _ = ctx.solve_se(rc.kmax)
+        np.testing.assert_allclose(pops_file, pops, rtol=1e-15, atol=0)
+        im = dict(l1=[1], l2=[2], th_inc=[0.78539816339], ph_az=[0.0], nvel=8, dvel=50.0, v0=0.0, im_pix=12,
+                  im_size=0.7)
+        lime.write_finish_input(os.path.join(d, "finish.dat"), im["l1"], im["l2"], im["th_inc"], im["ph_az"],
+                                im["nvel"], im["dvel"], im["v0"], im["im_pix"], im["im_size"])
+        r2 = _run(FINISH, case, env, input_name="finish.dat")
+        assert r2.returncode == 0, r2.stderr
+        cube, st = ctx.image(im["l1"], im["l2"], im["th_inc"][0], im["ph_az"][0], im["nvel"], im["dvel"], im["v0"],
+                             im["im_pix"], im["im_size"], pol_pops=pops_file)
+    nu0 = mol.e_levs[1] - mol.e_levs[0]
+    I_to_T = 3.255e39 / nu0 ** 2
+    h, dI = lime.read_fits(os.path.join(d, "inc01-trans01-im_i.fits"))
+    assert h["BITPIX"] == "-32" and h["CTYPE3"] == "VELO-LSR" and h["BUNIT"] == "K"
+    assert abs(float(h["RESTFREQ"]) - nu0) <= 1e-6 * nu0
+    np.testing.assert_allclose(dI, (I_to_T * cube[0, 0].astype(np.float64)).astype(np.float32), rtol=1e-6,
+                               atol=1e-30)
+    h, dtau = lime.read_fits(os.path.join(d, "inc01-trans01-im_tau.fits"))
+    np.testing.assert_array_equal(dtau, cube[3, 0])
+    h, ddust = lime.read_fits(os.path.join(d, "inc01-trans01-dust_i.fits"))
+    assert ddust.shape == (1, 25, 25)

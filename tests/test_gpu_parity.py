@@ -223,3 +223,32 @@ def test_image_against_oracle(ctx):
     assert (np.abs(U - oU) / denom).max() < 1e-4
     # dust is off in this cloud: the dust maps are zero in both
     assert np.abs(cube[4:]).max() == 0.0 and np.abs(o[4:]).max() == 0.0
+
+
+# ---- Lambda iteration -------------------------------------------------------
+
+def test_lambda_iteration_against_oracle(ctx):
+    """Three passes of the iterated node loop against the oracle iterated the
+    same way (n_J = n_mol sqrt(2J+1) rho^0_0 between passes)."""
+    import oracle
+    cloud, mol, rc = _small(1024, nlev=5, t_uniform=20.0)
+    n_mol = cloud.lev_p.sum(axis=1)
+    g = np.sqrt(2 * mol.j_lev + 1.0)
+    P = oracle.OracleProblem(cloud, mol)
+    res_o = []
+    for it in range(3):
+        oJ0, oJ2, _, _, _ = P.radiation_field(rc)
+        opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2)
+        new = n_mol[:, None] * g[None, :] * opp[:, 0::2]
+        old_rho = P.lev_p / (n_mol[:, None] * g[None, :])
+        res_o.append(np.max(np.abs(opp[:, 0::2] - old_rho) / np.abs(opp[:, 0::2])))
+        P.lev_p[:] = new          # the oracle struct points at this array
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    pops, lev, n, res, nseg = ctx.lambda_iterate(rc, tol=1e-30, max_iter=3)
+    assert n == 3
+    np.testing.assert_allclose(lev, P.lev_p, rtol=2e-4)
+    np.testing.assert_allclose(res, res_o, rtol=0.05, atol=1e-6)
+    # a warm start at the result of the passes continues from it
+    pops2, lev2, n2, res2, _ = ctx.lambda_iterate(rc, tol=1e-30, max_iter=1, start_pops=pops)
+    assert res2[0] < res[-1] * 1.5 + 1e-7
