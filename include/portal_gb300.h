@@ -218,6 +218,61 @@ int portal_set_stream(portal_ctx *ctx, void *cuda_stream);
  * integration kernel; launches[i] the number of launches each. */
 int portal_last_kernel_times(const portal_ctx *ctx, double *times_ms, int *launches, int n);
 
+/* ---- learned warm start (no counterpart in the reference) -------------
+ *
+ * A small MLP maps per-node features of the cloud and of the first
+ * radiation field to the converged level populations, which then start
+ * portal_lambda_iterate (start_pops); the plain iteration stays the judge of
+ * convergence, so the fixed point it reaches is unchanged.  The network is
+ * n_in -> width (SiLU) x depth -> n_out (linear), FP32 master parameters,
+ * BF16 operands and FP32 accumulation on the tensor cores in every GEMM of
+ * the forward and the backward pass.  Inputs and targets are standardised
+ * with statistics held in the model (mean, standard deviation).
+ *
+ * Parameter layout (flat FP32, portal_mlp_num_params values): per layer
+ * l = 0..depth, the weights W_l (fan_out x fan_in, row-major) followed by
+ * the bias b_l (fan_out).  Statistics: mean_x(n_in), std_x(n_in),
+ * mean_y(n_out), std_y(n_out).  Matrices X(rows, n_in) and Y(rows, n_out)
+ * are row-major (a node's features contiguous).  An MLP owns its own CUDA
+ * stream on its device; calls are synchronous. */
+typedef struct portal_mlp portal_mlp;
+
+int portal_mlp_create(portal_mlp **mlp, int device, int n_in, int width, int depth, int n_out,
+                      unsigned long long seed);
+int portal_mlp_destroy(portal_mlp *mlp);
+const char *portal_mlp_last_error(const portal_mlp *mlp);
+long long portal_mlp_num_params(const portal_mlp *mlp);
+/* copy parameters / statistics out or in (either pointer may be NULL) */
+int portal_mlp_get_params(const portal_mlp *mlp, float *params, float *stats);
+int portal_mlp_set_params(portal_mlp *mlp, const float *params, const float *stats);
+/* One forward and backward pass on B rows of already standardised inputs X
+ * and targets T: the mean squared error over the B*n_out outputs and its
+ * gradient with respect to the flat parameters (grads may be NULL). */
+int portal_mlp_gradients(portal_mlp *mlp, const float *X, const float *T, int B, float *grads,
+                         float *loss);
+/* Fit to (X, Y) in raw units, M rows: the standardisation statistics are
+ * taken from this set, then `epochs` passes of shuffled minibatches of
+ * `batch` rows (the remainder of each pass is dropped) with Adam
+ * (beta 0.9 / 0.999, eps 1e-8) at learning rate lr; loss_per_epoch
+ * (epochs values, may be NULL) the mean standardised MSE of each pass. */
+int portal_mlp_train(portal_mlp *mlp, const float *X, const float *Y, int M, int epochs, int batch,
+                     float lr, unsigned long long seed, float *loss_per_epoch);
+/* Raw-unit predictions Y(B, n_out) for raw inputs X(B, n_in). */
+int portal_mlp_predict(portal_mlp *mlp, const float *X, int B, float *Y);
+
+/* The warm start's node features from the context's cloud and its
+ * device-resident radiation field (the last portal_radiation_field call):
+ * features(8, N) column-major (a node's 8 values contiguous):
+ *   0 log10 n_H2 [cm^-3], 1 log10 T_kin [K],
+ *   2 log10 |grad v| [s^-1] (Frobenius norm of the least-squares velocity
+ *     gradient over the node's neighbours),
+ *   3 cos^2 of the angle between the field and the principal axis of the
+ *     symmetric velocity gradient,
+ *   4, 5 log10 J^0_0 / B_nu(T_kin) of lines 1 and 2,
+ *   6, 7 100 J^2_0 / J^0_0 of lines 1 and 2
+ * (line 1 again for a one-line molecule). */
+int portal_warmstart_features(portal_ctx *ctx, float *features);
+
 /* ---- utilities -------------------------------------------------------- */
 
 /* Wigner 3j and 6j symbols, arguments doubled (2j, 2m) like wigxjpf's

@@ -35,6 +35,9 @@ EXPORTS = (
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
     "portal_radiation_field_static", "portal_radiation_field_static_limits",
     "portal_lambda_iterate",
+    "portal_mlp_create", "portal_mlp_destroy", "portal_mlp_last_error", "portal_mlp_num_params",
+    "portal_mlp_get_params", "portal_mlp_set_params", "portal_mlp_gradients", "portal_mlp_train",
+    "portal_mlp_predict", "portal_warmstart_features",
 )
 
 _lib = None
@@ -88,6 +91,20 @@ def lib() -> C.CDLL:
                                         C.c_double, C.c_int, P_D, P_D, P_D, P_I, P_D, C.POINTER(C.c_longlong)]
     L.portal_radiation_field_static_limits.restype = None
     L.portal_radiation_field_static_limits.argtypes = [P_I, P_I, P_I, P_I, C.POINTER(C.c_longlong)]
+    P_F = C.POINTER(C.c_float)
+    L.portal_mlp_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_ulonglong]
+    L.portal_mlp_destroy.argtypes = [C.c_void_p]
+    L.portal_mlp_last_error.restype = C.c_char_p
+    L.portal_mlp_last_error.argtypes = [C.c_void_p]
+    L.portal_mlp_num_params.restype = C.c_longlong
+    L.portal_mlp_num_params.argtypes = [C.c_void_p]
+    L.portal_mlp_get_params.argtypes = [C.c_void_p, P_F, P_F]
+    L.portal_mlp_set_params.argtypes = [C.c_void_p, P_F, P_F]
+    L.portal_mlp_gradients.argtypes = [C.c_void_p, P_F, P_F, C.c_int, P_F, P_F]
+    L.portal_mlp_train.argtypes = [C.c_void_p, P_F, P_F, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, P_F]
+    L.portal_mlp_predict.argtypes = [C.c_void_p, P_F, C.c_int, P_F]
+    L.portal_warmstart_features.argtypes = [C.c_void_p, P_F]
     _lib = L
     return L
 
@@ -251,6 +268,96 @@ class Context:
         n = np.zeros(len(KERNEL_SLOTS), dtype=np.int32)
         self._check(lib().portal_last_kernel_times(self._h, _p(t), _p(n, P_I), len(KERNEL_SLOTS)))
         return {k: (float(t[i]), int(n[i])) for i, k in enumerate(KERNEL_SLOTS)}
+
+
+    def warmstart_features(self) -> np.ndarray:
+        """Features (N, 8) of the warm start from the device-resident
+        radiation field of the last radiation_field call."""
+        f = np.zeros((self.N, 8), dtype=np.float32)
+        self._check(lib().portal_warmstart_features(self._h, _p(f, P_F)))
+        return f
+
+
+P_F = C.POINTER(C.c_float)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class MLP:
+    """The warm start's network (portal_mlp_*): n_in -> width (SiLU) x depth
+    -> n_out, trained and evaluated by the library's own BF16 kernels."""
+
+    def __init__(self, n_in: int, width: int, depth: int, n_out: int, seed: int = 0, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().portal_mlp_create(C.byref(self._h), device, n_in, width, depth, n_out, seed)
+        if rc != PORTAL_OK:
+            raise PortalError(rc, "portal_mlp_create")
+        self.n_in, self.width, self.depth, self.n_out = n_in, width, depth, n_out
+
+    def close(self):
+        if self._h:
+            lib().portal_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != PORTAL_OK:
+            raise PortalError(rc, lib().portal_mlp_last_error(self._h).decode())
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().portal_mlp_num_params(self._h))
+
+    def layer_shapes(self):
+        """[(fan_out, fan_in)] per layer, the order of the flat parameters."""
+        dims = [self.n_in] + [self.width] * self.depth + [self.n_out]
+        return [(dims[i + 1], dims[i]) for i in range(len(dims) - 1)]
+
+    def get_params(self):
+        p = np.zeros(self.num_params, dtype=np.float32)
+        st = np.zeros(2 * (self.n_in + self.n_out), dtype=np.float32)
+        self._check(lib().portal_mlp_get_params(self._h, _p(p, P_F), _p(st, P_F)))
+        return p, st
+
+    def set_params(self, params=None, stats=None):
+        p = None if params is None else _f32(params)
+        st = None if stats is None else _f32(stats)
+        self._check(lib().portal_mlp_set_params(self._h, _p(p, P_F), _p(st, P_F)))
+
+    def gradients(self, X, T):
+        """(loss, flat gradient) of the MSE on standardised X (B, n_in), T (B, n_out)."""
+        X, T = _f32(X), _f32(T)
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = C.c_float(0.0)
+        self._check(lib().portal_mlp_gradients(self._h, _p(X, P_F), _p(T, P_F), X.shape[0], _p(g, P_F),
+                                               C.byref(loss)))
+        return float(loss.value), g
+
+    def train(self, X, Y, epochs: int, batch: int, lr: float, seed: int = 0):
+        X, Y = _f32(X), _f32(Y)
+        losses = np.zeros(epochs, dtype=np.float32)
+        self._check(lib().portal_mlp_train(self._h, _p(X, P_F), _p(Y, P_F), X.shape[0], epochs, batch, float(lr),
+                                           seed, _p(losses, P_F)))
+        return losses
+
+    def predict(self, X):
+        X = _f32(X)
+        Y = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
+        self._check(lib().portal_mlp_predict(self._h, _p(X, P_F), X.shape[0], _p(Y, P_F)))
+        return Y
 
 
 def wigner3j(tj1, tj2, tj3, tm1, tm2, tm3) -> float:

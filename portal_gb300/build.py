@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libportal_gb300.so")
-SOURCES = ["ctx.cu", "rf.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "wigner.cpp"]
+SOURCES = ["ctx.cu", "rf.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "mlp.cu", "warmstart.cu", "wigner.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -74,7 +74,11 @@ def build_apps() -> list:
         exe = os.path.join(OUT, prog + ".x")
         deps = [src, io_src, os.path.join(APPS, "portal_io.h"), LIB]
         if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
-            cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+            # no FMA contraction: the ingestion must round exactly as the
+            # reference's expressions (and the Python restatement) do on
+            # every architecture
+            cmd = [os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-std=c++17",
+                   "-I", os.path.join(ROOT, "include"),
                    "-I", APPS, src, io_src, "-o", exe, "-L", OUT, "-lportal_gb300", "-Wl,-rpath,$ORIGIN"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:

@@ -136,6 +136,38 @@ inline void timers_reset(portal_ctx *c) {
     for (int i = 0; i < T_NSLOT; i++) { c->t_ms[i] = 0.0; c->t_launch[i] = 0; }
 }
 
+// FP64 without FMA contraction, in the operation order of the oracle (the
+// reference's expressions evaluated left to right)
+__device__ __forceinline__ double dsum3sq(double x, double y, double z) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+__device__ __forceinline__ double ddot3(double ax, double ay, double az, double bx, double by, double bz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+
+// Distance from node position p to the unit sphere along d: pos_quadratic
+// (miscellaneous.f90:1078-1098) with the arguments check_neigh_fast forms
+// for trace_out's first step (:1033), norm2(d)**2, 2 p.d, norm2(p)**2 - 1.
+// Evaluated without contraction so that the sign of |p|^2 - 1 -- which, for
+// the outermost node of a cloud (|p| = 1 to the last bit after the
+// normalisation by r_max), decides whether its inward rays leave the sphere
+// at once -- is the same as in the FP64 restatement.  0 where the
+// discriminant is not positive (the reference leaves delta_x unset there).
+__device__ __forceinline__ double sphere_exit(double px, double py, double pz, double dx, double dy,
+                                              double dz) {
+    const double nd = __dsqrt_rn(dsum3sq(dx, dy, dz));
+    const double a = __dmul_rn(nd, nd);
+    const double b = __dmul_rn(2.0, ddot3(px, py, pz, dx, dy, dz));
+    const double np = __dsqrt_rn(dsum3sq(px, py, pz));
+    const double c = __dsub_rn(__dmul_rn(np, np), 1.0);
+    const double dis = __dsub_rn(__dmul_rn(b, b), __dmul_rn(__dmul_rn(4.0, a), c));
+    if (!(dis > 0.0)) return 0.0;
+    const double sq = __dsqrt_rn(dis);
+    const double x1 = __ddiv_rn(__dadd_rn(-b, sq), __dmul_rn(2.0, a));
+    const double x2 = __ddiv_rn(__dsub_rn(-b, sq), __dmul_rn(2.0, a));
+    return (x2 > 0.0) ? x2 : x1;
+}
+
 // host: Gauss-Legendre rule on (-1,1), ascending knots (Newton iteration on
 // the three-term recurrence, long double)
 void gauss_legendre(int n, double *x, double *w);

@@ -180,16 +180,17 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
         if (p < npix) {
             const int ia = p / a.npx - a.im_pix, ib = p % a.npx - a.im_pix;
             const double x = ia * a.im_size / a.im_pix, y = ib * a.im_size / a.im_pix;
-            const double z0 = -1.0 * sqrt(1.0 - x * x - y * y);
+            // the oracle's FP64 arithmetic, without FMA contraction, throughout the march
+            const double z0 = -1.0 * __dsqrt_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(x, x)), __dmul_rn(y, y)));
             int2 *dl = wbase + (size_t)lane * a.n_depth;
             // nearest node (raytrace.f90:126-134; strict <, so the lowest index wins)
             int c = -1;
-            double best = 1e300;
+            double best = 10.0;  // rsave = 10 (raytrace.f90:126)
             for (int i = 0; i < a.N; i++) {
                 const double dx0 = x - a.xyz[3 * (size_t)i], dy0 = y - a.xyz[3 * (size_t)i + 1],
                              dz0 = z0 - a.xyz[3 * (size_t)i + 2];
-                const double r2 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0;
-                if (r2 < best) { best = r2; c = i; }
+                const double r = __dsqrt_rn(dsum3sq(dx0, dy0, dz0));  // norm2(start - X)
+                if (r < best) { best = r; c = i; }
             }
             if (c < 0) st = 3;  // start point outside the unit sphere (NaN)
             double z = z0;
@@ -220,20 +221,20 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 while (!done && !changed) {
                     z = z + a.dx;
                     k++;
-                    const bool exited = sqrt(x * x + y * y + z * z) > 1.0;
+                    const bool exited = __dsqrt_rn(dsum3sq(x, y, z)) > 1.0;  // norm2(X_phot) > 1
                     if (exited) {
                         if (nc >= a.n_depth) { st = 1; break; }
                         dl[nc++] = make_int2(c, k);
                         done = true;
                     }
                     // check_neigh miscellaneous.f90:1-46
-                    double d0 = (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz);
+                    double d0 = dsum3sq(x - cx, y - cy, z - cz);
                     int nn = c;
                     for (int j = 0; j < deg; j++) {
                         const int nb = a.idx[o + j];
                         const double ex = x - a.xyz[3 * (size_t)nb], ey = y - a.xyz[3 * (size_t)nb + 1],
                                      ez = z - a.xyz[3 * (size_t)nb + 2];
-                        const double dd = ex * ex + ey * ey + ez * ez;
+                        const double dd = dsum3sq(ex, ey, ez);
                         if (dd < d0) { d0 = dd; nn = nb; }
                     }
                     if (nn != c) {

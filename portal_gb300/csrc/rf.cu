@@ -30,7 +30,8 @@
 //                       over channels, lines looped in registers, cell
 //                       records staged in shared memory 32 cells at a time;
 //                   (4) the profile-weighted channel sum (warp reduction)
-//                       and the FP64 accumulation of J^0_0 and J^2_0.
+//                       and the compensated accumulation of J^0_0, J^2_0
+//                       over directions (fixed order: deterministic).
 #include <cmath>
 #include <cstdlib>
 
@@ -73,6 +74,20 @@ struct RFArgs {
     int *status;
     int2 *walk;
     unsigned long long *counters;
+};
+
+// Compensated (Kahan) FP32 sum: J of one node is a sum of a few hundred ray
+// contributions; the compensation keeps it to ~1e-7 of the sum of magnitudes
+// without the FP64 pipe.
+struct KahanF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
 __device__ __forceinline__ float ex2(float x) {
@@ -144,7 +159,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
         if (lane == 0) node = (int)atomicAdd(&a.counters[0], 1ULL);
         node = __shfl_sync(FULL, node, 0);
         if (node >= a.bulk) break;
-        double acc0a = 0.0, acc0b = 0.0, acc2a = 0.0, acc2b = 0.0;  // lines lane, lane+32
+        KahanF acc0a, acc0b, acc2a, acc2b;  // lines lane and lane+32, compensated FP32
         int st = 0;
         if (a.ab[node] > 0.0) {
             if (lane == 0) {
@@ -178,16 +193,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                     const double dx = mu * f[0] + sth * (cph * f[6] + sph * f[3]);
                     const double dy = mu * f[1] + sth * (cph * f[7] + sph * f[4]);
                     const double dz = mu * f[2] + sth * (cph * f[8] + sph * f[5]);
-                    // pos_quadratic(|d|^2, 2 p.d, |p|^2 - 1) from the node
-                    const double aq = dx * dx + dy * dy + dz * dz;
-                    const double bq = 2.0 * (f[9] * dx + f[10] * dy + f[11] * dz);
-                    const double dis = bq * bq - 4.0 * aq * (f[12] - 1.0);
-                    double sexit = 0.0;
-                    if (dis > 0.0) {
-                        const double sq = sqrt(dis);
-                        const double x1 = (-bq + sq) / (2.0 * aq), x2 = (-bq - sq) / (2.0 * aq);
-                        sexit = (x2 > 0.0) ? x2 : x1;
-                    }
+                    const double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
                     int2 *wl = wbase + (size_t)lane * a.n_depth;
@@ -245,7 +251,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                     const int2 *wl = wbase + (size_t)rr * a.n_depth;
                     const float4 d4 = B.dir[rr];
                     const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
-                    const double wgt = dr[4], wgt2 = dr[5];
+                    const float wgt = (float)dr[4], wgt2 = (float)dr[5];
                     nseg += (unsigned long long)Kr;
                     const int2 w0 = wl[0];
                     for (int l0 = 0; l0 < a.L; l0 += NLG) {
@@ -380,11 +386,11 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                             const int line = l0 + l;
                             if (line < a.L && (line & 31) == lane) {
                                 if (line < 32) {
-                                    acc0a += wgt * (double)v;
-                                    acc2a += wgt2 * (double)v;
+                                    acc0a.add(wgt * v);
+                                    acc2a.add(wgt2 * v);
                                 } else {
-                                    acc0b += wgt * (double)v;
-                                    acc2b += wgt2 * (double)v;
+                                    acc0b.add(wgt * v);
+                                    acc2b.add(wgt2 * v);
                                 }
                             }
                         }
@@ -394,12 +400,12 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
             }
         }
         if (lane < a.L) {
-            a.J0[(size_t)node * a.L + lane] = (st == 0) ? acc0a : 0.0;
-            a.J2[(size_t)node * a.L + lane] = (st == 0) ? acc2a : 0.0;
+            a.J0[(size_t)node * a.L + lane] = (st == 0) ? acc0a.value() : 0.0;
+            a.J2[(size_t)node * a.L + lane] = (st == 0) ? acc2a.value() : 0.0;
         }
         if (lane + 32 < a.L) {
-            a.J0[(size_t)node * a.L + lane + 32] = (st == 0) ? acc0b : 0.0;
-            a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b : 0.0;
+            a.J0[(size_t)node * a.L + lane + 32] = (st == 0) ? acc0b.value() : 0.0;
+            a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b.value() : 0.0;
         }
         if (lane == 0) a.status[node] = st;
         __syncwarp();

@@ -134,15 +134,7 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
                     const double dx = dr[0] * bx + dr[1] * (dr[2] * wx + dr[3] * xx);
                     const double dy = dr[0] * by + dr[1] * (dr[2] * wy + dr[3] * xy);
                     const double dz = dr[0] * bz + dr[1] * (dr[2] * wz + dr[3] * xz);
-                    const double aq = dx * dx + dy * dy + dz * dz;
-                    const double bq = 2.0 * (px * dx + py * dy + pz * dz);
-                    const double dis = bq * bq - 4.0 * aq * (px * px + py * py + pz * pz - 1.0);
-                    double sexit = 0.0;
-                    if (dis > 0.0) {
-                        const double sq = sqrt(dis);
-                        const double x1 = (-bq + sq) / (2.0 * aq), x2 = (-bq - sq) / (2.0 * aq);
-                        sexit = (x2 > 0.0) ? x2 : x1;
-                    }
+                    const double sexit = sphere_exit(px, py, pz, dx, dy, dz);
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     s_dir[wib][lane] = make_float4(fdx, fdy, fdz, vnx * fdx + vny * fdy + vnz * fdz);
                     int2 *wl = wbase + (size_t)lane * a.n_depth;

@@ -323,6 +323,81 @@ def ingest(raw: dict, mol: Molecule, off, idx, bvec, bulk_node_num: int, tets=No
                  raw=raw if keep_raw else None)
 
 
+def gaussian_field(rng, n: int, slope: float = -11.0 / 3.0, components: int = 1) -> np.ndarray:
+    """Periodic Gaussian random field on an n^3 grid with power spectrum
+    P(k) ~ k^slope, zero mean, unit rms per component; shape (components, n, n, n)."""
+    k = np.fft.fftfreq(n) * n
+    kx, ky, kz = np.meshgrid(k, k, k, indexing="ij")
+    kk = np.sqrt(kx * kx + ky * ky + kz * kz)
+    amp = np.zeros_like(kk)
+    amp[kk > 0] = kk[kk > 0] ** (slope / 2.0)
+    out = np.empty((components, n, n, n))
+    for c in range(components):
+        w = np.fft.fftn(rng.normal(size=(n, n, n)))
+        f = np.fft.ifftn(w * amp).real
+        f -= f.mean()
+        out[c] = f / f.std()
+    return out
+
+
+def _trilinear(field: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """Periodic trilinear interpolation of field (C, n, n, n) at points u in
+    [0, 1)^3 (shape (M, 3)); returns (M, C)."""
+    n = field.shape[1]
+    g = u * n
+    i0 = np.floor(g).astype(np.int64)
+    f = g - i0
+    out = np.zeros((u.shape[0], field.shape[0]))
+    for dx in (0, 1):
+        wx = f[:, 0] if dx else 1 - f[:, 0]
+        for dy in (0, 1):
+            wy = f[:, 1] if dy else 1 - f[:, 1]
+            for dz in (0, 1):
+                wz = f[:, 2] if dz else 1 - f[:, 2]
+                ix = (i0[:, 0] + dx) % n
+                iy = (i0[:, 1] + dy) % n
+                iz = (i0[:, 2] + dz) % n
+                out += (wx * wy * wz)[:, None] * field[:, ix, iy, iz].T
+    return out
+
+
+def turbulent_cube(n_points: int, seed: int, mol: Molecule, *, grid: int = 64, sigma_ln: float = 1.5,
+                   n_mean_cm3: float = 1e4, v_rms: float = 1.0e3, T: float = 20.0, abundance: float = 1e-4,
+                   micro_turb: float = 200.0, size_pc: float = 1.0, keep_raw: bool = False) -> Cloud:
+    """The turbulent cloud of the 1M-point configuration: points uniform in a
+    cube of side size_pc; ln(density) a k^-11/3 Gaussian random field with
+    sigma_ln, scaled to mean n_mean_cm3; velocity a k^-11/3 Gaussian random
+    field with v_rms (3D); field = unit mean along x plus an equal-rms
+    turbulent part with the same spectrum.  The periodic fields are sampled
+    trilinearly; the reference's domain is the unit sphere around the
+    points (eat_lime.f90:269-279), so the cube is treated as non-periodic."""
+    from scipy.spatial import Delaunay
+
+    PC = 3.0856775814913673e16
+    rng = np.random.default_rng(seed)
+    u = rng.random((n_points, 3))
+    pos_m = (u - 0.5) * size_pc * PC
+    lnrho = gaussian_field(rng, grid)
+    vel_f = gaussian_field(rng, grid, components=3)
+    b_f = gaussian_field(rng, grid, components=3)
+    s = _trilinear(lnrho, u)[:, 0] * sigma_ln
+    n_h2 = np.exp(s)
+    n_h2 *= n_mean_cm3 / n_h2.mean()
+    n_h2 *= 1e6                                                   # m^-3
+    vel = _trilinear(vel_f, u) * (v_rms / math.sqrt(3.0))
+    bt = _trilinear(b_f, u) / math.sqrt(3.0)
+    bvec = bt + np.array([1.0, 0.0, 0.0])
+    bvec /= np.linalg.norm(bvec, axis=1, keepdims=True)
+    tri = Delaunay(pos_m)
+    tets = tri.simplices.astype(np.int32)
+    off, idx = neighbours_from_tets(tets, n_points)
+    Tk = np.full(n_points, float(T))
+    raw = dict(pos_m=pos_m, vel=vel, n_h2=n_h2, t_kin=Tk, t_dust=Tk.copy(), b=np.full(n_points, micro_turb),
+               ab=np.full(n_points, abundance), gas_ii_dust=np.zeros(n_points), frac=lte_fractions(mol, Tk))
+    return ingest(raw, mol, off, idx, bvec, bulk_node_num=n_points, tets=tets if keep_raw else None,
+                  keep_raw=keep_raw)
+
+
 def gauge_vector(seed: int) -> tuple:
     """main_para.f90:172-176 draws three uniform numbers and normalises
     them; here the draw is seeded so both paths share it."""
@@ -354,6 +429,11 @@ def config_cloud(name: str, n_points: int | None = None):
         n = n_points or 262144
         cloud = power_law_sphere(n, 1, mol, t_law="loglinear", b_random=0.3)
         rc = RunConfig(nth=24, nph=24, nvel=64, kmax=6, gvec=gauge_vector(1))
+    elif name == "cfg4":
+        mol = linear_rotor(20)
+        n = n_points or 1048576
+        cloud = turbulent_cube(n, 4, mol, grid=128 if n > 200000 else 64)
+        rc = RunConfig(nth=32, nph=32, nvel=64, kmax=2, gvec=gauge_vector(4))
     else:
         raise ValueError(f"unknown configuration {name!r}")
     return cloud, mol, rc
