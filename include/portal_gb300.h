@@ -112,6 +112,17 @@ int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const do
                            double dx, int n_depth, double *J0, double *J2, int *status,
                            long long *n_segments);
 
+/* portal_radiation_field plus the split of J^0_0 that the accelerated Lambda
+ * iteration uses (no reference counterpart): J_eff(r_num,N) the profile-
+ * averaged J^0_0 without the node's own line emission (the central cell's
+ * term S_line (1 - e^-tau) removed, ray_in inverse_rt.f90:320-339) and
+ * L_star(r_num,N) = dJ^0_0 / dS_line, the diagonal of the Lambda operator,
+ * so that J^0_0 = J_eff + L_star S_line.  A following portal_solve_se with
+ * J0 = J2 = NULL solves the preconditioned population equations. */
+int portal_radiation_field_split(portal_ctx *ctx, int nth, int nph, int nvel, const double *gvec,
+                                 double dx, int n_depth, double *J0, double *J2, double *J_eff,
+                                 double *L_star, int *status, long long *n_segments);
+
 /* Polarized statistical equilibrium of every bulk node: make_AC
  * (miscellaneous.f90:288-392) + get_rhovec (em_coefs.f90:115-201, with
  * setup_stateq pop_eqs.f90:361-653) + the packing of trace_node
@@ -133,12 +144,25 @@ int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J
  * (main_para.f90:210-257); iteration 1 from the cloud's populations is that
  * pass.  start_pops(N, 2*nlev) (pol_pops layout) replaces the starting
  * populations of the bulk nodes by those of its rho^0_0 (a warm start), or
- * NULL to start from the cloud's.  Outputs (any may be NULL): the last
+ * NULL to start from the cloud's.  ng_period 0 iterates plainly; ng_period
+ * >= 3 adds Ng acceleration (no reference counterpart): after every
+ * ng_period passes the state moves to the order-2 Ng extrapolation of the
+ * last four iterates of rho^0_0 (weights 1/rho^2), clipped to positive
+ * values and renormalised per node; convergence is still judged by the
+ * change of one plain pass.  local_operator != 0 (no reference counterpart)
+ * makes the passes accelerated Lambda iterations: the radiation-field
+ * kernel also splits J^0_0 = J_eff + L* S at each node's own cell (L* the
+ * diagonal of the Lambda operator) and the SE's population equations take
+ * the preconditioned net rates (B_lu n_l - B_ul n_u) J_eff - A (1 - L*) n_u
+ * (Rybicki & Hummer 1991); the fixed point is the plain one, and once an
+ * accelerated pass changes rho^0_0 by less than tol a plain pass follows and
+ * decides convergence.  Outputs (any may be NULL): the last
  * pol_pops(N, 2*nlev), the final lev_p(nlev, N) (they also become the
  * context's populations), the number of passes, residuals(max_iter) per
  * pass, and the total ray segments walked. */
 int portal_lambda_iterate(portal_ctx *ctx, int nth, int nph, int nvel, const double *gvec, double dx,
-                          int n_depth, int kmax, double tol, int max_iter, const double *start_pops,
+                          int n_depth, int kmax, double tol, int max_iter, int ng_period,
+                          int local_operator, const double *start_pops,
                           double *pol_pops, double *lev_p_out, int *iterations, double *residuals,
                           long long *n_segments);
 

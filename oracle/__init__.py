@@ -120,6 +120,19 @@ class OracleProblem:
                                           nthreads, _p(J0), _p(J2), _p(st, P_I), C.byref(nseg))
         return J0, J2, st, int(nseg.value), nfail
 
+    def radiation_field_split(self, rc, node_lo=1, node_hi=None, nthreads=0):
+        """J0, J2, J_eff, L* of shape (N, r_num) and the per-node status."""
+        N, R = self.cloud.node_num, self.mol.r_num
+        node_hi = self.cloud.bulk_node_num if node_hi is None else node_hi
+        J0, J2, JE, LS = (np.zeros((N, R)) for _ in range(4))
+        st = np.zeros(N, dtype=np.int32)
+        nseg = C.c_int64(0)
+        g = np.ascontiguousarray(rc.gvec, dtype=np.float64)
+        lib().orc_radiation_field_split(C.byref(self.c), C.byref(self.m), rc.nth, rc.nph, rc.nvel, _p(g),
+                                        C.c_double(rc.dx), rc.n_depth, node_lo, node_hi, nthreads, _p(J0),
+                                        _p(J2), _p(JE), _p(LS), _p(st, P_I), C.byref(nseg))
+        return J0, J2, JE, LS, st
+
     def solve_se(self, kmax, J0, J2, node_lo=1, node_hi=None, nthreads=0, rates=False):
         """pol_pops as an (N, 2*nlev) array (reference pol_pops(node,:))."""
         N, nlev = self.cloud.node_num, self.mol.nlev

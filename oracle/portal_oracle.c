@@ -315,11 +315,16 @@ int orc_trace_out(const orc_cloud *c, int node, const double *dir, double dx, in
 }
 
 /* ray_in inverse_rt.f90:217-344 (gathered cell lists passed as in the
- * call at inverse_rt.f90:121-124) */
+ * call at inverse_rt.f90:121-124).  When I_eff / lam are given (an
+ * extension without reference counterpart: the split of the accelerated
+ * Lambda iteration), the channel sum is also formed without the node's own
+ * line emission, sum phi (I e^-tau + S_dust (1 - e^-tau)) dv, and for the
+ * derivative with respect to the node's line source function,
+ * sum phi (kv phi / kappa) (1 - e^-tau) dv. */
 static double ray_in(const orc_cloud *c, const int *depth_list, int node_count, int node,
                      double vel_node, const double *vel_ray, int l1, int l2, double kd,
                      int nvel, double dx, double nu0, double Aji, double Bij, int g1, int g2,
-                     double I_in)
+                     double I_in, double *I_eff, double *lam)
 {
     const int nlev = c->nlev;
     double c1 = 2.2102191e-42 * nu0;   /* h nu0 / c      */
@@ -330,7 +335,7 @@ static double ray_in(const orc_cloud *c, const int *depth_list, int node_count, 
     double p2_node = c->lev_p[(size_t)nlev * (node - 1) + (l2 - 1)];
     double dust_node = c->dust_p[node - 1];
     double bb_node = c->t_dust[node - 1];
-    double I_tot = 0.0;
+    double I_tot = 0.0, Ie_tot = 0.0, lam_tot = 0.0;
     double d_v = 2.0 * temp_node / nvel;
     double spi = sqrt(acos(-1.0));
     double kv, ev, I_bb, alpha_v, j_v, phi_v, tau_v, Sv, e_tau, I_out;
@@ -372,15 +377,21 @@ static double ray_in(const orc_cloud *c, const int *depth_list, int node_count, 
         e_tau = exp(-tau_v);
         I_out = Iv * e_tau + Sv * (1.0 - e_tau);
         I_tot = I_tot + phi_v0 * I_out * d_v;
+        if (I_eff) {
+            double kap = kv * phi_v + alpha_v;
+            Ie_tot += phi_v0 * (Iv * e_tau + (j_v / kap) * (1.0 - e_tau)) * d_v;
+            lam_tot += phi_v0 * (kv * phi_v / kap) * (1.0 - e_tau) * d_v;
+        }
     }
+    if (I_eff) { *I_eff = Ie_tot; *lam = lam_tot; }
     return I_tot;
 }
 
 /* inverse_rt inverse_rt.f90:1-137 (star_mode = 0).  dx here is the
  * trace step (main_para.f90:135); ray_in receives tx*dx. */
-int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const double *xth,
-                   int n_sphere, const double *gvec, int nvel, double dx, int n_depth,
-                   double *J0, double *J2, int64_t *n_segments)
+static int inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const double *xth,
+                      int n_sphere, const double *gvec, int nvel, double dx, int n_depth,
+                      double *J0, double *J2, double *JE, double *LS, int64_t *n_segments)
 {
     int t_num = m->r_num;
     int *depth_list = (int *)malloc(sizeof(int) * 2 * (size_t)(n_depth + 2));
@@ -390,6 +401,8 @@ int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const do
     int st = ORC_OK;
     int64_t nseg = 0;
     for (int k = 0; k < t_num; k++) { J0[k] = 0.0; J2[k] = 0.0; }
+    if (JE)
+        for (int k = 0; k < t_num; k++) { JE[k] = 0.0; LS[k] = 0.0; }
     for (int i = 0; i < n_sphere; i++) {
         double mu = xth[3 * i], ph = xth[3 * i + 1], w = xth[3 * i + 2];
         double c_in = (3.0 * mu * mu - 1.0) / 2.0;
@@ -408,11 +421,17 @@ int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const do
             double nu0 = m->nu[k];
             int l1 = m->r_trans[2 * k], l2 = m->r_trans[2 * k + 1];
             double I_in = orc_black_body(2.73, nu0);
+            double Ie = 0.0, lam = 0.0;
             double I_out = ray_in(c, depth_list, node_count, node, vel_node, vel_ray, l1, l2,
                                   m->kd_v[k], nvel, c->tx * dx, nu0, m->A[k], m->Bij[k],
-                                  2 * m->j_lev[l1 - 1] + 1, 2 * m->j_lev[l2 - 1] + 1, I_in);
+                                  2 * m->j_lev[l1 - 1] + 1, 2 * m->j_lev[l2 - 1] + 1, I_in,
+                                  JE ? &Ie : NULL, JE ? &lam : NULL);
             J0[k] = J0[k] + I_out * w;
             J2[k] = J2[k] + I_out * w * c_in / sqrt(2.0);
+            if (JE) {
+                JE[k] += Ie * w;
+                LS[k] += lam * w;
+            }
         }
     }
     free(depth_list);
@@ -421,12 +440,20 @@ int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const do
     return st;
 }
 
+int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const double *xth,
+                   int n_sphere, const double *gvec, int nvel, double dx, int n_depth,
+                   double *J0, double *J2, int64_t *n_segments)
+{
+    return inverse_rt(c, m, node, xth, n_sphere, gvec, nvel, dx, n_depth, J0, J2, NULL, NULL,
+                      n_segments);
+}
+
 /* The node loop main_para.f90:210-257 (star_mod = 0 branch), radiation
  * field half of trace_node (main_sub.f90:82-84). */
-int orc_radiation_field(const orc_cloud *c, const orc_molecule *m, int nth, int nph, int nvel,
-                        const double *gvec, double dx, int n_depth, int node_lo, int node_hi,
-                        int nthreads, double *J0, double *J2, int *status,
-                        int64_t *n_segments)
+int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth, int nph,
+                              int nvel, const double *gvec, double dx, int n_depth, int node_lo,
+                              int node_hi, int nthreads, double *J0, double *J2, double *JE,
+                              double *LS, int *status, int64_t *n_segments)
 {
     double *xth = (double *)malloc(sizeof(double) * 3 * (size_t)nth * nph);
     int n_sphere = orc_legendre_all(nth, nph, xth);
@@ -442,12 +469,16 @@ int orc_radiation_field(const orc_cloud *c, const orc_molecule *m, int nth, int 
     for (int node = node_lo; node <= node_hi; node++) {
         double *j0 = J0 + (size_t)t_num * (node - 1);
         double *j2 = J2 + (size_t)t_num * (node - 1);
+        double *je = JE ? JE + (size_t)t_num * (node - 1) : NULL;
+        double *ls = JE ? LS + (size_t)t_num * (node - 1) : NULL;
         int st = ORC_OK;
         int64_t ns = 0;
         if (c->ab_all[node - 1] > 0.0) {
-            st = orc_inverse_rt(c, m, node, xth, n_sphere, gvec, nvel, dx, n_depth, j0, j2, &ns);
+            st = inverse_rt(c, m, node, xth, n_sphere, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
         } else {
             for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
+            if (je)
+                for (int k = 0; k < t_num; k++) { je[k] = 0.0; ls[k] = 0.0; }
         }
         if (status) status[node - 1] = st;
         if (st != ORC_OK) nfail++;
@@ -456,6 +487,15 @@ int orc_radiation_field(const orc_cloud *c, const orc_molecule *m, int nth, int 
     free(xth);
     if (n_segments) *n_segments = nseg;
     return nfail;
+}
+
+int orc_radiation_field(const orc_cloud *c, const orc_molecule *m, int nth, int nph, int nvel,
+                        const double *gvec, double dx, int n_depth, int node_lo, int node_hi,
+                        int nthreads, double *J0, double *J2, int *status,
+                        int64_t *n_segments)
+{
+    return orc_radiation_field_split(c, m, nth, nph, nvel, gvec, dx, n_depth, node_lo, node_hi,
+                                     nthreads, J0, J2, NULL, NULL, status, n_segments);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -96,6 +96,14 @@ int orc_radiation_field(const orc_cloud *c, const orc_molecule *m, int nth, int 
                         int nvel, const double *gvec, double dx, int n_depth,
                         int node_lo, int node_hi, int nthreads, double *J0,
                         double *J2, int *status, int64_t *n_segments);
+/* The same, with the split of the accelerated Lambda iteration (no
+ * reference counterpart): JE(r_num,N) J^0_0 without the node's own line
+ * emission, LS(r_num,N) its derivative with respect to the node's line
+ * source function (the diagonal of the Lambda operator). */
+int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth, int nph,
+                              int nvel, const double *gvec, double dx, int n_depth, int node_lo,
+                              int node_hi, int nthreads, double *J0, double *J2, double *JE,
+                              double *LS, int *status, int64_t *n_segments);
 
 /* ---- statistical equilibrium ---- */
 int orc_setup_count_array(const int *j_lev, int nlev, int kmax, int *count_array);

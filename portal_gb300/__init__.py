@@ -30,7 +30,7 @@ KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_w
 EXPORTS = (
     "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
     "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
-    "portal_radiation_field", "portal_solve_se", "portal_image", "portal_last_kernel_times",
+    "portal_radiation_field", "portal_radiation_field_split", "portal_solve_se", "portal_image", "portal_last_kernel_times",
     "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
     "portal_radiation_field_static", "portal_radiation_field_static_limits",
@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
     L.portal_set_populations.argtypes = [C.c_void_p, P_D]
     L.portal_radiation_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int,
                                          P_D, P_D, P_I, C.POINTER(C.c_longlong)]
+    L.portal_radiation_field_split.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int,
+                                               P_D, P_D, P_D, P_D, P_I, C.POINTER(C.c_longlong)]
     L.portal_solve_se.argtypes = [C.c_void_p, C.c_int, P_D, P_D, P_D, P_D, P_D, P_I]
     L.portal_last_kernel_times.argtypes = [C.c_void_p, P_D, P_I, C.c_int]
     L.portal_set_stream.argtypes = [C.c_void_p, C.c_void_p]
@@ -88,7 +90,7 @@ def lib() -> C.CDLL:
         [V, C.c_int, C.c_int, C.c_int] + [V] * 8 + [C.c_int, V, V, C.c_double] +
         [P_I, C.c_int, P_I, P_D, P_D, P_D, P_D, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int] + [V] * 3)
     L.portal_lambda_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int, C.c_int,
-                                        C.c_double, C.c_int, P_D, P_D, P_D, P_I, P_D, C.POINTER(C.c_longlong)]
+                                        C.c_double, C.c_int, C.c_int, C.c_int, P_D, P_D, P_D, P_I, P_D, C.POINTER(C.c_longlong)]
     L.portal_radiation_field_static_limits.restype = None
     L.portal_radiation_field_static_limits.argtypes = [P_I, P_I, P_I, P_I, C.POINTER(C.c_longlong)]
     P_F = C.POINTER(C.c_float)
@@ -206,6 +208,18 @@ class Context:
                                                  rc.n_depth, _p(J0), _p(J2), _p(st, P_I), C.byref(nseg)))
         return J0, J2, st, int(nseg.value)
 
+    def radiation_field_split(self, rc):
+        """J0, J2, J_eff, L* as (N, r_num) arrays and the status; the split
+        stays on the device for a following solve_se (preconditioned SE)."""
+        g = _f64(rc.gvec)
+        nseg = C.c_longlong(0)
+        J0, J2, JE, LS = (np.zeros((self.N, self.r_num)) for _ in range(4))
+        st = np.zeros(self.N, dtype=np.int32)
+        self._check(lib().portal_radiation_field_split(self._h, rc.nth, rc.nph, rc.nvel, _p(g), float(rc.dx),
+                                                       rc.n_depth, _p(J0), _p(J2), _p(JE), _p(LS), _p(st, P_I),
+                                                       C.byref(nseg)))
+        return J0, J2, JE, LS, st
+
     def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False, out=None):
         """pol_pops as (N, 2*nlev) (reference pol_pops(node,:)), status.
         out: a float64 (2*nlev, N) C-contiguous buffer (the reference's
@@ -243,9 +257,12 @@ class Context:
                                        n_depth_rt, *ptrs, _p(st, P_I)))
         return out, st
 
-    def lambda_iterate(self, rc, tol=1e-6, max_iter=100, start_pops=None, fetch=True):
-        """Plain Lambda iteration.  Returns (pol_pops (N, 2 nlev), lev_p
-        (N, nlev), passes, residual per pass, segments)."""
+    def lambda_iterate(self, rc, tol=1e-6, max_iter=100, start_pops=None, fetch=True, ng_period=0,
+                       local_operator=False):
+        """Lambda iteration: plain, with Ng extrapolation every ng_period
+        passes, and/or with the local (diagonal) Lambda operator.  Returns
+        (pol_pops (N, 2 nlev), lev_p (N, nlev), passes, residual per pass,
+        segments)."""
         pp = np.zeros((2 * self.nlev, self.N)) if fetch else None
         lp = np.zeros((self.N, self.nlev)) if fetch else None
         res = np.zeros(max_iter)
@@ -254,7 +271,9 @@ class Context:
         sp = None if start_pops is None else np.ascontiguousarray(np.asarray(start_pops, dtype=np.float64).T)
         g = _f64(rc.gvec)
         self._check(lib().portal_lambda_iterate(self._h, rc.nth, rc.nph, rc.nvel, _p(g), float(rc.dx), rc.n_depth,
-                                                rc.kmax, float(tol), int(max_iter), _p(sp), _p(pp), _p(lp),
+                                                rc.kmax, float(tol), int(max_iter), int(ng_period),
+                                                int(bool(local_operator)), _p(sp),
+                                                _p(pp), _p(lp),
                                                 C.byref(it), _p(res), C.byref(nseg)))
         n = it.value
         return (None if pp is None else pp.T.copy()), lp, n, res[:n].copy(), int(nseg.value)

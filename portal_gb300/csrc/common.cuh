@@ -77,6 +77,8 @@ struct portal_ctx {
     // ---- derived / results ----
     portal::DevBuf<float4> ltab;      // (r_num,N) line table
     portal::DevBuf<double> J0, J2;    // (r_num,N)
+    portal::DevBuf<double> JE, LS;    // (r_num,N) J0 without the node's own emission, local operator L*
+    bool ali_valid = false;           // JE / LS belong to the current J0 (the SE splits the field)
     portal::DevBuf<int> status;       // N
     portal::DevBuf<int2> walk;        // per-warp walk scratch
     portal::DevBuf<unsigned long long> counters;  // [0] work, [1] segments, [2..] misc

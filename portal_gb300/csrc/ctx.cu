@@ -118,6 +118,7 @@ extern "C" int portal_set_molecule(portal_ctx *c, int nlev, const int *j_lev, co
     c->have_mol = true;
     c->se_kmax = -1;  // SE program must be rebuilt
     c->j_valid = false;
+    c->ali_valid = false;
     return PORTAL_OK;
 }
 
@@ -189,6 +190,7 @@ extern "C" int portal_set_cloud(portal_ctx *c, int N, int bulk, int nlev, const 
     int nnz = off[N];
     c->have_cloud = false;
     c->j_valid = false;
+    c->ali_valid = false;
     if (c->pos64.reserve(3 * (size_t)N) || c->bvec64.reserve(3 * (size_t)N) ||
         c->cellv.reserve(N) || c->nb_off.reserve(N + 1) || c->nb_idx.reserve(nnz) ||
         c->edge.reserve(nnz) || c->levp.reserve((size_t)nlev * N) || c->b64.reserve(N) ||
@@ -248,6 +250,7 @@ extern "C" int portal_set_populations(portal_ctx *c, const double *lev_p) {
                               cudaMemcpyHostToDevice, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
     c->j_valid = false;
+    c->ali_valid = false;
     return PORTAL_OK;
 }
 

@@ -32,6 +32,12 @@
 //                   (4) the profile-weighted channel sum (warp reduction)
 //                       and the compensated accumulation of J^0_0, J^2_0
 //                       over directions (fixed order: deterministic).
+//                  On request it also splits J^0_0 = J_eff + L* S_line at
+//                  the central cell: J_eff the field without the node's own
+//                  line emission, L* = dJ^0_0/dS_line the diagonal of the
+//                  Lambda operator (what the node's own cell contributes per
+//                  unit source function) -- the inputs of the preconditioned
+//                  SE of the accelerated Lambda iteration.
 #include <cmath>
 #include <cstdlib>
 
@@ -71,6 +77,7 @@ struct RFArgs {
     const float *__restrict__ chw;    // (nch) exp(-q0^2) * 2/(sqrt(pi) nvel)
     double gx, gy, gz;
     double *J0, *J2;
+    double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
     int *status;
     int2 *walk;
     unsigned long long *counters;
@@ -160,6 +167,8 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
         node = __shfl_sync(FULL, node, 0);
         if (node >= a.bulk) break;
         KahanF acc0a, acc0b, acc2a, acc2b;  // lines lane and lane+32, compensated FP32
+        KahanF accEa, accEb, accLa, accLb;  // J_eff and L* of the same lines (split field only)
+        const bool split = (a.JE != nullptr);
         int st = 0;
         if (a.ab[node] > 0.0) {
             if (lane == 0) {
@@ -350,10 +359,12 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                         // central cell (inverse_rt.f90:320-339): no gate, profile at
                         // the node's own b, then the weighted channel sum
                         const float fst0 = (float)w0.y;
-                        float part[NLG];
+                        float part[NLG], pe[NLG], pl[NLG];
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
                             part[l] = 0.f;
+                            pe[l] = 0.f;
+                            pl[l] = 0.f;
                             if (l0 + l < a.L) {
                                 const float4 v = a.ltab[(size_t)node * a.L + l0 + l];
 #pragma unroll
@@ -362,11 +373,13 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                     if (ch < a.nch) {
                                         const float q0c = a.chq[ch];
                                         const float g0 = ex2(-q0c * q0c * LOG2E_F);
-                                        float tau, Sv;
+                                        float tau, Sv, lf = 1.f, Sd = 0.f;
                                         if (DUST) {
                                             const float kap = fmaf(v.x, g0, v.z);
                                             tau = kap * fst0;
                                             Sv = fmaf(v.y, g0, v.w) / kap;
+                                            lf = v.x * g0 / kap;   // line share of the opacity
+                                            Sd = v.w / kap;        // dust emission share of S
                                         } else {
                                             tau = v.x * g0 * fst0;
                                             Sv = v.y / v.x;
@@ -374,6 +387,10 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                         const float e = ex2(-tau * LOG2E_F);
                                         const float Io = fmaf(I[s2][l], e, Sv * (1.f - e));
                                         part[l] = fmaf(a.chw[ch], Io, part[l]);
+                                        if (split) {
+                                            pe[l] = fmaf(a.chw[ch], fmaf(I[s2][l], e, Sd * (1.f - e)), pe[l]);
+                                            pl[l] = fmaf(a.chw[ch], lf * (1.f - e), pl[l]);
+                                        }
                                     }
                                 }
                             }
@@ -394,6 +411,27 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                 }
                             }
                         }
+                        if (split) {
+#pragma unroll
+                            for (int l = 0; l < NLG; l++) {
+                                float ve = pe[l], vl = pl[l];
+#pragma unroll
+                                for (int o2 = 16; o2 >= 1; o2 >>= 1) {
+                                    ve += __shfl_xor_sync(FULL, ve, o2);
+                                    vl += __shfl_xor_sync(FULL, vl, o2);
+                                }
+                                const int line = l0 + l;
+                                if (line < a.L && (line & 31) == lane) {
+                                    if (line < 32) {
+                                        accEa.add(wgt * ve);
+                                        accLa.add(wgt * vl);
+                                    } else {
+                                        accEb.add(wgt * ve);
+                                        accLb.add(wgt * vl);
+                                    }
+                                }
+                            }
+                        }
                     }
                 }
                 __syncwarp();
@@ -406,6 +444,16 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
         if (lane + 32 < a.L) {
             a.J0[(size_t)node * a.L + lane + 32] = (st == 0) ? acc0b.value() : 0.0;
             a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b.value() : 0.0;
+        }
+        if (split) {
+            if (lane < a.L) {
+                a.JE[(size_t)node * a.L + lane] = (st == 0) ? accEa.value() : 0.0;
+                a.LS[(size_t)node * a.L + lane] = (st == 0) ? accLa.value() : 0.0;
+            }
+            if (lane + 32 < a.L) {
+                a.JE[(size_t)node * a.L + lane + 32] = (st == 0) ? accEb.value() : 0.0;
+                a.LS[(size_t)node * a.L + lane + 32] = (st == 0) ? accLb.value() : 0.0;
+            }
         }
         if (lane == 0) a.status[node] = st;
         __syncwarp();
@@ -483,9 +531,10 @@ int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
 
 namespace portal {
 
-// Runs the line table + radiation field on the device; J stays in c->J0/J2.
+// Runs the line table + radiation field on the device; J stays in c->J0/J2
+// (and the split field in c->JE/LS when `split`).
 int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
-                        int n_depth, long long *n_segments, int *n_failed) {
+                        int n_depth, long long *n_segments, int *n_failed, bool split) {
     if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
     if (c->nlev != (int)c->j_lev.size())
         return set_err(c, PORTAL_ERR_STATE, "cloud and molecule disagree on nlev");
@@ -531,6 +580,13 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     PCHECK(c, cudaMemsetAsync(c->J0.p, 0, (size_t)L * N * sizeof(double), c->stream));
     PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), c->stream));
     PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), c->stream));
+    c->ali_valid = false;
+    if (split) {
+        if (c->JE.reserve((size_t)L * N) || c->LS.reserve((size_t)L * N))
+            return set_err(c, PORTAL_ERR_NOMEM, "split-field buffers");
+        PCHECK(c, cudaMemsetAsync(c->JE.p, 0, (size_t)L * N * sizeof(double), c->stream));
+        PCHECK(c, cudaMemsetAsync(c->LS.p, 0, (size_t)L * N * sizeof(double), c->stream));
+    }
     // line table
     {
         long long tot = (long long)N * L;
@@ -548,6 +604,8 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     a.dirs = c->dirtab.p; a.chq = c->chtab.p; a.chw = c->chtab.p + nch;
     a.gx = gvec[0]; a.gy = gvec[1]; a.gz = gvec[2];
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
+    a.JE = split ? c->JE.p : nullptr;
+    a.LS = split ? c->LS.p : nullptr;
     a.walk = nullptr;
     if (nch <= 32) rc = dispatch_nlg<1>(c, a, n_depth);
     else if (nch <= 64) rc = dispatch_nlg<2>(c, a, n_depth);
@@ -564,21 +622,26 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     // failed nodes: count on the host from the status array only when asked
     if (n_failed) *n_failed = 0;
     c->j_valid = true;
+    c->ali_valid = split;
     return PORTAL_OK;
 }
 
 }  // namespace portal
 
-extern "C" int portal_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec,
-                                      double dx, int n_depth, double *J0, double *J2, int *status,
-                                      long long *n_segments) {
+namespace {
+
+int radiation_field_call(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
+                         int n_depth, double *J0, double *J2, double *JE, double *LS, bool split, int *status,
+                         long long *n_segments) {
     if (!c) return PORTAL_ERR_ARG;
     timers_reset(c);
-    int rc = portal::run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, n_segments, nullptr);
+    int rc = portal::run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, n_segments, nullptr, split);
     if (rc) return rc;
     const size_t LN = (size_t)c->r_num * c->N;
     if (J0) PCHECK(c, cudaMemcpyAsync(J0, c->J0.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (J2) PCHECK(c, cudaMemcpyAsync(J2, c->J2.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (split && JE) PCHECK(c, cudaMemcpyAsync(JE, c->JE.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (split && LS) PCHECK(c, cudaMemcpyAsync(LS, c->LS.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     std::vector<int> st_host;
     int *st = status;
     if (!st) { st_host.resize(c->N); st = st_host.data(); }
@@ -588,4 +651,20 @@ extern "C" int portal_radiation_field(portal_ctx *c, int nth, int nph, int nvel,
         if (st[i] & PORTAL_NODE_DEPTH)
             return set_err(c, PORTAL_ERR_DEPTH, "node_count > n_depth for node " + std::to_string(i + 1));
     return PORTAL_OK;
+}
+
+}  // namespace
+
+extern "C" int portal_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec,
+                                      double dx, int n_depth, double *J0, double *J2, int *status,
+                                      long long *n_segments) {
+    return radiation_field_call(c, nth, nph, nvel, gvec, dx, n_depth, J0, J2, nullptr, nullptr, false, status,
+                                n_segments);
+}
+
+extern "C" int portal_radiation_field_split(portal_ctx *c, int nth, int nph, int nvel, const double *gvec,
+                                            double dx, int n_depth, double *J0, double *J2, double *J_eff,
+                                            double *L_star, int *status, long long *n_segments) {
+    return radiation_field_call(c, nth, nph, nvel, gvec, dx, n_depth, J0, J2, J_eff, L_star, true, status,
+                                n_segments);
 }

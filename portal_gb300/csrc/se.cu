@@ -6,12 +6,21 @@
 // em_coefs.f90:115-201, setup_stateq pop_eqs.f90:361-653 and the coupling
 // constants pop_eqs.f90:1-359.
 //
-// Every entry of the SE matrix is a linear combination of five per-node,
+// Every entry of the SE matrix is a linear combination of seven per-node,
 // per-transition quantities
 //     f0 = B21 J0,  f1 = B21 J2,  f2 = A21,  f3 = C21 (n_H2, T),
-//     f4 = C21 exp(-h nu / k T)
+//     f4 = C21 exp(-h nu / k T),  f5 = B21 J0_eff,  f6 = A21 (1 - L*)
 // with node-independent coefficients built from the Wigner coupling
-// constants.  The host turns setup_stateq's loops into that program once per
+// constants.  f5 and f6 serve the couplings between K = 0 components
+// (populations) only.  Without a local operator J0_eff = J0 and L* = 0, so
+// they equal f0 and f2 exactly and the matrix is setup_stateq's.  With one
+// (the accelerated Lambda iteration) J0 = J0_eff + L* S is split into the
+// field of everything but the node's own emission and the node's own
+// contribution L* S, and the net radiative rates of the K = 0 equations,
+// (B_lu n_l - B_ul n_u) J0 - A n_u, become (B_lu n_l - B_ul n_u) J0_eff -
+// A (1 - L*) n_u (Rybicki & Hummer 1991, A&A 245, 171: the preconditioned
+// rate equations), still linear in the populations.  At the fixed point
+// (S unchanged) both forms are the same equations.  The host turns setup_stateq's loops into that program once per
 // (molecule, kmax): a CSR list over matrix entries of (feature, coefficient)
 // terms.  The kernel (one warp per node) evaluates the features, assembles
 // the matrix in shared memory (FP64), replaces row 1 by the normalisation
@@ -39,6 +48,8 @@ struct SEArgs {
     int N, bulk, c_dim, n_trans, nlev, L, c_temp, c_num, c_par, nent;
     const double *__restrict__ J0;
     const double *__restrict__ J2;
+    const double *__restrict__ JE;      // J0_eff (r_num, N) or null
+    const double *__restrict__ LS;      // L* (r_num, N) or null
     const double *__restrict__ h2;
     const double *__restrict__ tkin;
     const double *__restrict__ ab;
@@ -137,11 +148,13 @@ __device__ void warp_lu_solve(int n, const T *M, const int *piv, V *b, int lane)
 }
 
 // Dynamic shared memory per warp:
-//   A64 [n*n] double | feat [5*n_trans] double | x, r [n] double | d32 [n] float
+//   A64 [n*n] double | feat [NF*n_trans] double | x, r [n] double | d32 [n] float
 //   LU32 [n*n] float | scale [n] float | piv [n] int
+constexpr int NF = 7;  // features per transition
+
 __host__ __device__ inline size_t se_warp_bytes(int n, int n_trans) {
     size_t b = 0;
-    b += sizeof(double) * ((size_t)n * n + 5 * (size_t)n_trans + 2 * (size_t)n);
+    b += sizeof(double) * ((size_t)n * n + NF * (size_t)n_trans + 2 * (size_t)n);
     b += sizeof(float) * ((size_t)n * n + 2 * (size_t)n);
     b += sizeof(int) * (size_t)n;
     return (b + 15) & ~(size_t)15;
@@ -154,7 +167,7 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
     unsigned char *base = smem + se_warp_bytes(n, a.n_trans) * wib;
     double *A64 = (double *)base;
     double *feat = A64 + (size_t)n * n;
-    double *x = feat + 5 * (size_t)a.n_trans;
+    double *x = feat + NF * (size_t)a.n_trans;
     double *r = x + n;
     float *LU = (float *)(r + n);
     float *d32 = LU + (size_t)n * n;
@@ -168,10 +181,12 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
         for (int t = lane; t < a.n_trans; t += 32) {
             const int rr = a.tr_rad[t], cc = a.tr_col[t];
             const double B21 = a.tr_B21[t];
-            double j0 = 0.0, j2 = 0.0, C21 = 0.0;
+            double j0 = 0.0, j2 = 0.0, je = 0.0, ls = 0.0, C21 = 0.0;
             if (rr >= 0) {
                 j0 = a.J0[(size_t)node * a.L + rr];
                 j2 = a.J2[(size_t)node * a.L + rr];
+                je = a.JE ? a.JE[(size_t)node * a.L + rr] : j0;
+                ls = a.LS ? a.LS[(size_t)node * a.L + rr] : 0.0;
             }
             if (cc >= 0) {
                 // temperature interpolation (first bracket; below the table the
@@ -191,12 +206,14 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
                 }
                 C21 = cr * nH2 * 1e-6;
             }
-            double *f = feat + 5 * (size_t)t;
+            double *f = feat + NF * (size_t)t;
             f[0] = B21 * j0;
             f[1] = B21 * j2;
             f[2] = a.tr_A[t];
             f[3] = C21;
             f[4] = C21 * exp(-HK * a.tr_nu[t] / T);
+            f[5] = B21 * je;
+            f[6] = a.tr_A[t] * (1.0 - ls);
         }
         for (int i = lane; i < n * n; i += 32) A64[i] = 0.0;
         __syncwarp();
@@ -362,10 +379,16 @@ void build_program(const portal_ctx *c, int kmax, Program &P) {
         return cache[key] = std::make_pair(a0, a2);
     };
     const int n = P.c_dim;
+    std::vector<int> k_of(n, 0);  // K of each component
+    for (int i = 0; i < nlev; i++)
+        for (int k = 0; k <= std::min(2 * J[i], kmax); k += 2) k_of[P.count_array[i] + k / 2] = k;
     std::map<int, std::vector<std::pair<int, double>>> ent;  // pos -> terms
     auto add = [&](int c1, int c2, int t, int f, double coef) {
         auto &v = ent[c1 + n * c2];
-        if (coef != 0.0) v.push_back({5 * t + f, coef});
+        // couplings between K = 0 components take the split field (f5, f6)
+        const bool k00 = (k_of[c1] == 0 && k_of[c2] == 0);
+        const int ff = (k00 && f == 0) ? 5 : (k00 && f == 2) ? 6 : f;
+        if (coef != 0.0) v.push_back({NF * t + ff, coef});
     };
     auto touch = [&](int c1, int c2) { ent[c1 + n * c2]; };
     for (int i1 = 0; i1 < nlev; i1++) {
@@ -511,6 +534,8 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
     a.N = c->N; a.bulk = c->bulk; a.c_dim = n; a.n_trans = c->n_trans; a.nlev = c->nlev; a.L = c->r_num;
     a.c_temp = c->c_temp; a.c_num = c->c_num; a.c_par = c->c_par; a.nent = c->se_ni;
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.h2 = c->h2.p; a.tkin = c->tkin.p; a.ab = c->ab.p;
+    a.JE = c->ali_valid ? c->JE.p : nullptr;
+    a.LS = c->ali_valid ? c->LS.p : nullptr;
     const int *I = c->se_ints.p;
     const double *D = c->se_dbls.p;
     a.tr_rad = I + c->se_offs[0]; a.tr_col = I + c->se_offs[1]; a.ent_off = I + c->se_offs[2];
@@ -552,6 +577,7 @@ extern "C" int portal_solve_se(portal_ctx *c, int kmax, const double *J0, const 
         PCHECK(c, cudaMemcpyAsync(c->J2.p, J2, LN * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)c->N * sizeof(int), c->stream));
         c->j_valid = true;
+        c->ali_valid = false;  // a field from the host carries no split
     } else if (!c->j_valid) {
         return set_err(c, PORTAL_ERR_STATE, "portal_solve_se: no device-resident radiation field");
     }

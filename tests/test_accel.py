@@ -1,0 +1,112 @@
+"""Ng acceleration of the Lambda iteration: the numpy restatement on a model
+problem (CPU), the device step against it on the device's own iterates, and
+the accelerated iteration against the plain one (GPU)."""
+import numpy as np
+import pytest
+
+from oracle import accel
+
+
+def test_ng_solves_two_mode_linear_iteration():
+    # x_{k+1} = x* + M (x_k - x*), the error in a two-dimensional invariant
+    # subspace of M: order-2 Ng is exact
+    rng = np.random.default_rng(0)
+    n = 40
+    xs = rng.uniform(1, 2, size=(n, 1))
+    U = np.linalg.qr(rng.normal(size=(n, 2)))[0]
+    M = U @ np.diag([0.97, 0.6]) @ U.T
+    x = [xs + U @ rng.normal(size=(2, 1)) * 0.1]
+    for _ in range(3):
+        x.append(xs + M @ (x[-1] - xs))
+    xe, (a, b) = accel.ng_extrapolate(*x)
+    # (with any weights: the residual combination vanishes exactly)
+    assert np.abs(xe - xs).max() < 1e-9
+    assert np.abs(x[-1] - xs).max() > 1e-3
+
+
+@pytest.mark.gpu
+def test_device_ng_step_matches_restatement(built_lib, cfg1):
+    import portal_gb300 as pg
+
+    cloud, mol, rc = cfg1
+    n_mol = cloud.lev_p.sum(axis=1)
+    g = np.sqrt(2 * mol.j_lev + 1.0)
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        xs = [cloud.lev_p / (n_mol[:, None] * g[None, :])]
+        for _ in range(3):
+            _, lev, n, _, _ = ctx.lambda_iterate(rc, tol=1e-30, max_iter=1)
+            xs.append(lev / (n_mol[:, None] * g[None, :]))
+        ctx.set_cloud(cloud)
+        # three passes, then the Ng step: the final populations are its result
+        _, lev_ng, n, _, _ = ctx.lambda_iterate(rc, tol=1e-30, max_iter=3, ng_period=3)
+        assert n == 3
+    want, (a, b) = accel.ng_populations(*xs, g)
+    got = lev_ng / (n_mol[:, None] * g[None, :])
+    assert abs(a) + abs(b) > 1e-3        # the step does something
+    np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-14)
+
+
+@pytest.mark.gpu
+def test_ng_reaches_the_plain_fixed_point_sooner(built_lib, cfg1):
+    import portal_gb300 as pg
+
+    cloud, mol, rc = cfg1
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        pp0, _, n0, res0, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=400)
+        ctx.set_cloud(cloud)
+        pp1, _, n1, res1, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=400, ng_period=4)
+    assert res0[-1] < 1e-6 and res1[-1] < 1e-6
+    assert n1 < 0.6 * n0
+    r0, r1 = pp0[:, 0::2], pp1[:, 0::2]
+    # both stop within 1e-6 of a fixed point of a map contracting at ~0.94
+    assert np.abs(r1 - r0).max() <= 5e-5 * np.abs(r0).max()
+
+
+@pytest.mark.gpu
+def test_split_field_matches_oracle(built_lib, cfg1):
+    """J_eff and L* of the radiation-field kernel against the FP64 oracle."""
+    import portal_gb300 as pg
+    import oracle
+
+    cloud, mol, rc = cfg1
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, _, oJE, oLS, _ = P.radiation_field_split(rc)
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        J0, _, JE, LS, st = ctx.radiation_field_split(rc)
+    assert not st.any()
+    bulk = cloud.bulk_node_num
+    live = cloud.ab_all[:bulk] > 0
+    # the same tolerances as J0 itself: FP32 integration against FP64
+    for got, want in ((J0, oJ0), (JE, oJE)):
+        rel = np.abs(got[:bulk][live] - want[:bulk][live]) / np.abs(want[:bulk][live])
+        assert rel.max() < 2e-4 and np.median(rel) < 2e-7
+    # L* is a weighted mean of (1 - e^-tau) over channels and directions
+    err = np.abs(LS[:bulk][live] - oLS[:bulk][live])
+    assert err.max() < 2e-6
+    assert (oLS[:bulk][live] > 0).all() and (oLS[:bulk][live] < 1).all()
+    assert (oJE[:bulk][live] < oJ0[:bulk][live]).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ng", [0, 4])
+def test_local_operator_reaches_the_plain_fixed_point(built_lib, cfg1, ng):
+    import portal_gb300 as pg
+
+    cloud, mol, rc = cfg1
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        pp0, _, n0, res0, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=400)
+        ctx.set_cloud(cloud)
+        pp1, _, n1, res1, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=400, ng_period=ng, local_operator=True)
+    # the last pass is the plain pass that confirmed convergence
+    assert res1[-1] < 1e-6 and res1[-2] < 1e-6
+    assert n1 < 0.5 * n0
+    r0, r1 = pp0[:, 0::2], pp1[:, 0::2]
+    assert np.abs(r1 - r0).max() <= 5e-5 * np.abs(r0).max()
