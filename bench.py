@@ -15,7 +15,11 @@ main_para.f90:210-257 of the reference.  Workload: the power-law sphere with
            step uploads the cloud (portal_set_cloud), runs the node loop and
            reads pol_pops back;
   cpu_baseline  the FP64 oracle port (OpenMP over nodes like the reference)
-           on this host's cores, on a bounded sample of the same nodes.
+           on this host's cores, on a bounded sample of the same nodes;
+  convergence   time to a converged Lambda iteration (1e-6 relative change
+           per pass) on a held-out 16,384-point turbulent cube: plain, Ng,
+           accelerated (local operator + Ng), warm-started by the MLP the
+           run trains on eight other cubes, and warm-started + accelerated.
 
 --impl reference times that CPU port alone on the same workload.
 Multi-GPU: every rank runs its own replica of the workload (weak scaling);
@@ -182,6 +186,67 @@ def reference_arm(args, rank, world):
     return 0
 
 
+def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
+    """Time to a converged Lambda iteration (largest relative change of
+    rho^0_0 per pass below 1e-6) on a held-out turbulent cube, plain against
+    the accelerated (local operator + Ng every 4 passes) and the warm-started
+    iterations.  The network is trained here, by the library's kernels, on
+    the converged solutions of n_train seeded cubes of the same recipe."""
+    import torch
+    import portal_gb300 as pg
+    from portal_gb300 import synth
+    from portal_gb300.warmstart import WarmStart
+
+    mol = synth.linear_rotor(20)
+    rc = synth.RunConfig(nth=16, nph=16, nvel=32, kmax=2, gvec=synth.gauge_vector(4))
+    out = {"workload": "turbulent cube (lognormal density sigma_ln 1.5, mean 1e4 cm^-3; k^-11/3 velocity, "
+                       "1 km/s rms; field along x + equal turbulent part), %d points, 20-level rotor, 16x16 "
+                       "directions, 65 channels, kmax 2; held-out seed 300" % n_points,
+           "tol": 1e-6}
+    with WarmStart(mol.j_lev, seed=1, device=device) as ws, pg.Context(device) as ctx:
+        ctx.set_molecule(mol)
+        t0 = time.perf_counter()
+        Xs, Ys = [], []
+        for i in range(n_train):
+            cl = synth.turbulent_cube(n_points, 200 + i, mol, grid=32)
+            ctx.set_cloud(cl)
+            X, Y, _ = ws.collect(ctx, rc, cl.ab_all, cl.bulk_node_num)
+            Xs.append(X)
+            Ys.append(Y)
+        t1 = time.perf_counter()
+        losses = ws.fit(np.concatenate(Xs), np.concatenate(Ys), epochs=epochs)
+        t2 = time.perf_counter()
+        out["training"] = {"clouds": n_train, "rows": int(sum(len(x) for x in Xs)), "epochs": epochs,
+                           "data_seconds": t1 - t0, "fit_seconds": t2 - t1,
+                           "loss_first_last": [float(losses[0]), float(losses[-1])]}
+        cl = synth.turbulent_cube(n_points, 300, mol, grid=32)
+        ref = None
+        for name, warm, ng, lo in (("plain", False, 0, False), ("ng", False, 4, False),
+                                   ("accelerated", False, 4, True), ("warm", True, 0, False),
+                                   ("warm_accelerated", True, 4, True)):
+            ctx.set_cloud(cl)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if warm:
+                pp, _, n, res, _ = ws.solve(ctx, rc, tol=1e-6, max_iter=3000, ng_period=ng, local_operator=lo)
+            else:
+                pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=3000, ng_period=ng,
+                                                      local_operator=lo)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            r0 = pp[:, 0::2]
+            if ref is None:
+                ref = r0
+            out[name] = {"passes": int(n) + (1 if warm else 0), "seconds": dt,
+                         "final_residual": float(res[-1]),
+                         "max_rel_diff_vs_plain": float(np.abs(r0 - ref).max() / np.abs(ref).max())}
+    out["speedup_vs_plain"] = {k: out["plain"]["seconds"] / out[k]["seconds"]
+                               for k in ("ng", "accelerated", "warm", "warm_accelerated")}
+    out["note"] = ("passes of warm runs include the radiation-field pass that feeds the network; "
+                   "wall time on the host around each call, network inference included")
+    return out
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import portal_gb300 as pg
@@ -310,9 +375,11 @@ def gpu_arm(args, rank, world, local_rank):
         line["cpu_baseline"] = {"value": rates[0][0], "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": "%d consecutive nodes of %d (all their rays + SE), %.1f s" %
                                           (rates[0][2], cloud.bulk_node_num, rates[0][1])}
+    ctx.close()
+    if rank == 0 and world == 1 and not args.no_convergence:
+        line["convergence"] = convergence_leg(local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -329,6 +396,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-convergence", action="store_true",
+                    help="skip the time-to-converged comparison (plain / accelerated / warm-started)")
     ap.add_argument("--n-depth", type=int, default=10000,
                     help="walk length limit (main_portal.x's n_depth); smaller values shrink the walk scratch")
     args = ap.parse_args()

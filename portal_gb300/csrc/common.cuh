@@ -170,6 +170,34 @@ __device__ __forceinline__ double sphere_exit(double px, double py, double pz, d
     return (x2 > 0.0) ? x2 : x1;
 }
 
+// 1 - e^-tau of a cell's optical depth tau = x ln 2, given e = 2^-x from
+// ex2: the weight of the transfer update I' = I + (1 - e^-tau) (S - I).
+//   - 1 - e alone loses the small-tau regime (e rounds to 1 below tau ~ 6e-8
+//     and keeps only ~1.5e-7/tau of relative accuracy above), where an
+//     optically thin line's emission S tau can be all there is (a high line
+//     whose source function exceeds the background by 1e14); below
+//     |tau| = 0.0435 the cubic Taylor form tau (1 - tau/2 + tau^2/6) is used
+//     (relative error <= 3.5e-6 on both sides of the switch).
+//   - The reference forms 1 - exp(-tau) in FP64, which rounds it to a
+//     multiple of 2^-53 (exp(-tau) lies on the 2^-53 grid below 1) and drops
+//     tau below 2^-54 altogether; its results for such lines depend on that
+//     rounding.  The Taylor value is rounded the same way: adding and
+//     removing 1.5 * 2^-30 rounds anything below 2^-31 to a multiple of 2^-53
+//     (the FP32 grid spacing at that magnitude) and changes larger values by
+//     at most an FP32 rounding.
+constexpr float OM_TAYLOR_X = 0.0628f;                 // |x| below which the Taylor form is used
+constexpr float OM_MAGIC = 1.3969838619232178e-09f;    // 1.5 * 2^-30
+__device__ __forceinline__ float om_taylor(float x) {
+    constexpr float C1 = 0.693147181f;   // ln 2
+    constexpr float C2 = -0.240226507f;  // -(ln 2)^2 / 2
+    constexpr float C3 = 0.0555041087f;  // (ln 2)^3 / 6
+    const float h = fmaf(x, fmaf(x, C3, C2), C1);
+    return __fsub_rn(fmaf(x, h, OM_MAGIC), OM_MAGIC);
+}
+__device__ __forceinline__ float one_minus_exp(float x, float e) {
+    return (fabsf(x) < OM_TAYLOR_X) ? om_taylor(x) : 1.f - e;
+}
+
 // host: Gauss-Legendre rule on (-1,1), ascending knots (Newton iteration on
 // the three-term recurrence, long double)
 void gauss_legendre(int n, double *x, double *w);

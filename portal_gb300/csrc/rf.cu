@@ -127,7 +127,12 @@ __global__ void k_line_table(int N, int L, double dxp, const double *__restrict_
         double c2b = 4.79924e-11 / Td;
         Ibb = 1.4744995e-50 * lc.nu * lc.nu * lc.nu / (exp(c2b * lc.nu) - 1.0);
     }
-    ltab[t] = make_float4((float)(kv * phif), (float)(ev * phif), (float)Ad, (float)(Ad * Ibb));
+    // (optical depth per trace step at unit profile, line source function
+    // ev/kv, dust optical depth per step, dust emissivity per step): the
+    // source function is stored as the FP64 ratio, not the emissivity, so a
+    // weak line's S keeps full FP32 precision where kv and ev alone would be
+    // FP32 denormals
+    ltab[t] = make_float4((float)(kv * phif), (float)(kv != 0.0 ? ev / kv : 0.0), (float)Ad, (float)(Ad * Ibb));
 }
 
 template <int NLG, bool DUST>
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                         if (l0 + l < a.L) {
                                             const float4 v = lt[l];
                                             R.As[lane][l] = v.x * fst;
-                                            R.Ss[lane][l] = v.y * fst;
+                                            R.Ss[lane][l] = v.y * v.x * fst;   // emissivity x steps
                                             R.Ad[lane][DUST ? l : 0] = v.z * fst;
                                             R.Jd[lane][DUST ? l : 0] = v.w * fst;
                                         }
@@ -299,13 +304,13 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                         // line with kv <= 0 fails ray_in's gate tau > 1e-30
                                         // in every channel (inverse_rt.f90:308), and so does
                                         // a padding line of the last group: both get A = S
-                                        // = 0, which leaves I unchanged exactly (e = 1).
+                                        // = 0, which leaves I unchanged exactly.
                                         float As = 0.f, Ss = 0.f;
                                         if (l0 + l < a.L) {
                                             const float4 v = lt[l];
                                             if (v.x > 0.f) {
                                                 As = v.x * fst * LOG2E_F;
-                                                Ss = v.y / v.x;
+                                                Ss = v.y;
                                             }
                                         }
                                         R.As[lane][l] = As;
@@ -334,23 +339,27 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                                 // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
                                                 const float tau = fmaf(Au, g[s2], Adu);
                                                 const float Sv = fmaf(Su, g[s2], Jdu) / tau;
-                                                const float e = ex2(-tau * LOG2E_F);
-                                                const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                                const float x = tau * LOG2E_F;
+                                                const float om = one_minus_exp(x, ex2(-x));
+                                                const float In = fmaf(om, Sv - I[s2][l], I[s2][l]);
                                                 I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
                                             }
                                         }
                                     } else {
-                                        // ray_in's gate tau > 1e-30 (inverse_rt.f90:308) needs no
-                                        // test here: channels below it have ex2(-tau) == 1
-                                        // exactly (the rounding of ex2.approx for arguments above
-                                        // -2^-23), and I e + S (1 - e), formed as
-                                        // fma(I, e, fma(-S, e, S)), then leaves I unchanged;
-                                        // lines with kv <= 0 carry A = S = 0.  Branch-free, so
-                                        // the NS x NLG update chains of a cell interleave.
+                                        // I' = I + (1 - e^-tau)(S - I) with 1 - e^-tau accurate
+                                        // down to tau = 0 and rounded as the reference's FP64
+                                        // (one_minus_exp).  ray_in's gate tau > 1e-30
+                                        // (inverse_rt.f90:308) needs no test: lines with kv <= 0
+                                        // carry A = S = 0 and leave I unchanged exactly, and
+                                        // 0 < tau < 2^-54 rounds to a zero weight as in FP64.
+                                        // Branch-free, so the NS x NLG update chains of a cell
+                                        // interleave (a uniform thin-line branch measured 7 %
+                                        // slower).
 #pragma unroll
                                         for (int s2 = 0; s2 < NS; s2++) {
-                                            const float e = ex2(-Au * g[s2]);
-                                            I[s2][l] = fmaf(I[s2][l], e, fmaf(-Su, e, Su));
+                                            const float x = Au * g[s2];
+                                            const float om = one_minus_exp(x, ex2(-x));
+                                            I[s2][l] = fmaf(om, Su - I[s2][l], I[s2][l]);
                                         }
                                     }
                                 }
@@ -377,19 +386,21 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                                         if (DUST) {
                                             const float kap = fmaf(v.x, g0, v.z);
                                             tau = kap * fst0;
-                                            Sv = fmaf(v.y, g0, v.w) / kap;
+                                            Sv = fmaf(v.y * v.x, g0, v.w) / kap;
                                             lf = v.x * g0 / kap;   // line share of the opacity
                                             Sd = v.w / kap;        // dust emission share of S
                                         } else {
                                             tau = v.x * g0 * fst0;
-                                            Sv = v.y / v.x;
+                                            Sv = v.y;
                                         }
-                                        const float e = ex2(-tau * LOG2E_F);
-                                        const float Io = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                        const float x = tau * LOG2E_F;
+                                        const float e = ex2(-x);
+                                        const float om = one_minus_exp(x, e);
+                                        const float Io = fmaf(om, Sv - I[s2][l], I[s2][l]);
                                         part[l] = fmaf(a.chw[ch], Io, part[l]);
                                         if (split) {
-                                            pe[l] = fmaf(a.chw[ch], fmaf(I[s2][l], e, Sd * (1.f - e)), pe[l]);
-                                            pl[l] = fmaf(a.chw[ch], lf * (1.f - e), pl[l]);
+                                            pe[l] = fmaf(a.chw[ch], fmaf(om, Sd - I[s2][l], I[s2][l]), pe[l]);
+                                            pl[l] = fmaf(a.chw[ch], lf * om, pl[l]);
                                         }
                                     }
                                 }

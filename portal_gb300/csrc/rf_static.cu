@@ -84,7 +84,9 @@ __device__ float4 rs_line_coef(const RsArgs &a, int n, int l) {
     const double Td = a.temp_all[2 * (size_t)n + 1];
     double Ibb = 0.0;
     if (Td != 0.0) Ibb = 1.4744995e-50 * lc.nu * lc.nu * lc.nu / (exp(4.79924e-11 / Td * lc.nu) - 1.0);
-    return make_float4((float)(kv * phif), (float)(ev * phif), (float)Ad, (float)(Ad * Ibb));
+    // the line's source function as the FP64 ratio (full FP32 precision for
+    // weak lines whose kv, ev alone would be FP32 denormals)
+    return make_float4((float)(kv * phif), (float)(kv != 0.0 ? ev / kv : 0.0), (float)Ad, (float)(Ad * Ibb));
 }
 
 constexpr int RS_NLG = 5;
@@ -206,7 +208,8 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
                                 for (int l = 0; l < RS_NLG; l++)
                                     if (l0 + l < a.L) {
                                         const float4 v = rs_line_coef(a, wc.x, l0 + l);
-                                        s_c[wib][lane][l] = make_float4(v.x * fst, v.y * fst, v.z * fst, v.w * fst);
+                                        const float tc = v.x * fst;  // line-centre optical depth
+                                        s_c[wib][lane][l] = make_float4(tc, v.y * tc, v.z * fst, v.w * fst);
                                     }
                             }
                             __syncwarp();
@@ -227,8 +230,9 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
                                             // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
                                             const float tau = fmaf(cf.x, g[s2], cf.z);
                                             const float Sv = fmaf(cf.y, g[s2], cf.w) / tau;
-                                            const float e = rs_ex2(-tau * RS_LOG2E);
-                                            const float In = fmaf(I[s2][l], e, Sv * (1.f - e));
+                                            const float x = tau * RS_LOG2E;
+                                            const float om = one_minus_exp(x, rs_ex2(-x));
+                                            const float In = fmaf(om, Sv - I[s2][l], I[s2][l]);
                                             I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
                                         }
                                     }
@@ -249,9 +253,10 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
                                         const float g0 = rs_ex2(-chq[ch] * chq[ch] * RS_LOG2E);
                                         const float kap = fmaf(v.x, g0, v.z);
                                         const float tau = kap * (float)steps0;
-                                        const float Sv = fmaf(v.y, g0, v.w) / kap;
-                                        const float e = rs_ex2(-tau * RS_LOG2E);
-                                        part[l] = fmaf(chw[ch], fmaf(I[s2][l], e, Sv * (1.f - e)), part[l]);
+                                        const float Sv = fmaf(v.y * v.x, g0, v.w) / kap;
+                                        const float x = tau * RS_LOG2E;
+                                        const float om = one_minus_exp(x, rs_ex2(-x));
+                                        part[l] = fmaf(chw[ch], fmaf(om, Sv - I[s2][l], I[s2][l]), part[l]);
                                     }
                                 }
                             }

@@ -227,14 +227,16 @@ def neighbours_from_tets(tets: np.ndarray, n: int):
     return off, d
 
 
-def _radii_power_law(rng, n, r_out, r_core):
-    m_in = r_core ** 1.5 / 3.0
-    m_out = (2.0 / 3.0) * (r_out ** 1.5 - r_core ** 1.5)
+def _radii_power_law(rng, n, r_out, r_core, p=1.5):
+    """Radii of points with density ~ r^-p outside r_core, uniform inside."""
+    q = 3.0 - p
+    m_in = r_core ** q / 3.0
+    m_out = (1.0 / q) * (r_out ** q - r_core ** q)
     u = rng.random(n) * (m_in + m_out)
     r = np.empty(n)
     inner = u < m_in
-    r[inner] = np.cbrt(3.0 * u[inner] * r_core ** 1.5)
-    r[~inner] = (1.5 * (u[~inner] - m_in) + r_core ** 1.5) ** (2.0 / 3.0)
+    r[inner] = np.cbrt(3.0 * u[inner] * r_core ** p)
+    r[~inner] = (q * (u[~inner] - m_in) + r_core ** q) ** (1.0 / q)
     return r
 
 
@@ -248,16 +250,18 @@ def lte_fractions(mol: Molecule, T: np.ndarray) -> np.ndarray:
 def power_law_sphere(n_points: int, seed: int, mol: Molecule, *, t_law: str = "uniform",
                      t_uniform: float = 20.0, b_random: float = 0.0,
                      abundance: float = 1e-4, r_out_au: float = 1e4, r_core_au: float = 200.0,
-                     micro_turb: float = 200.0, keep_raw: bool = False) -> Cloud:
-    """The power-law sphere of the benchmark configurations.
+                     micro_turb: float = 200.0, keep_raw: bool = False, density_exp: float = 1.5,
+                     n0_cm3: float = 1e5, b_dir=(0.0, 0.0, 1.0)) -> Cloud:
+    """The power-law sphere of the benchmark configurations: points and
+    n_H2 = n0_cm3 (r/1000 AU)^-density_exp outside a core of r_core_au.
 
     t_law "uniform" (T = t_uniform) or "loglinear" (40 K at the core radius
     falling linearly in log r to 10 K at the edge).  b_random is the rms of
-    an isotropic Gaussian component added to a unit field along z."""
+    an isotropic Gaussian component added to a unit field along b_dir."""
     from scipy.spatial import Delaunay
 
     rng = np.random.default_rng(seed)
-    r = _radii_power_law(rng, n_points, r_out_au, r_core_au)
+    r = _radii_power_law(rng, n_points, r_out_au, r_core_au, density_exp)
     u = rng.normal(size=(n_points, 3))
     u /= np.linalg.norm(u, axis=1, keepdims=True)
     pos_au = u * r[:, None]
@@ -267,7 +271,7 @@ def power_law_sphere(n_points: int, seed: int, mol: Molecule, *, t_law: str = "u
     off, idx = neighbours_from_tets(tets, n_points)
 
     r_eff = np.maximum(r, r_core_au)
-    n_h2 = 1e5 * 1e6 * (r_eff / 1000.0) ** -1.5                     # m^-3
+    n_h2 = n0_cm3 * 1e6 * (r_eff / 1000.0) ** -density_exp          # m^-3
     if t_law == "uniform":
         T = np.full(n_points, float(t_uniform))
     else:
@@ -278,7 +282,7 @@ def power_law_sphere(n_points: int, seed: int, mol: Molecule, *, t_law: str = "u
     b_turb = np.full(n_points, micro_turb)
     ab = np.full(n_points, abundance)
     gas_ii_dust = np.zeros(n_points)
-    bvec = np.tile(np.array([0.0, 0.0, 1.0]), (n_points, 1))
+    bvec = np.tile(np.asarray(b_dir, dtype=np.float64), (n_points, 1))
     if b_random > 0.0:
         bvec = bvec + b_random * rng.normal(size=(n_points, 3))
     bvec /= np.linalg.norm(bvec, axis=1, keepdims=True)
@@ -396,6 +400,29 @@ def turbulent_cube(n_points: int, seed: int, mol: Molecule, *, grid: int = 64, s
                ab=np.full(n_points, abundance), gas_ii_dust=np.zeros(n_points), frac=lte_fractions(mol, Tk))
     return ingest(raw, mol, off, idx, bvec, bulk_node_num=n_points, tets=tets if keep_raw else None,
                   keep_raw=keep_raw)
+
+
+def batch_clouds(n_clouds: int = 64, points_scale: float = 1.0, n_min: int = 10000, n_max: int = 300000):
+    """The batched uneven configuration: cloud i from seed 100 + i with a
+    point count log-uniform in [n_min, n_max] (times points_scale), a linear
+    rotor of 5..20 levels, density exponent uniform in 1..2, n0 log-uniform
+    in 1e4..1e7 cm^-3 and an isotropically drawn field direction; T = 20 K.
+    Returns [(cloud, molecule)] and the run configuration shared by all
+    (16x16 directions, 65 channels, kmax 2)."""
+    out = []
+    for i in range(n_clouds):
+        rng = np.random.default_rng(100 + i)
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max))) * points_scale))
+        nlev = int(rng.integers(5, 21))
+        p = float(rng.uniform(1.0, 2.0))
+        n0 = float(10.0 ** rng.uniform(4.0, 7.0))
+        b = rng.normal(size=3)
+        b /= np.linalg.norm(b)
+        mol = linear_rotor(nlev)
+        cloud = power_law_sphere(max(n, 64), 100 + i, mol, density_exp=p, n0_cm3=n0, b_dir=tuple(b))
+        out.append((cloud, mol))
+    rc = RunConfig(nth=16, nph=16, nvel=32, kmax=2, gvec=gauge_vector(3))
+    return out, rc
 
 
 def gauge_vector(seed: int) -> tuple:

@@ -183,6 +183,39 @@ def test_cfg2_shape_subset():
     assert (np.abs(pops[:64, 0::2] - opp[:64, 0::2]) / np.abs(opp[:64, 0::2])).max() < 2e-4
 
 
+def test_cfg4_shape_subset():
+    """The turbulent-cube shape (20-level rotor, 32x32 directions, 129
+    channels, kmax 2) on a 32,768-point cube: the full node loop on the
+    device, first 24 nodes against the oracle, and the split of the
+    accelerated iteration."""
+    import oracle
+    import portal_gb300 as pg
+    from portal_gb300 import synth
+    cloud, mol, rc = synth.config_cloud("cfg4", n_points=32768)
+    with pg.Context(0) as c:
+        c.set_molecule(mol)
+        c.set_cloud(cloud)
+        J0, J2, JE, LS, st = c.radiation_field_split(rc)
+    assert not st.any()
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, oJE, oLS, _ = P.radiation_field_split(rc, 1, 24)
+    _check_J(J0[:24], J2[:24], oJ0[:24], oJ2[:24])
+    assert (np.abs(JE[:24] - oJE[:24]) / oJE[:24]).max() < 2e-4
+    assert np.abs(LS[:24] - oLS[:24]).max() < 2e-6
+    # the plain node loop (setup_stateq's equations) against the oracle
+    with pg.Context(0) as c:
+        c.set_molecule(mol)
+        c.set_cloud(cloud)
+        c.radiation_field(rc, fetch=False)
+        pops, _ = c.solve_se(rc.kmax)
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2, 1, 24)
+    # 20 levels at 20 K span ~60 decades: compare the levels above 1e-8 of a
+    # node's largest (the SE's refinement converges normwise)
+    r, o = pops[:24, 0::2], opp[:24, 0::2]
+    sig = np.abs(o) >= 1e-8 * np.abs(o).max(axis=1, keepdims=True)
+    assert (np.abs(r - o) / np.abs(o))[sig].max() < 2e-4
+
+
 # ---- Stokes image (finish_portal.x pixel mode) ----------------------------
 
 def _image_case(n=4096, im_pix=16, nvel=8):
