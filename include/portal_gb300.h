@@ -242,6 +242,45 @@ int portal_set_stream(portal_ctx *ctx, void *cuda_stream);
  * integration kernel; launches[i] the number of launches each. */
 int portal_last_kernel_times(const portal_ctx *ctx, double *times_ms, int *launches, int n);
 
+/* Copy the device-resident results of the last pass out (any pointer may be
+ * NULL): J0, J2 (r_num,N), pol_pops(N, 2*nlev), status(N).  For models run by
+ * a batch, whose results stay on the device. */
+int portal_get_results(portal_ctx *ctx, double *J0, double *J2, double *pol_pops, int *status);
+
+/* ---- many models in one launch (no counterpart in the reference) --------
+ *
+ * PORTAL post-processes one LIME model per run.  A batch runs the node loop
+ * (radiation field + SE, as portal_radiation_field + portal_solve_se) of
+ * many models -- each a context with its own cloud and molecule, uneven in
+ * point and level counts -- as one persistent radiation-field launch and
+ * one SE launch over all models' (model, node) work items, captured once
+ * into a CUDA graph and replayed.  portal_batch_prepare picks the launch
+ * shapes (line group and blocks per SM of the radiation-field kernel, warps
+ * per block of the SE kernel) by timing each candidate on a 1-in-16 sample
+ * of the work when autotune != 0.  Results stay in each model's context
+ * (portal_get_results).  The contexts must outlive the batch and must not
+ * be used on their own while a batch run is in flight. */
+typedef struct portal_batch portal_batch;
+
+int portal_batch_create(portal_batch **batch, int device);
+int portal_batch_destroy(portal_batch *batch);
+const char *portal_batch_last_error(const portal_batch *batch);
+/* Add a model (a context with cloud and molecule set, on the batch's
+ * device); returns its index (>= 0) or an error code. */
+int portal_batch_add(portal_batch *batch, portal_ctx *model);
+/* Set up every model for the pass (directions, channels, kmax as in
+ * portal_radiation_field / portal_solve_se), tune and capture the graph. */
+int portal_batch_prepare(portal_batch *batch, int nth, int nph, int nvel, const double *gvec, double dx,
+                         int n_depth, int kmax, int autotune);
+/* One pass over every model; use_graph 0 issues the same launches without
+ * the graph.  n_segments: ray segments walked; ms: device time of the pass. */
+int portal_batch_run(portal_batch *batch, int use_graph, long long *n_segments, double *ms);
+/* Launch shapes in use (config[4]: line group, radiation-field blocks per
+ * SM, SE warps per block, SE blocks per SM) and the tuner's timings
+ * (triples: shape, shape, ms per candidate); returns the number of timing
+ * values available. */
+int portal_batch_config(const portal_batch *batch, int *config, double *tune, int max_tune);
+
 /* ---- learned warm start (no counterpart in the reference) -------------
  *
  * A small MLP maps per-node features of the cloud and of the first

@@ -37,7 +37,9 @@ EXPORTS = (
     "portal_lambda_iterate",
     "portal_mlp_create", "portal_mlp_destroy", "portal_mlp_last_error", "portal_mlp_num_params",
     "portal_mlp_get_params", "portal_mlp_set_params", "portal_mlp_gradients", "portal_mlp_train",
-    "portal_mlp_predict", "portal_warmstart_features",
+    "portal_mlp_predict", "portal_warmstart_features", "portal_get_results",
+    "portal_batch_create", "portal_batch_destroy", "portal_batch_last_error", "portal_batch_add",
+    "portal_batch_prepare", "portal_batch_run", "portal_batch_config",
 )
 
 _lib = None
@@ -107,6 +109,16 @@ def lib() -> C.CDLL:
     L.portal_mlp_train.argtypes = [C.c_void_p, P_F, P_F, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, P_F]
     L.portal_mlp_predict.argtypes = [C.c_void_p, P_F, C.c_int, P_F]
     L.portal_warmstart_features.argtypes = [C.c_void_p, P_F]
+    L.portal_get_results.argtypes = [C.c_void_p, P_D, P_D, P_D, P_I]
+    L.portal_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    L.portal_batch_destroy.argtypes = [C.c_void_p]
+    L.portal_batch_last_error.restype = C.c_char_p
+    L.portal_batch_last_error.argtypes = [C.c_void_p]
+    L.portal_batch_add.argtypes = [C.c_void_p, C.c_void_p]
+    L.portal_batch_prepare.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P_D, C.c_double, C.c_int, C.c_int,
+                                       C.c_int]
+    L.portal_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
+    L.portal_batch_config.argtypes = [C.c_void_p, P_I, P_D, C.c_int]
     _lib = L
     return L
 
@@ -289,6 +301,15 @@ class Context:
         return {k: (float(t[i]), int(n[i])) for i, k in enumerate(KERNEL_SLOTS)}
 
 
+    def results(self, field=True, pops=True):
+        """Device-resident results of the last pass: (J0, J2) as (N, r_num)
+        and pol_pops (N, 2 nlev), each None when not asked for."""
+        J0 = np.zeros((self.N, self.r_num)) if field else None
+        J2 = np.zeros((self.N, self.r_num)) if field else None
+        pp = np.zeros((2 * self.nlev, self.N)) if pops else None
+        self._check(lib().portal_get_results(self._h, _p(J0), _p(J2), _p(pp), None))
+        return J0, J2, (None if pp is None else pp.T.copy())
+
     def warmstart_features(self) -> np.ndarray:
         """Features (N, 8) of the warm start from the device-resident
         radiation field of the last radiation_field call."""
@@ -377,6 +398,64 @@ class MLP:
         Y = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
         self._check(lib().portal_mlp_predict(self._h, _p(X, P_F), X.shape[0], _p(Y, P_F)))
         return Y
+
+
+class Batch:
+    """Many models in one launch (portal_batch_*): add contexts, prepare
+    (tunes the launch shapes, captures the CUDA graph), run passes."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().portal_batch_create(C.byref(self._h), device)
+        if rc != PORTAL_OK:
+            raise PortalError(rc, "portal_batch_create")
+        self.models = []
+
+    def close(self):
+        if self._h:
+            lib().portal_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc < 0:
+            raise PortalError(rc, lib().portal_batch_last_error(self._h).decode())
+        return rc
+
+    def add(self, ctx: "Context") -> int:
+        i = self._check(lib().portal_batch_add(self._h, ctx._h))
+        self.models.append(ctx)
+        return i
+
+    def prepare(self, rc, autotune: bool = True):
+        g = _f64(rc.gvec)
+        self._check(lib().portal_batch_prepare(self._h, rc.nth, rc.nph, rc.nvel, _p(g), float(rc.dx), rc.n_depth,
+                                               rc.kmax, int(bool(autotune))))
+
+    def run(self, use_graph: bool = True):
+        """One pass over every model: (segments, device ms)."""
+        nseg, ms = C.c_longlong(0), C.c_double(0.0)
+        self._check(lib().portal_batch_run(self._h, int(bool(use_graph)), C.byref(nseg), C.byref(ms)))
+        return int(nseg.value), float(ms.value)
+
+    def config(self):
+        """(line group, RF blocks/SM, SE warps/block, SE blocks/SM) and the
+        tuner's (shape, shape, ms) rows."""
+        cfg = np.zeros(4, dtype=np.int32)
+        tune = np.zeros(64)
+        n = self._check(lib().portal_batch_config(self._h, _p(cfg, P_I), _p(tune), 64))
+        return tuple(int(v) for v in cfg), tune[:n].reshape(-1, 3)
 
 
 def wigner3j(tj1, tj2, tj3, tm1, tm2, tm3) -> float:

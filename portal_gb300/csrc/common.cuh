@@ -76,6 +76,8 @@ struct portal_ctx {
 
     // ---- derived / results ----
     portal::DevBuf<float4> ltab;      // (r_num,N) line table
+    portal::DevBuf<unsigned char> linebuf;  // per-line constants of the molecule (rf.cu)
+    portal::DevBuf<float> bbcmb;      // (r_num) black_body(2.73 K) per line
     portal::DevBuf<double> J0, J2;    // (r_num,N)
     portal::DevBuf<double> JE, LS;    // (r_num,N) J0 without the node's own emission, local operator L*
     bool ali_valid = false;           // JE / LS belong to the current J0 (the SE splits the field)
@@ -85,6 +87,7 @@ struct portal_ctx {
     portal::DevBuf<double> dirtab;    // direction table
     portal::DevBuf<float> chtab;      // channel tables
     bool j_valid = false;
+    double rf_dxp = 0.0;              // r_max * trace step of the last radiation-field set-up
 
     // SE program (device) -- built per (molecule, kmax)
     int se_kmax = -1, c_dim = 0, n_trans = 0;

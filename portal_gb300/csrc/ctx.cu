@@ -262,6 +262,24 @@ extern "C" int portal_set_stream(portal_ctx *c, void *stream) {
     return PORTAL_OK;
 }
 
+extern "C" int portal_get_results(portal_ctx *c, double *J0, double *J2, double *pol_pops, int *status) {
+    if (!c) return PORTAL_ERR_ARG;
+    if (!c->j_valid) return set_err(c, PORTAL_ERR_STATE, "no device-resident results");
+    cudaSetDevice(c->device);
+    const size_t LN = (size_t)c->r_num * c->N;
+    if (J0) PCHECK(c, cudaMemcpyAsync(J0, c->J0.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (J2) PCHECK(c, cudaMemcpyAsync(J2, c->J2.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (pol_pops) {
+        if (!c->pops.p || c->se_kmax < 0) return set_err(c, PORTAL_ERR_STATE, "no device-resident populations");
+        PCHECK(c, cudaMemcpyAsync(pol_pops, c->pops.p, (size_t)c->N * 2 * c->nlev * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (status)
+        PCHECK(c, cudaMemcpyAsync(status, c->status.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    return PORTAL_OK;
+}
+
 extern "C" int portal_last_kernel_times(const portal_ctx *c, double *times_ms, int *launches, int n) {
     if (!c) return PORTAL_ERR_ARG;
     for (int i = 0; i < n && i < T_NSLOT; i++) {

@@ -1,0 +1,94 @@
+// Kernel argument blocks and the internal entry points shared by the
+// single-model calls (rf.cu, se.cu) and the batched launch (batch.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace portal {
+
+// Everything the radiation-field kernel reads or writes for one model.
+struct RFArgs {
+    int N, bulk, L, nvel, nch, ndir, n_depth;
+    float dx32;
+    const double *__restrict__ pos;
+    const double *__restrict__ bvec;
+    const double *__restrict__ ab;
+    const float4 *__restrict__ cellv;
+    const int *__restrict__ off;
+    const int *__restrict__ idx;
+    const float4 *__restrict__ edge;
+    const float4 *__restrict__ ltab;
+    const double *__restrict__ dirs;  // (ndir, 6): mu, sin th, cos ph, sin ph, w, w*c_in/sqrt2
+    const float *__restrict__ chq;    // (nch) 2 nv / nvel
+    const float *__restrict__ chw;    // (nch) exp(-q0^2) * 2/(sqrt(pi) nvel)
+    const float *__restrict__ bb;     // (L) black_body(2.73 K) per line: the incoming intensity
+    double gx, gy, gz;
+    double *J0, *J2;
+    double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
+    int *status;
+    int2 *walk;
+    unsigned long long *counters;
+};
+
+// Everything the SE kernel reads or writes for one model.
+struct SEArgs {
+    int N, bulk, c_dim, n_trans, nlev, L, c_temp, c_num, c_par, nent;
+    const double *__restrict__ J0;
+    const double *__restrict__ J2;
+    const double *__restrict__ JE;      // J0_eff (r_num, N) or null
+    const double *__restrict__ LS;      // L* (r_num, N) or null
+    const double *__restrict__ h2;
+    const double *__restrict__ tkin;
+    const double *__restrict__ ab;
+    // per transition
+    const int *__restrict__ tr_rad;
+    const int *__restrict__ tr_col;
+    const double *__restrict__ tr_nu;
+    const double *__restrict__ tr_A;
+    const double *__restrict__ tr_B21;
+    const double *__restrict__ col_temps;
+    const double *__restrict__ Cji;
+    // program over the matrix entries
+    const int *__restrict__ ent_off;
+    const int *__restrict__ ent_pos;
+    const int *__restrict__ term_f;
+    const double *__restrict__ term_c;
+    const int *__restrict__ norm_col;   // (nlev) count_array
+    const double *__restrict__ norm_val;
+    const int *__restrict__ pack;       // (2 nlev) rho index or -1
+    double *pops;                       // (N, 2 nlev) column-major
+    double *jj20;                       // (N, L) or null
+    int *status;
+    int *nfail;
+};
+
+// A batched launch: work items (model, node) over many models, the models'
+// argument blocks in device memory.
+struct RFBatch {
+    const RFArgs *models;
+    const int2 *items;
+    long long n_items;
+    unsigned long long *queue;   // [0] next item, [1] segments walked
+    int2 *walk;                  // per warp: 32 rays x n_depth
+    int n_depth;
+};
+struct SEBatch {
+    const SEArgs *models;
+    const int2 *items;
+    long long n_items;
+    size_t warp_bytes;           // dynamic shared memory per warp (largest model)
+};
+
+// rf.cu
+int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx, int n_depth,
+               bool split, RFArgs *a);
+int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s);
+int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int *blocks);
+int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, const RFBatch &bw);
+// se.cu
+int se_prepare(portal_ctx *c, int kmax, SEArgs *a, size_t *warp_bytes);
+int se_pass(portal_ctx *c, cudaStream_t s);
+int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw);
+int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks);
+
+}  // namespace portal

@@ -41,7 +41,7 @@
 #include <cmath>
 #include <cstdlib>
 
-#include "common.cuh"
+#include "internal.cuh"
 
 using namespace portal;
 
@@ -59,29 +59,6 @@ struct LineConst {
     int lo, up;
 };
 constexpr int MAX_LINES = 64;
-__constant__ LineConst c_lines[MAX_LINES];
-
-struct RFArgs {
-    int N, bulk, L, nvel, nch, ndir, n_depth;
-    float dx32;
-    const double *__restrict__ pos;
-    const double *__restrict__ bvec;
-    const double *__restrict__ ab;
-    const float4 *__restrict__ cellv;
-    const int *__restrict__ off;
-    const int *__restrict__ idx;
-    const float4 *__restrict__ edge;
-    const float4 *__restrict__ ltab;
-    const double *__restrict__ dirs;  // (ndir, 6): mu, sin th, cos ph, sin ph, w, w*c_in/sqrt2
-    const float *__restrict__ chq;    // (nch) 2 nv / nvel
-    const float *__restrict__ chw;    // (nch) exp(-q0^2) * 2/(sqrt(pi) nvel)
-    double gx, gy, gz;
-    double *J0, *J2;
-    double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
-    int *status;
-    int2 *walk;
-    unsigned long long *counters;
-};
 
 // Compensated (Kahan) FP32 sum: J of one node is a sum of a few hundred ray
 // contributions; the compensation keeps it to ~1e-7 of the sum of magnitudes
@@ -104,13 +81,14 @@ __device__ __forceinline__ float ex2(float x) {
 }
 
 // Line table: one thread per (node, line).
-__global__ void k_line_table(int N, int L, double dxp, const double *__restrict__ levp, int nlev,
-                             const double *__restrict__ b, const double *__restrict__ dustp,
-                             const double *__restrict__ tdust, float4 *__restrict__ ltab) {
+__global__ void k_line_table(int N, int L, double dxp, const LineConst *__restrict__ lines,
+                             const double *__restrict__ levp, int nlev, const double *__restrict__ b,
+                             const double *__restrict__ dustp, const double *__restrict__ tdust,
+                             float4 *__restrict__ ltab) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)N * L) return;
     int n = (int)(t / L), l = (int)(t - (long long)n * L);
-    const LineConst lc = c_lines[l];
+    const LineConst lc = lines[l];
     double p1 = levp[(size_t)nlev * n + lc.lo];
     double p2 = levp[(size_t)nlev * n + lc.up];
     // ray_in inverse_rt.f90:263-266, 293-294, 298-301
@@ -153,24 +131,48 @@ struct RayBatch {
 };
 
 // NS channel slots per lane (nch <= 32 NS), NLG lines per register group.
-template <int NS, int NLG, bool DUST>
-__global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
+// BATCH: the work items are (model, node) pairs of many models (RFBatch);
+// each warp copies the argument block of its current model into shared
+// memory.  Otherwise the nodes of the one model a0.
+template <int NS, int NLG, bool DUST, bool BATCH>
+__global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch bw) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
-    int2 *const wbase = a.walk + (size_t)gw * 32 * (size_t)a.n_depth;
+    const int n_depth = BATCH ? bw.n_depth : a0.n_depth;
+    int2 *const wbase = (BATCH ? bw.walk : a0.walk) + (size_t)gw * 32 * (size_t)n_depth;
     __shared__ CellRec<NLG, DUST> recs[8];
     __shared__ RayBatch rbs[8];
+    __shared__ RFArgs margs[BATCH ? 8 : 1];
     CellRec<NLG, DUST> &R = recs[wib];
     RayBatch &B = rbs[wib];
 
     unsigned long long nseg = 0;
+    int cur_model = -1;
     for (;;) {
         int node = 0;
-        if (lane == 0) node = (int)atomicAdd(&a.counters[0], 1ULL);
-        node = __shfl_sync(FULL, node, 0);
-        if (node >= a.bulk) break;
+        if (BATCH) {
+            long long item = 0;
+            if (lane == 0) item = (long long)atomicAdd(&bw.queue[0], 1ULL);
+            item = __shfl_sync(FULL, item, 0);
+            if (item >= bw.n_items) break;
+            const int2 wi = bw.items[item];
+            if (wi.x != cur_model) {
+                __syncwarp();
+                const int *src = reinterpret_cast<const int *>(bw.models + wi.x);
+                int *dst = reinterpret_cast<int *>(&margs[wib]);
+                for (int k = lane; k < (int)(sizeof(RFArgs) / sizeof(int)); k += 32) dst[k] = src[k];
+                __syncwarp();
+                cur_model = wi.x;
+            }
+            node = wi.y;
+        } else {
+            if (lane == 0) node = (int)atomicAdd(&a0.counters[0], 1ULL);
+            node = __shfl_sync(FULL, node, 0);
+            if (node >= a0.bulk) break;
+        }
+        const RFArgs &a = BATCH ? margs[wib] : a0;
         KahanF acc0a, acc0b, acc2a, acc2b;  // lines lane and lane+32, compensated FP32
         KahanF accEa, accEb, accLa, accLb;  // J_eff and L* of the same lines (split field only)
         const bool split = (a.JE != nullptr);
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                     const double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
-                    int2 *wl = wbase + (size_t)lane * a.n_depth;
+                    int2 *wl = wbase + (size_t)lane * n_depth;
                     // distance left to the sphere exit as an unevaluated float pair
                     // (rh + rl), decremented exactly by each step
                     float rh = (float)sexit, rl = (float)(sexit - (double)rh);
@@ -236,7 +238,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                             }
                         }
                         const float delta = (bj < 0) ? tsph : bnum / bden;
-                        if (K >= a.n_depth) { over = true; break; }
+                        if (K >= n_depth) { over = true; break; }
                         wl[K] = make_int2(c, (int)roundf(delta / a.dx32));  // nint(delta_x/dx)
                         K++;
                         if (bj < 0) break;
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                 // ---- (3)+(4) channel integration of each ray of the batch ----
                 for (int rr = 0; rr < nr; rr++) {
                     const int Kr = B.K[rr];
-                    const int2 *wl = wbase + (size_t)rr * a.n_depth;
+                    const int2 *wl = wbase + (size_t)rr * n_depth;
                     const float4 d4 = B.dir[rr];
                     const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
                     const float wgt = (float)dr[4], wgt2 = (float)dr[5];
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
                         float I[NS][NLG];
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
-                            const float bb = (l0 + l < a.L) ? (float)c_lines[l0 + l].bb_cmb : 0.f;
+                            const float bb = (l0 + l < a.L) ? a.bb[l0 + l] : 0.f;
 #pragma unroll
                             for (int s2 = 0; s2 < NS; s2++) I[s2][l] = bb;
                         }
@@ -470,18 +472,19 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a) {
         __syncwarp();
     }
     // segment count (every lane holds the same count)
-    if (lane == 0) atomicAdd(&a.counters[1], nseg);
+    if (lane == 0) atomicAdd(BATCH ? &bw.queue[1] : &a0.counters[1], nseg);
 }
 
 }  // namespace
 
 namespace {
 
-// upload per-line constants of the molecule
+// upload per-line constants of the molecule into the context
 int upload_lines(portal_ctx *c) {
     if (c->r_num > MAX_LINES)
         return set_err(c, PORTAL_ERR_ARG, "more than 64 radiative lines are not supported");
-    LineConst h[MAX_LINES];
+    std::vector<LineConst> h(c->r_num);
+    std::vector<float> bb(c->r_num);
     for (int k = 0; k < c->r_num; k++) {
         int lo = c->r_trans[2 * k] - 1, up = c->r_trans[2 * k + 1] - 1;
         h[k].nu = c->nu[k];
@@ -495,15 +498,20 @@ int upload_lines(portal_ctx *c) {
                       std::pow(std::exp(4.79924e-11 / 2.73 * c->nu[k]) - 1.0, -1.0);
         h[k].lo = lo;
         h[k].up = up;
+        bb[k] = (float)h[k].bb_cmb;
     }
-    PCHECK(c, cudaMemcpyToSymbolAsync(c_lines, h, sizeof(LineConst) * c->r_num, 0,
-                                      cudaMemcpyHostToDevice, c->stream));
+    if (c->linebuf.reserve(sizeof(LineConst) * c->r_num) || c->bbcmb.reserve(c->r_num))
+        return set_err(c, PORTAL_ERR_NOMEM, "line constants");
+    PCHECK(c, cudaMemcpyAsync(c->linebuf.p, h.data(), sizeof(LineConst) * c->r_num, cudaMemcpyHostToDevice,
+                              c->stream));
+    PCHECK(c, cudaMemcpyAsync(c->bbcmb.p, bb.data(), sizeof(float) * c->r_num, cudaMemcpyHostToDevice,
+                              c->stream));
     return PORTAL_OK;
 }
 
 template <int NS, int NLG, bool DUST>
 int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
-    auto kern = k_radiation_field<NS, NLG, DUST>;
+    auto kern = k_radiation_field<NS, NLG, DUST, false>;
     int nb = 0;
     PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, 0));
     if (nb < 1) nb = 1;
@@ -514,7 +522,7 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     a.walk = c->walk.p;
     PCHECK(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     timer_start(c, T_RF);
-    kern<<<grid, 256, 0, c->stream>>>(a);
+    kern<<<grid, 256, 0, c->stream>>>(a, RFBatch{});
     timer_stop(c, T_RF);
     PCHECK(c, cudaGetLastError());
     return PORTAL_OK;
@@ -538,14 +546,32 @@ int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
     return c->has_dust ? launch_rf<NS, 10, true>(c, a, n_depth) : launch_rf<NS, 10, false>(c, a, n_depth);
 }
 
+// the batched kernel for a channel count and line group
+template <int NS>
+const void *batch_kernel_ns(bool dust, int nlg) {
+    if (nlg == 10)
+        return dust ? (const void *)k_radiation_field<NS, 10, true, true>
+                    : (const void *)k_radiation_field<NS, 10, false, true>;
+    return dust ? (const void *)k_radiation_field<NS, 5, true, true>
+                : (const void *)k_radiation_field<NS, 5, false, true>;
+}
+const void *batch_kernel(int nch, bool dust, int nlg) {
+    if (nch <= 32) return batch_kernel_ns<1>(dust, nlg);
+    if (nch <= 64) return batch_kernel_ns<2>(dust, nlg);
+    if (nch <= 96) return batch_kernel_ns<3>(dust, nlg);
+    if (nch <= 160) return batch_kernel_ns<5>(dust, nlg);
+    return batch_kernel_ns<9>(dust, nlg);
+}
+
 }  // namespace
 
 namespace portal {
 
-// Runs the line table + radiation field on the device; J stays in c->J0/J2
-// (and the split field in c->JE/LS when `split`).
-int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
-                        int n_depth, long long *n_segments, int *n_failed, bool split) {
+// Validates the call, uploads the molecule's line constants and the
+// direction / channel tables, sizes the outputs and fills the kernel's
+// argument block (walk scratch and counters are the launcher's).
+int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx, int n_depth,
+               bool split, RFArgs *out) {
     if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
     if (c->nlev != (int)c->j_lev.size())
         return set_err(c, PORTAL_ERR_STATE, "cloud and molecule disagree on nlev");
@@ -584,40 +610,78 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     if (c->dirtab.reserve(dt.size()) || c->chtab.reserve(ct.size()) ||
         c->ltab.reserve((size_t)L * N) || c->J0.reserve((size_t)L * N) || c->J2.reserve((size_t)L * N))
         return set_err(c, PORTAL_ERR_NOMEM, "radiation-field buffers");
+    if (split && (c->JE.reserve((size_t)L * N) || c->LS.reserve((size_t)L * N)))
+        return set_err(c, PORTAL_ERR_NOMEM, "split-field buffers");
     PCHECK(c, cudaMemcpyAsync(c->dirtab.p, dt.data(), dt.size() * sizeof(double),
                               cudaMemcpyHostToDevice, c->stream));
     PCHECK(c, cudaMemcpyAsync(c->chtab.p, ct.data(), ct.size() * sizeof(float),
                               cudaMemcpyHostToDevice, c->stream));
-    PCHECK(c, cudaMemsetAsync(c->J0.p, 0, (size_t)L * N * sizeof(double), c->stream));
-    PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), c->stream));
-    PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), c->stream));
-    c->ali_valid = false;
-    if (split) {
-        if (c->JE.reserve((size_t)L * N) || c->LS.reserve((size_t)L * N))
-            return set_err(c, PORTAL_ERR_NOMEM, "split-field buffers");
-        PCHECK(c, cudaMemsetAsync(c->JE.p, 0, (size_t)L * N * sizeof(double), c->stream));
-        PCHECK(c, cudaMemsetAsync(c->LS.p, 0, (size_t)L * N * sizeof(double), c->stream));
-    }
-    // line table
-    {
-        long long tot = (long long)N * L;
-        timer_start(c, T_LINETAB);
-        k_line_table<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(
-            N, L, c->tx * dx, c->levp.p, c->nlev, c->b64.p, c->dustp.p, c->tdust.p, c->ltab.p);
-        timer_stop(c, T_LINETAB);
-        PCHECK(c, cudaGetLastError());
-    }
+    // the host vectors go out of scope: the copies must have happened
+    PCHECK(c, cudaStreamSynchronize(c->stream));
     RFArgs a;
     a.N = N; a.bulk = c->bulk; a.L = L; a.nvel = nvel; a.nch = nch; a.ndir = ndir; a.n_depth = n_depth;
     a.dx32 = (float)dx;
     a.pos = c->pos64.p; a.bvec = c->bvec64.p; a.ab = c->ab.p; a.cellv = c->cellv.p;
     a.off = c->nb_off.p; a.idx = c->nb_idx.p; a.edge = c->edge.p; a.ltab = c->ltab.p;
-    a.dirs = c->dirtab.p; a.chq = c->chtab.p; a.chw = c->chtab.p + nch;
+    a.dirs = c->dirtab.p; a.chq = c->chtab.p; a.chw = c->chtab.p + nch; a.bb = c->bbcmb.p;
     a.gx = gvec[0]; a.gy = gvec[1]; a.gz = gvec[2];
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
     a.JE = split ? c->JE.p : nullptr;
     a.LS = split ? c->LS.p : nullptr;
     a.walk = nullptr;
+    // the line table's transfer step (main_para.f90:135 dx times r_max)
+    c->rf_dxp = c->tx * dx;
+    *out = a;
+    return PORTAL_OK;
+}
+
+// The per-pass device work before the walk: zeroed outputs and the line
+// table from the current populations.  Stream-ordered only (capturable).
+int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s) {
+    const int L = c->r_num, N = c->N;
+    PCHECK(c, cudaMemsetAsync(c->J0.p, 0, (size_t)L * N * sizeof(double), s));
+    PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), s));
+    PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), s));
+    if (a.JE) {
+        PCHECK(c, cudaMemsetAsync(c->JE.p, 0, (size_t)L * N * sizeof(double), s));
+        PCHECK(c, cudaMemsetAsync(c->LS.p, 0, (size_t)L * N * sizeof(double), s));
+    }
+    const long long tot = (long long)N * L;
+    k_line_table<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
+        N, L, c->rf_dxp, reinterpret_cast<const LineConst *>(c->linebuf.p), c->levp.p, c->nlev, c->b64.p,
+        c->dustp.p, c->tdust.p, c->ltab.p);
+    PCHECK(c, cudaGetLastError());
+    return PORTAL_OK;
+}
+
+int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int *blocks) {
+    const void *k = batch_kernel(nch, dust, nlg);
+    *blocks = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 256, 0);
+    return e == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
+}
+
+int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, const RFBatch &bw) {
+    const void *k = batch_kernel(nch, dust, nlg);
+    RFArgs a0{};
+    RFBatch b = bw;
+    void *args[] = {&a0, &b};
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(256), args, 0, s);
+    return e == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
+}
+
+// Runs the line table + radiation field on the device; J stays in c->J0/J2
+// (and the split field in c->JE/LS when `split`).
+int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
+                        int n_depth, long long *n_segments, int *n_failed, bool split) {
+    RFArgs a;
+    int rc = rf_prepare(c, nth, nph, nvel, gvec, dx, n_depth, split, &a);
+    if (rc) return rc;
+    c->ali_valid = false;
+    timer_start(c, T_LINETAB);
+    if ((rc = rf_pass(c, a, c->stream))) return rc;
+    timer_stop(c, T_LINETAB);
+    const int nch = a.nch;
     if (nch <= 32) rc = dispatch_nlg<1>(c, a, n_depth);
     else if (nch <= 64) rc = dispatch_nlg<2>(c, a, n_depth);
     else if (nch <= 96) rc = dispatch_nlg<3>(c, a, n_depth);

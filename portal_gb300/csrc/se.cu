@@ -32,7 +32,7 @@
 #include <cmath>
 #include <map>
 
-#include "common.cuh"
+#include "internal.cuh"
 
 namespace portal {
 void coupling_constants(int which, int j, int k, int j2, int k2, double *c0, double *c2);
@@ -43,37 +43,6 @@ namespace {
 
 constexpr double A_TO_B = 6.781962e49;  // pop_eqs.f90:419
 constexpr double HK = 4.79924e-11;      // pop_eqs.f90:535
-
-struct SEArgs {
-    int N, bulk, c_dim, n_trans, nlev, L, c_temp, c_num, c_par, nent;
-    const double *__restrict__ J0;
-    const double *__restrict__ J2;
-    const double *__restrict__ JE;      // J0_eff (r_num, N) or null
-    const double *__restrict__ LS;      // L* (r_num, N) or null
-    const double *__restrict__ h2;
-    const double *__restrict__ tkin;
-    const double *__restrict__ ab;
-    // per transition
-    const int *__restrict__ tr_rad;
-    const int *__restrict__ tr_col;
-    const double *__restrict__ tr_nu;
-    const double *__restrict__ tr_A;
-    const double *__restrict__ tr_B21;
-    const double *__restrict__ col_temps;
-    const double *__restrict__ Cji;
-    // program over the matrix entries
-    const int *__restrict__ ent_off;
-    const int *__restrict__ ent_pos;
-    const int *__restrict__ term_f;
-    const double *__restrict__ term_c;
-    const int *__restrict__ norm_col;   // (nlev) count_array
-    const double *__restrict__ norm_val;
-    const int *__restrict__ pack;       // (2 nlev) rho index or -1
-    double *pops;                       // (N, 2 nlev) column-major
-    double *jj20;                       // (N, L) or null
-    int *status;
-    int *nfail;
-};
 
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -160,21 +129,47 @@ __host__ __device__ inline size_t se_warp_bytes(int n, int n_trans) {
     return (b + 15) & ~(size_t)15;
 }
 
-__global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a) {
+// One warp per node.  BATCH: the work items are (model, node) pairs of many
+// models (SEBatch); each warp copies its current model's argument block into
+// shared memory, and the dynamic shared memory per warp fits the largest
+// model.  Otherwise the nodes of the one model a0.
+template <bool BATCH>
+__global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ SEArgs margs[BATCH ? 8 : 1];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int n = a.c_dim;
-    unsigned char *base = smem + se_warp_bytes(n, a.n_trans) * wib;
-    double *A64 = (double *)base;
-    double *feat = A64 + (size_t)n * n;
-    double *x = feat + NF * (size_t)a.n_trans;
-    double *r = x + n;
-    float *LU = (float *)(r + n);
-    float *d32 = LU + (size_t)n * n;
-    float *scl = d32 + n;
-    int *piv = (int *)(scl + n);
+    const long long n_items = BATCH ? bw.n_items : (long long)a0.bulk;
+    const size_t wbytes = BATCH ? bw.warp_bytes : se_warp_bytes(a0.c_dim, a0.n_trans);
+    unsigned char *base = smem + wbytes * wib;
+    int cur_model = -1;
 
-    for (int node = blockIdx.x * nw + wib; node < a.bulk; node += gridDim.x * nw) {
+    for (long long item = (long long)blockIdx.x * nw + wib; item < n_items; item += (long long)gridDim.x * nw) {
+        int node;
+        if (BATCH) {
+            const int2 wi = bw.items[item];
+            if (wi.x != cur_model) {
+                __syncwarp();
+                const int *src = reinterpret_cast<const int *>(bw.models + wi.x);
+                int *dst = reinterpret_cast<int *>(&margs[wib]);
+                for (int k = lane; k < (int)(sizeof(SEArgs) / sizeof(int)); k += 32) dst[k] = src[k];
+                __syncwarp();
+                cur_model = wi.x;
+            }
+            node = wi.y;
+        } else {
+            node = (int)item;
+        }
+        const SEArgs &a = BATCH ? margs[wib] : a0;
+        const int n = a.c_dim;
+        double *A64 = (double *)base;
+        double *feat = A64 + (size_t)n * n;
+        double *x = feat + NF * (size_t)a.n_trans;
+        double *r = x + n;
+        float *LU = (float *)(r + n);
+        float *d32 = LU + (size_t)n * n;
+        float *scl = d32 + n;
+        int *piv = (int *)(scl + n);
+        (void)r;
         if (!(a.ab[node] > 0.0)) continue;  // main_para.f90:213 (pops stay 0)
         const double T = a.tkin[node], nH2 = a.h2[node];
         // ---- features (make_AC miscellaneous.f90:331-390) ----
@@ -513,7 +508,9 @@ int prepare_se(portal_ctx *c, int kmax) {
     return PORTAL_OK;
 }
 
-int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
+// Validates kmax, builds the SE program of the molecule (once per kmax),
+// sizes the outputs and fills the kernel's argument block.
+int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
     if (kmax < 2 || (kmax & 1))
         return set_err(c, PORTAL_ERR_ARG, "kmax must be even and >= 2 (trace_node packs rho^2_0)");
@@ -521,15 +518,9 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
     if (rc) return rc;
     const int n = c->c_dim;
     const size_t wb = se_warp_bytes(n, c->n_trans);
-    int wpb = (int)std::min<size_t>(8, (200 * 1024) / wb);
-    if (wpb < 1) return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
-    const size_t smem = wb * wpb;
-    PCHECK(c, cudaFuncSetAttribute(k_solve_se, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (wb > 200 * 1024) return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
     if (c->pops.reserve((size_t)c->N * 2 * c->nlev) || c->jj20.reserve((size_t)c->N * c->r_num))
         return set_err(c, PORTAL_ERR_NOMEM, "SE outputs");
-    PCHECK(c, cudaMemsetAsync(c->pops.p, 0, (size_t)c->N * 2 * c->nlev * sizeof(double), c->stream));
-    PCHECK(c, cudaMemsetAsync(c->jj20.p, 0, (size_t)c->N * c->r_num * sizeof(double), c->stream));
-    PCHECK(c, cudaMemsetAsync(c->counters.p + 2, 0, sizeof(unsigned long long), c->stream));
     SEArgs a;
     a.N = c->N; a.bulk = c->bulk; a.c_dim = n; a.n_trans = c->n_trans; a.nlev = c->nlev; a.L = c->r_num;
     a.c_temp = c->c_temp; a.c_num = c->c_num; a.c_par = c->c_par; a.nent = c->se_ni;
@@ -546,11 +537,54 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
     a.Cji = D + c->se_offs[13];
     a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
     a.nfail = (int *)(c->counters.p + 2);
+    *out = a;
+    if (warp_bytes) *warp_bytes = wb;
+    return PORTAL_OK;
+}
+
+// The per-pass device work before the solve: zeroed outputs and failure
+// count.  Stream-ordered only (capturable).
+int se_pass(portal_ctx *c, cudaStream_t s) {
+    PCHECK(c, cudaMemsetAsync(c->pops.p, 0, (size_t)c->N * 2 * c->nlev * sizeof(double), s));
+    PCHECK(c, cudaMemsetAsync(c->jj20.p, 0, (size_t)c->N * c->r_num * sizeof(double), s));
+    PCHECK(c, cudaMemsetAsync(c->counters.p + 2, 0, sizeof(unsigned long long), s));
+    return PORTAL_OK;
+}
+
+int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) {
+    const size_t smem = warp_bytes * warps_per_block;
+    *blocks = 0;
+    if (cudaFuncSetAttribute(k_solve_se<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return PORTAL_ERR_CUDA;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solve_se<true>, 32 * warps_per_block, smem) ==
+                   cudaSuccess
+               ? PORTAL_OK
+               : PORTAL_ERR_CUDA;
+}
+
+// (the kernel's dynamic shared memory limit must have been raised by
+// se_batch_blocks_per_sm for at least this many warps)
+int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw) {
+    const size_t smem = bw.warp_bytes * warps_per_block;
+    k_solve_se<true><<<grid, 32 * warps_per_block, smem, s>>>(SEArgs{}, bw);
+    return cudaGetLastError() == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
+}
+
+int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
+    SEArgs a;
+    size_t wb = 0;
+    int rc = se_prepare(c, kmax, &a, &wb);
+    if (rc) return rc;
+    const int wpb = (int)std::min<size_t>(8, (200 * 1024) / wb);
+    const size_t smem = wb * wpb;
+    PCHECK(c, cudaFuncSetAttribute(k_solve_se<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if ((rc = se_pass(c, c->stream))) return rc;
     int nb = 0;
-    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_solve_se, 32 * wpb, smem));
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_solve_se<false>, 32 * wpb, smem));
     int grid = c->sm_count * std::max(1, nb);
     timer_start(c, T_SE);
-    k_solve_se<<<grid, 32 * wpb, smem, c->stream>>>(a);
+    k_solve_se<false><<<grid, 32 * wpb, smem, c->stream>>>(a, SEBatch{});
     timer_stop(c, T_SE);
     PCHECK(c, cudaGetLastError());
     int nf = 0;
