@@ -232,10 +232,13 @@ class Context:
                                                        C.byref(nseg)))
         return J0, J2, JE, LS, st
 
-    def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False, out=None):
+    def solve_se(self, kmax, J0=None, J2=None, fetch: bool = True, jj20: bool = False, out=None,
+                 rates: bool = False):
         """pol_pops as (N, 2*nlev) (reference pol_pops(node,:)), status.
         out: a float64 (2*nlev, N) C-contiguous buffer (the reference's
-        pol_pops(N, 2*nlev) memory) to receive the result without a copy."""
+        pol_pops(N, 2*nlev) memory) to receive the result without a copy.
+        jj20 / rates append J2/J0 (N, r_num) and the extra_info rates
+        (N, 3, 2*nlev: spontaneous, radiative, collisional)."""
         if out is not None:
             self._check(lib().portal_solve_se(self._h, kmax, None, None, _p(out), None, None, None))
             return out, None
@@ -244,10 +247,13 @@ class Context:
         st = np.zeros(self.N, dtype=np.int32) if fetch else None
         j0 = None if J0 is None else _f64(J0)
         j2 = None if J2 is None else _f64(J2)
-        self._check(lib().portal_solve_se(self._h, kmax, _p(j0), _p(j2), _p(pp), None, _p(jj), _p(st, P_I)))
+        rt = np.zeros((2 * self.nlev, 3, self.N)) if rates else None  # Fortran (N, 3, 2 nlev)
+        self._check(lib().portal_solve_se(self._h, kmax, _p(j0), _p(j2), _p(pp), _p(rt), _p(jj), _p(st, P_I)))
         out = (None if pp is None else pp.T.copy(), st)
         if jj20:
             out = out + (jj.T.copy(),)
+        if rates:
+            out = out + (np.transpose(rt, (2, 1, 0)).copy(),)
         return out
 
     def image(self, l1, l2, th_inc, ph_az, nvel, dvel, v0, im_pix, im_size, alpha=0.15,

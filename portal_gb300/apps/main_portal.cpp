@@ -6,8 +6,9 @@
 //
 // Outputs: <output_map>/pol_pops.dat (one line per node, rho^0_0 and
 // rho^2_0 per level, main_para.f90:271-275); with extra_info = 1 also
-// mag_field.dat (:158-167) and rad_anis.dat (J^2_0 / J^0_0 per line,
-// :296-300).  The rate files of extra_info (:278-294) are not produced.
+// mag_field.dat (:158-167), the rate files spont_rates.dat, rad_rates.dat,
+// col_rates.dat (:277-294) and rad_anis.dat (J^2_0 / J^0_0 per line,
+// :296-300).
 //
 // Two inputs the reference leaves implicit are explicit here:
 //   PORTAL_GVEC="gx gy gz"   the gauge vector (the reference draws it with an
@@ -134,8 +135,10 @@ int main(int argc, char **argv) {
     chk(portal_radiation_field(ctx, in.nth, in.nph, in.nvel, g, dx, in.n_depth, nullptr, nullptr, nullptr, &nseg),
         "portal_radiation_field");
     const int N = c.node_num, nlev = m.nlev;
-    std::vector<double> pops((size_t)N * 2 * nlev), jj((size_t)N * m.r_num);
-    chk(portal_solve_se(ctx, in.kmax, nullptr, nullptr, pops.data(), nullptr, jj.data(), nullptr),
+    std::vector<double> pops((size_t)N * 2 * nlev), jj((size_t)N * m.r_num), rates;
+    if (in.extra_info == 1) rates.resize((size_t)N * 3 * 2 * nlev);
+    chk(portal_solve_se(ctx, in.kmax, nullptr, nullptr, pops.data(), rates.empty() ? nullptr : rates.data(),
+                        jj.data(), nullptr),
         "portal_solve_se");
     portal_destroy(ctx);
     if (!write_rows(out + "/pol_pops.dat", pops, N, 2 * nlev)) return fail("cannot write " + out + "/pol_pops.dat");
@@ -146,8 +149,18 @@ int main(int argc, char **argv) {
                 mf[(size_t)i + (size_t)N * k] = c.xyz[3 * (size_t)i + k];
                 mf[(size_t)i + (size_t)N * (3 + k)] = bvec[3 * (size_t)i + k];
             }
-        if (!write_rows(out + "/mag_field.dat", mf, N, 6) || !write_rows(out + "/rad_anis.dat", jj, N, m.r_num))
+        if (!write_rows(out + "/mag_field.dat", mf, N, 6))
             return fail("cannot write the extra_info files");
+        // pol_rates(N, 3, 2 nlev): one file per kind (main_para.f90:277-294)
+        const char *names[3] = {"/spont_rates.dat", "/rad_rates.dat", "/col_rates.dat"};
+        std::vector<double> one((size_t)N * 2 * nlev);
+        for (int k = 0; k < 3; k++) {
+            for (int cc = 0; cc < 2 * nlev; cc++)
+                for (int i = 0; i < N; i++)
+                    one[(size_t)i + (size_t)N * cc] = rates[(size_t)i + (size_t)N * (k + 3 * (size_t)cc)];
+            if (!write_rows(out + names[k], one, N, 2 * nlev)) return fail("cannot write the extra_info files");
+        }
+        if (!write_rows(out + "/rad_anis.dat", jj, N, m.r_num)) return fail("cannot write the extra_info files");
     }
     printf("main_portal: %d nodes, %lld ray segments\n", c.bulk_node_num, nseg);
     return 0;

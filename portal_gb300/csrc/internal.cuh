@@ -56,8 +56,11 @@ struct SEArgs {
     const int *__restrict__ norm_col;   // (nlev) count_array
     const double *__restrict__ norm_val;
     const int *__restrict__ pack;       // (2 nlev) rho index or -1
+    const int *__restrict__ row_off;    // (c_dim + 1) entries of each matrix row,
+    const int *__restrict__ row_ent;    // ascending column (the rates' summation order)
     double *pops;                       // (N, 2 nlev) column-major
     double *jj20;                       // (N, L) or null
+    double *rates;                      // (N, 3, 2 nlev) column-major or null
     int *status;
     int *nfail;
 };

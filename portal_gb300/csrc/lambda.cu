@@ -35,7 +35,7 @@
 namespace portal {
 int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx,
                         int n_depth, long long *n_segments, int *n_failed, bool split);
-int run_solve_se(portal_ctx *c, int kmax, int *n_singular);
+int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates);
 }  // namespace portal
 using namespace portal;
 
@@ -211,7 +211,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
         if ((rc = run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, &nseg, nullptr, split))) return rc;
         nseg_tot += nseg;
         int nsing = 0;
-        if ((rc = run_solve_se(c, kmax, &nsing))) return rc;
+        if ((rc = run_solve_se(c, kmax, &nsing, false))) return rc;
         if (nsing) return set_err(c, PORTAL_ERR_SINGULAR, std::to_string(nsing) + " singular SE systems");
         PCHECK(c, cudaMemsetAsync(c->counters.p + 3, 0, sizeof(unsigned long long), c->stream));
         k_update<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, c->pops.p, c->nmol.p, c->ab.p, jl.p, c->levp.p,

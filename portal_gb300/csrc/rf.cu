@@ -135,7 +135,7 @@ struct RayBatch {
 // each warp copies the argument block of its current model into shared
 // memory.  Otherwise the nodes of the one model a0.
 template <int NS, int NLG, bool DUST, bool BATCH>
-__global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch bw) {
+__global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiation_field(RFArgs a0, RFBatch bw) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -271,12 +271,15 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch b
                     nseg += (unsigned long long)Kr;
                     const int2 w0 = wl[0];
                     for (int l0 = 0; l0 < a.L; l0 += NLG) {
-                        float I[NS][NLG];
+                        // intensities of the lane's channels: slot pairs (s, s+1) in one
+                        // float2 (packed FP32x2 arithmetic), an odd last slot in .x
+                        float2 I2[(NS + 1) / 2][NLG];
+#define IV(s, l) (((s) & 1) ? I2[(s) >> 1][l].y : I2[(s) >> 1][l].x)
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
                             const float bb = (l0 + l < a.L) ? a.bb[l0 + l] : 0.f;
 #pragma unroll
-                            for (int s2 = 0; s2 < NS; s2++) I[s2][l] = bb;
+                            for (int s2 = 0; s2 < NS; s2++) IV(s2, l) = bb;
                         }
                         for (int hi = Kr - 1; hi >= 1; hi -= 32) {
                             const int nc = min(32, hi);
@@ -343,8 +346,8 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch b
                                                 const float Sv = fmaf(Su, g[s2], Jdu) / tau;
                                                 const float x = tau * LOG2E_F;
                                                 const float om = one_minus_exp(x, ex2(-x));
-                                                const float In = fmaf(om, Sv - I[s2][l], I[s2][l]);
-                                                I[s2][l] = (tau > 1e-30f) ? In : I[s2][l];
+                                                const float In = fmaf(om, Sv - IV(s2, l), IV(s2, l));
+                                                IV(s2, l) = (tau > 1e-30f) ? In : IV(s2, l);
                                             }
                                         }
                                     } else {
@@ -356,12 +359,21 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch b
                                         // 0 < tau < 2^-54 rounds to a zero weight as in FP64.
                                         // Branch-free, so the NS x NLG update chains of a cell
                                         // interleave (a uniform thin-line branch measured 7 %
-                                        // slower).
+                                        // slower).  Channel-slot pairs go through the packed
+                                        // FP32x2 pipe (one issue slot for two updates).
+                                        const float2 A2 = make_float2(Au, Au), S2 = make_float2(Su, Su);
 #pragma unroll
-                                        for (int s2 = 0; s2 < NS; s2++) {
-                                            const float x = Au * g[s2];
+                                        for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
+                                            const float2 x = __fmul2_rn(A2, make_float2(g[s2], g[s2 + 1]));
+                                            const float2 om = one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
+                                            float2 &Ip = I2[s2 >> 1][l];
+                                            Ip = __ffma2_rn(om, __ffma2_rn(Ip, make_float2(-1.f, -1.f), S2), Ip);
+                                        }
+                                        if (NS & 1) {
+                                            const float x = Au * g[NS - 1];
                                             const float om = one_minus_exp(x, ex2(-x));
-                                            I[s2][l] = fmaf(om, Su - I[s2][l], I[s2][l]);
+                                            float &Is = I2[NS >> 1][l].x;
+                                            Is = fmaf(om, Su - Is, Is);
                                         }
                                     }
                                 }
@@ -398,10 +410,10 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch b
                                         const float x = tau * LOG2E_F;
                                         const float e = ex2(-x);
                                         const float om = one_minus_exp(x, e);
-                                        const float Io = fmaf(om, Sv - I[s2][l], I[s2][l]);
+                                        const float Io = fmaf(om, Sv - IV(s2, l), IV(s2, l));
                                         part[l] = fmaf(a.chw[ch], Io, part[l]);
                                         if (split) {
-                                            pe[l] = fmaf(a.chw[ch], fmaf(om, Sd - I[s2][l], I[s2][l]), pe[l]);
+                                            pe[l] = fmaf(a.chw[ch], fmaf(om, Sd - IV(s2, l), IV(s2, l)), pe[l]);
                                             pl[l] = fmaf(a.chw[ch], lf * om, pl[l]);
                                         }
                                     }
@@ -450,6 +462,7 @@ __global__ void __launch_bounds__(256, 1) k_radiation_field(RFArgs a0, RFBatch b
                 __syncwarp();
             }
         }
+#undef IV
         if (lane < a.L) {
             a.J0[(size_t)node * a.L + lane] = (st == 0) ? acc0a.value() : 0.0;
             a.J2[(size_t)node * a.L + lane] = (st == 0) ? acc2a.value() : 0.0;

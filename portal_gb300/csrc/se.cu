@@ -164,12 +164,11 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
         double *A64 = (double *)base;
         double *feat = A64 + (size_t)n * n;
         double *x = feat + NF * (size_t)a.n_trans;
-        double *r = x + n;
+        double *r = x + n;   // scratch (the rates)
         float *LU = (float *)(r + n);
         float *d32 = LU + (size_t)n * n;
         float *scl = d32 + n;
         int *piv = (int *)(scl + n);
-        (void)r;
         if (!(a.ab[node] > 0.0)) continue;  // main_para.f90:213 (pops stay 0)
         const double T = a.tkin[node], nH2 = a.h2[node];
         // ---- features (make_AC miscellaneous.f90:331-390) ----
@@ -302,6 +301,47 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
                 a.pops[(size_t)node + (size_t)a.N * (2 * lane + 1)] = 0.0;
             }
         }
+        if (a.rates) {
+            // extra_info rates (em_coefs.f90:188-198): per component i and kind
+            // k (spontaneous, radiative, collisional), sum_j |M_k(i,j)| rho_j,
+            // M_k the part of setup_stateq's matrix from A, from B J, from C
+            // (pop_eqs.f90:424-426, 510-512, 558-559, 599-645); the unsplit
+            // field's values (f0, f2) stand for f5, f6.  Row by row in
+            // ascending column order, as the reference sums.
+            for (int k = 0; k < 3; k++) {
+                for (int i = lane; i < n; i += 32) {
+                    double acc = 0.0;
+                    if (!(st & PORTAL_NODE_SINGULAR))
+                        for (int q = a.row_off[i]; q < a.row_off[i + 1]; q++) {
+                            const int e = a.row_ent[q];
+                            double v = 0.0;
+                            for (int t = a.ent_off[e]; t < a.ent_off[e + 1]; t++) {
+                                const int tf = a.term_f[t], f = tf % NF, base = tf - f;
+                                const int kind = (f == 2 || f == 6) ? 0 : (f == 3 || f == 4) ? 2 : 1;
+                                if (kind != k) continue;
+                                const int fu = (f == 5) ? 0 : (f == 6) ? 2 : f;
+                                v += a.term_c[t] * feat[base + fu];
+                            }
+                            acc += fabs(v) * x[a.ent_pos[e] / n];
+                        }
+                    r[i] = acc;
+                }
+                __syncwarp();
+                // packing as the populations (main_sub.f90:116-135): K = 2
+                // components of J = 0 levels are 0; a NaN population zeroes the
+                // K = 2 rate entry (twice, as in the reference)
+                for (int c2 = lane; c2 < 2 * a.nlev; c2 += 32) {
+                    const int pidx = a.pack[c2];
+                    double v = (pidx >= 0) ? r[pidx] : 0.0;
+                    if (c2 & 1) {
+                        const double p0 = x[a.pack[c2 - 1]];
+                        if (p0 != p0) v = 0.0;
+                    }
+                    a.rates[(size_t)node + (size_t)a.N * (k + 3 * (size_t)c2)] = v;
+                }
+                __syncwarp();
+            }
+        }
         if (a.jj20)
             for (int l = lane; l < a.L; l += 32)
                 a.jj20[(size_t)node + (size_t)a.N * l] =
@@ -320,7 +360,7 @@ struct Program {
     int c_dim = 0, n_trans = 0;
     std::vector<int> count_array, tr_lo, tr_up, tr_rad, tr_col;
     std::vector<double> tr_nu, tr_A, tr_B21;
-    std::vector<int> ent_off, ent_pos, term_f, pack;
+    std::vector<int> ent_off, ent_pos, term_f, pack, row_off, row_ent;
     std::vector<double> term_c;
 };
 
@@ -462,6 +502,16 @@ void build_program(const portal_ctx *c, int kmax, Program &P) {
         for (auto &tc : kv.second) { P.term_f.push_back(tc.first); P.term_c.push_back(tc.second); }
         P.ent_off.push_back((int)P.term_f.size());
     }
+    // the entries of each row in ascending column order (ent is keyed by
+    // c1 + n c2: column-major)
+    P.row_off.assign(n + 1, 0);
+    for (int pos : P.ent_pos) P.row_off[pos % n + 1]++;
+    for (int i = 0; i < n; i++) P.row_off[i + 1] += P.row_off[i];
+    P.row_ent.assign(P.ent_pos.size(), 0);
+    {
+        std::vector<int> fill(P.row_off.begin(), P.row_off.end() - 1);
+        for (int e = 0; e < (int)P.ent_pos.size(); e++) P.row_ent[fill[P.ent_pos[e] % n]++] = e;
+    }
     // packing main_sub.f90:112-129
     P.pack.assign(2 * nlev, -1);
     for (int i = 0; i < nlev; i++) {
@@ -487,7 +537,7 @@ int prepare_se(portal_ctx *c, int kmax) {
     for (int i = 0; i < c->nlev; i++) norm_val[i] = std::sqrt(2.0 * c->j_lev[i] + 1.0);
     size_t o_rad = putI(P.tr_rad), o_col = putI(P.tr_col), o_eoff = putI(P.ent_off),
            o_epos = putI(P.ent_pos), o_tf = putI(P.term_f), o_nc = putI(P.count_array),
-           o_pack = putI(P.pack);
+           o_pack = putI(P.pack), o_roff = putI(P.row_off), o_rent = putI(P.row_ent);
     size_t o_nu = putD(P.tr_nu), o_A = putD(P.tr_A), o_B = putD(P.tr_B21), o_tc = putD(P.term_c),
            o_nv = putD(norm_val), o_ct = putD(c->col_temps), o_C = putD(c->Cji);
     if (c->se_ints.reserve(I.size()) || c->se_dbls.reserve(D.size()))
@@ -505,6 +555,7 @@ int prepare_se(portal_ctx *c, int kmax) {
     c->se_offs[4] = o_tf; c->se_offs[5] = o_nc; c->se_offs[6] = o_pack;
     c->se_offs[7] = o_nu; c->se_offs[8] = o_A; c->se_offs[9] = o_B; c->se_offs[10] = o_tc;
     c->se_offs[11] = o_nv; c->se_offs[12] = o_ct; c->se_offs[13] = o_C;
+    c->se_offs[14] = o_roff; c->se_offs[15] = o_rent;
     return PORTAL_OK;
 }
 
@@ -535,7 +586,9 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     a.tr_nu = D + c->se_offs[7]; a.tr_A = D + c->se_offs[8]; a.tr_B21 = D + c->se_offs[9];
     a.term_c = D + c->se_offs[10]; a.norm_val = D + c->se_offs[11]; a.col_temps = D + c->se_offs[12];
     a.Cji = D + c->se_offs[13];
+    a.row_off = I + c->se_offs[14]; a.row_ent = I + c->se_offs[15];
     a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
+    a.rates = nullptr;
     a.nfail = (int *)(c->counters.p + 2);
     *out = a;
     if (warp_bytes) *warp_bytes = wb;
@@ -571,11 +624,17 @@ int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch
     return cudaGetLastError() == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
 }
 
-int run_solve_se(portal_ctx *c, int kmax, int *n_singular) {
+int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates) {
     SEArgs a;
     size_t wb = 0;
     int rc = se_prepare(c, kmax, &a, &wb);
     if (rc) return rc;
+    if (rates) {
+        const size_t nr = (size_t)c->N * 3 * 2 * c->nlev;
+        if (c->rates.reserve(nr)) return set_err(c, PORTAL_ERR_NOMEM, "rates output");
+        PCHECK(c, cudaMemsetAsync(c->rates.p, 0, nr * sizeof(double), c->stream));
+        a.rates = c->rates.p;
+    }
     const int wpb = (int)std::min<size_t>(8, (200 * 1024) / wb);
     const size_t smem = wb * wpb;
     PCHECK(c, cudaFuncSetAttribute(k_solve_se<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -617,7 +676,7 @@ extern "C" int portal_solve_se(portal_ctx *c, int kmax, const double *J0, const 
     }
     timers_reset(c);
     int nsing = 0;
-    int rc = portal::run_solve_se(c, kmax, &nsing);
+    int rc = portal::run_solve_se(c, kmax, &nsing, rates != nullptr);
     if (rc) return rc;
     if (pol_pops)
         PCHECK(c, cudaMemcpyAsync(pol_pops, c->pops.p, (size_t)c->N * 2 * c->nlev * sizeof(double),
@@ -626,10 +685,9 @@ extern "C" int portal_solve_se(portal_ctx *c, int kmax, const double *J0, const 
         PCHECK(c, cudaMemcpyAsync(JJ_20, c->jj20.p, LN * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (status)
         PCHECK(c, cudaMemcpyAsync(status, c->status.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    if (rates) {
-        // rates output (extra_info = 1) is not implemented on the device yet
-        return set_err(c, PORTAL_ERR_ARG, "portal_solve_se: rates output is not supported; pass NULL");
-    }
+    if (rates)
+        PCHECK(c, cudaMemcpyAsync(rates, c->rates.p, (size_t)c->N * 3 * 2 * c->nlev * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
     if (nsing) return set_err(c, PORTAL_ERR_SINGULAR, std::to_string(nsing) + " singular SE systems");
     return PORTAL_OK;

@@ -111,8 +111,13 @@ def test_main_and_finish_portal_end_to_end(case):
         ctx.set_molecule(mol)
         ctx.set_cloud(cloud)
         ctx.radiation_field(rc, fetch=False)
-        pops, _ = ctx.solve_se(rc.kmax)
+        pops, _, jj, rates = ctx.solve_se(rc.kmax, jj20=True, rates=True)
         np.testing.assert_allclose(pops_file, pops, rtol=1e-15, atol=0)
+        # extra_info = 1: the three rate files and the anisotropy
+        for k, name in enumerate(("spont_rates.dat", "rad_rates.dat", "col_rates.dat")):
+            np.testing.assert_allclose(np.loadtxt(os.path.join(d, name)), rates[:, k, :], rtol=1e-15, atol=0)
+        got = np.loadtxt(os.path.join(d, "rad_anis.dat")).reshape(jj.shape)
+        np.testing.assert_allclose(got, jj, rtol=1e-15, atol=0, equal_nan=True)
         im = dict(l1=[1], l2=[2], th_inc=[0.78539816339], ph_az=[0.0], nvel=8, dvel=50.0, v0=0.0, im_pix=12,
                   im_size=0.7)
         lime.write_finish_input(os.path.join(d, "finish.dat"), im["l1"], im["l2"], im["th_inc"], im["ph_az"],

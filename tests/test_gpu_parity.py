@@ -68,6 +68,27 @@ def test_solve_se_same_J_cfg1(ctx, cfg1, cfg1_oracle):
     np.testing.assert_allclose((pops[:, 0::2] * g).sum(1), 1.0, rtol=1e-12)
 
 
+def test_extra_info_rates_cfg1(ctx, cfg1, cfg1_oracle):
+    """The extra_info rates (spontaneous, radiative, collisional per
+    component, em_coefs.f90:188-198 packed like the populations) and
+    J2/J0 from the same J as the oracle."""
+    cloud, mol, rc = cfg1
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    for kmax in (2, rc.kmax):
+        pops, st, jj, rt = ctx.solve_se(kmax, cfg1_oracle["J0"], cfg1_oracle["J2"], jj20=True, rates=True)
+        _, _, _, ort = cfg1_oracle["P"].solve_se(kmax, cfg1_oracle["J0"], cfg1_oracle["J2"], rates=True)
+        bulk = cloud.bulk_node_num
+        scale = np.abs(ort[:bulk]).max(axis=2, keepdims=True) + 1e-300
+        assert (np.abs(rt[:bulk] - ort[:bulk]) / scale).max() < 1e-10
+        assert np.abs(ort[:bulk]).max() > 0
+        assert not rt[bulk:].any()
+        with np.errstate(invalid="ignore", divide="ignore"):
+            want = cfg1_oracle["J2"] / cfg1_oracle["J0"]
+        live = cloud.ab_all[:bulk] > 0
+        np.testing.assert_allclose(jj[:bulk][live], want[:bulk][live], rtol=1e-15)
+
+
 def test_node_loop_chain_cfg1(ctx, cfg1, cfg1_oracle):
     """Device-resident chain radiation field -> SE against oracle -> oracle."""
     cloud, mol, rc = cfg1
