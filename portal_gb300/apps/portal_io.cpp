@@ -11,6 +11,8 @@
 #include <fstream>
 #include <random>
 #include <sstream>
+#include <thread>
+#include <type_traits>
 
 namespace portal_io {
 
@@ -21,17 +23,38 @@ static double f4(double x) { return (double)(float)x; }  // REAL*4 literal promo
 // ---------------------------------------------------------------------------
 
 ListReader::ListReader(const std::string &path) : path_(path) {
-    std::ifstream f(path);
+    FILE *f = fopen(path.c_str(), "rb");
     if (!f) return;
-    std::string l;
-    while (std::getline(f, l)) {
-        if (!l.empty() && l.back() == '\r') l.pop_back();
-        lines_.push_back(l);
+    fseek(f, 0, SEEK_END);
+    const long sz = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    buf_.resize(sz > 0 ? (size_t)sz : 0);
+    const size_t got = sz > 0 ? fread(&buf_[0], 1, (size_t)sz, f) : 0;
+    fclose(f);
+    buf_.resize(got);
+    size_t b = 0;
+    while (b < buf_.size()) {
+        const void *nl = memchr(buf_.data() + b, '\n', buf_.size() - b);
+        size_t e = nl ? (size_t)((const char *)nl - buf_.data()) : buf_.size();
+        size_t ee = e;
+        if (ee > b && buf_[ee - 1] == '\r') ee--;
+        lbeg_.push_back(b);
+        lend_.push_back(ee);
+        b = e + 1;
     }
     ok_ = true;
 }
 
-static void tokenize(const std::string &line, std::vector<std::string> &toks) {
+int io_threads() {
+    if (const char *e = getenv("PORTAL_THREADS")) {
+        const int t = atoi(e);
+        if (t > 0) return t;
+    }
+    const unsigned h = std::thread::hardware_concurrency();
+    return h ? (int)std::min(h, 64u) : 1;
+}
+
+static void tokenize(const char *line, size_t len, std::vector<std::string> &toks) {
     toks.clear();
     std::string cur;
     auto flush = [&]() {
@@ -50,7 +73,8 @@ static void tokenize(const std::string &line, std::vector<std::string> &toks) {
     };
     bool quote = false;
     char qc = 0;
-    for (char ch : line) {
+    for (size_t i = 0; i < len; i++) {
+        const char ch = line[i];
         if (quote) {
             if (ch == qc) { quote = false; flush(); }
             else cur.push_back(ch);
@@ -65,10 +89,94 @@ static void tokenize(const std::string &line, std::vector<std::string> &toks) {
 }
 
 bool ListReader::next_record() {
-    if (line_ >= lines_.size()) return false;
-    tokenize(lines_[line_++], toks_);
+    if (line_ >= lbeg_.size()) return false;
+    tokenize(buf_.data() + lbeg_[line_], lend_[line_] - lbeg_[line_], toks_);
+    line_++;
     pos_ = 0;
     return true;
+}
+
+namespace {
+
+inline bool is_sep(char ch) { return ch == ' ' || ch == '\t' || ch == ','; }
+
+// One line of exactly n plain numbers (no repeat counts, quotes, slashes or
+// D exponents: those take the general path) into out; false otherwise.
+template <typename T>
+bool parse_plain_line(const char *p, const char *end, size_t n, T *out) {
+    size_t k = 0;
+    char tmp[64];
+    while (true) {
+        while (p < end && is_sep(*p)) p++;
+        if (p >= end) break;
+        const char *q = p;
+        while (q < end && !is_sep(*q)) {
+            const char ch = *q;
+            if (ch == '*' || ch == '/' || ch == '\'' || ch == '"' || ch == 'd' || ch == 'D') return false;
+            q++;
+        }
+        if (k >= n || (size_t)(q - p) >= sizeof tmp) return false;
+        memcpy(tmp, p, (size_t)(q - p));
+        tmp[q - p] = 0;
+        char *ep = nullptr;
+        if (std::is_floating_point<T>::value) {
+            out[k] = (T)strtod(tmp, &ep);
+        } else {
+            out[k] = (T)strtol(tmp, &ep, 10);
+        }
+        if (ep != tmp + (q - p)) return false;  // the general path's token conversion would differ
+        k++;
+        p = q;
+    }
+    return k == n;
+}
+
+}  // namespace
+
+template <typename T>
+size_t ListReader::read_block(T *out, size_t n_rec, size_t n, int threads) {
+    const size_t avail = lbeg_.size() > line_ ? lbeg_.size() - line_ : 0;
+    const size_t m = std::min(n_rec, avail);
+    bool fast = m > 0;
+    if (fast) {
+        const int nt = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(threads, 1), m / 4096 + 1));
+        std::vector<char> okv(nt, 1);
+        std::vector<std::thread> th;
+        auto work = [&](int t) {
+            const size_t r0 = m * t / nt, r1 = m * (t + 1) / nt;
+            for (size_t r = r0; r < r1; r++) {
+                const size_t L = line_ + r;
+                if (!parse_plain_line<T>(buf_.data() + lbeg_[L], buf_.data() + lend_[L], n, out + r * n)) {
+                    okv[t] = 0;
+                    return;
+                }
+            }
+        };
+        for (int t = 1; t < nt; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+        for (char v : okv) fast = fast && v;
+    }
+    if (fast) {
+        line_ += m;
+        return m;
+    }
+    // the general list-directed path, record by record
+    std::vector<std::string> t;
+    size_t r = 0;
+    for (; r < n_rec; r++) {
+        if (!read(t, n)) break;
+        for (size_t k = 0; k < n; k++)
+            out[r * n + k] = std::is_floating_point<T>::value ? (T)to_double(t[k]) : (T)to_int(t[k]);
+    }
+    return r;
+}
+
+size_t ListReader::read_block_doubles(double *out, size_t n_rec, size_t n, int threads) {
+    return read_block<double>(out, n_rec, n, threads);
+}
+size_t ListReader::read_block_ints(int *out, size_t n_rec, size_t n, int threads) {
+    return read_block<int>(out, n_rec, n, threads);
 }
 
 bool ListReader::skip() { return next_record(); }
@@ -188,45 +296,66 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     if (N < 1) { err = grid + ": no points"; return false; }
     c.node_num = N;
     c.xyz.resize(3 * (size_t)N);
-    for (int i = 0; i < N; i++) {
-        if (!g.read_doubles(vd, 3)) { err = grid + ": point " + std::to_string(i + 1); return false; }
-        for (int k = 0; k < 3; k++) c.xyz[3 * (size_t)i + k] = vd[k];
-    }
+    const int nth = io_threads();
+    const size_t np = g.read_block_doubles(c.xyz.data(), (size_t)N, 3, nth);
+    if (np < (size_t)N) { err = grid + ": point " + std::to_string(np + 1); return false; }
     g.skip();
     if (!g.read(t, 2)) { err = grid + ": CELLS line"; return false; }
     const int ntet = to_int(t[1]);
-    // adj_list_no_delaunay miscellaneous.f90:910-1015: each tetrahedron gives
-    // its vertices the other three; SortUnique then sorts and de-duplicates
-    std::vector<std::vector<int>> nb(N);
-    for (int q = 0; q < ntet; q++) {
-        std::vector<int> vi;
-        if (!g.read_ints(vi, 5)) { err = grid + ": cell " + std::to_string(q + 1); return false; }
-        int v[4];
+    std::vector<int> cells(5 * (size_t)std::max(ntet, 0));
+    const size_t nc = g.read_block_ints(cells.data(), (size_t)std::max(ntet, 0), 5, nth);
+    if (nc < (size_t)std::max(ntet, 0)) { err = grid + ": cell " + std::to_string(nc + 1); return false; }
+    for (size_t q = 0; q < nc; q++)
         for (int k = 0; k < 4; k++) {
-            v[k] = vi[1 + k] + 1;
-            if (v[k] < 1 || v[k] > N) { err = grid + ": cell vertex out of range"; return false; }
+            const int v = cells[5 * q + 1 + k] + 1;
+            if (v < 1 || v > N) { err = grid + ": cell vertex out of range"; return false; }
         }
-        for (int k = 0; k < 4; k++)
-            for (int k2 = 0; k2 < 4; k2++)
-                if (k2 != k) nb[v[k] - 1].push_back(v[k2]);
-    }
-    int maxne = 0;
-    c.del_num_ne.assign(N, 0);
-    for (int i = 0; i < N; i++) {
-        if ((int)nb[i].size() > max_ne_temp) {  // miscellaneous.f90:1000-1004
-            err = "count_ne=" + std::to_string(nb[i].size()) + " while max_ne_temp=" +
+    // adj_list_no_delaunay miscellaneous.f90:910-1015: each tetrahedron gives
+    // its vertices the other three; SortUnique then sorts and de-duplicates.
+    // Built as a CSR: incidence counts, offsets, the raw lists (filled in
+    // tetrahedron order per thread range, so the per-node lists are the same
+    // multiset whatever the thread count), then a per-node sort + unique.
+    std::vector<long long> roff((size_t)N + 1, 0);
+    for (size_t q = 0; q < nc; q++)
+        for (int k = 0; k < 4; k++) roff[(size_t)cells[5 * q + 1 + k] + 1] += 3;
+    for (int i = 0; i < N; i++) roff[i + 1] += roff[i];
+    for (int i = 0; i < N; i++)
+        if (roff[i + 1] - roff[i] > max_ne_temp) {  // miscellaneous.f90:1000-1004
+            err = "count_ne=" + std::to_string(roff[i + 1] - roff[i]) + " while max_ne_temp=" +
                   std::to_string(max_ne_temp) + "; adjust max_ne_temp parameter! Make it bigger.";
             return false;
         }
-        std::sort(nb[i].begin(), nb[i].end());
-        nb[i].erase(std::unique(nb[i].begin(), nb[i].end()), nb[i].end());
-        c.del_num_ne[i] = (int)nb[i].size();
-        maxne = std::max(maxne, c.del_num_ne[i]);
+    std::vector<int> raw((size_t)roff[N]);
+    {
+        std::vector<long long> fill(roff.begin(), roff.end() - 1);
+        for (size_t q = 0; q < nc; q++)
+            for (int k = 0; k < 4; k++) {
+                const int a = cells[5 * q + 1 + k];
+                for (int k2 = 0; k2 < 4; k2++)
+                    if (k2 != k) raw[(size_t)fill[a]++] = cells[5 * q + 1 + k2] + 1;
+            }
     }
+    c.del_num_ne.assign(N, 0);
+    {
+        std::vector<std::thread> th;
+        auto work = [&](int t) {
+            const int i0 = (int)((long long)N * t / nth), i1 = (int)((long long)N * (t + 1) / nth);
+            for (int i = i0; i < i1; i++) {
+                int *b = raw.data() + roff[i], *e = raw.data() + roff[i + 1];
+                std::sort(b, e);
+                c.del_num_ne[i] = (int)(std::unique(b, e) - b);
+            }
+        };
+        for (int t = 1; t < nth; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+    }
+    int maxne = 0;
+    for (int i = 0; i < N; i++) maxne = std::max(maxne, c.del_num_ne[i]);
     c.maxne = maxne;
     c.del_ne.assign((size_t)N * maxne, 0);  // main_para.f90:124-128
     for (int i = 0; i < N; i++)
-        for (size_t s = 0; s < nb[i].size(); s++) c.del_ne[(size_t)i + (size_t)N * s] = nb[i][s];
+        for (int s2 = 0; s2 < c.del_num_ne[i]; s2++) c.del_ne[(size_t)i + (size_t)N * s2] = raw[(size_t)roff[i] + s2];
 
     // ---- LAMDA (eat_lime_dim :38-62, eat_lime_no_delaunay :151-196) ----
     ListReader f(mol);
@@ -307,18 +436,19 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     c.ab_all.assign(N, 1e-3);
     c.lev_p.assign((size_t)nl * N, 0.0);
     std::vector<double> g2d(N, 0.0);
-    int bulk = 0;
-    while (bulk < N && p.read_doubles(vd, 13 + (size_t)nl)) {
-        const int i = bulk;
-        for (int k = 0; k < 3; k++) c.vel[3 * (size_t)i + k] = vd[3 + k];
-        c.h2_dens[i] = vd[6];
-        c.temp_all[2 * (size_t)i] = vd[7];
-        c.temp_all[2 * (size_t)i + 1] = vd[8];
-        c.b_all[i] = vd[9];
-        c.ab_all[i] = vd[10];
-        g2d[i] = vd[11];
-        for (int l = 0; l < nl; l++) c.lev_p[(size_t)nl * i + l] = vd[13 + l];
-        bulk++;
+    const size_t nv = 13 + (size_t)nl;
+    std::vector<double> rows((size_t)N * nv);
+    const int bulk = (int)p.read_block_doubles(rows.data(), (size_t)N, nv, nth);
+    for (int i = 0; i < bulk; i++) {
+        const double *r = rows.data() + (size_t)i * nv;
+        for (int k = 0; k < 3; k++) c.vel[3 * (size_t)i + k] = r[3 + k];
+        c.h2_dens[i] = r[6];
+        c.temp_all[2 * (size_t)i] = r[7];
+        c.temp_all[2 * (size_t)i + 1] = r[8];
+        c.b_all[i] = r[9];
+        c.ab_all[i] = r[10];
+        g2d[i] = r[11];
+        for (int l = 0; l < nl; l++) c.lev_p[(size_t)nl * i + l] = r[13 + l];
     }
     c.bulk_node_num = bulk;
     // surface nodes (eat_lime.f90:227-245)
@@ -432,11 +562,11 @@ bool read_rows(const std::string &path, std::vector<double> &cm, int rows, int c
     ListReader r(path);
     if (!r.ok()) { err = "cannot open " + path; return false; }
     cm.assign((size_t)rows * cols, 0.0);
-    std::vector<double> v;
-    for (int i = 0; i < rows; i++) {  // para_finish.f90:226-227
-        if (!r.read_doubles(v, cols)) { err = path + ": row " + std::to_string(i + 1); return false; }
-        for (int k = 0; k < cols; k++) cm[(size_t)i + (size_t)rows * k] = v[k];
-    }
+    std::vector<double> v((size_t)rows * cols);
+    const size_t got = r.read_block_doubles(v.data(), (size_t)rows, (size_t)cols, io_threads());
+    if (got < (size_t)rows) { err = path + ": row " + std::to_string(got + 1); return false; }
+    for (int i = 0; i < rows; i++)  // para_finish.f90:226-227
+        for (int k = 0; k < cols; k++) cm[(size_t)i + (size_t)rows * k] = v[(size_t)i * cols + k];
     return true;
 }
 

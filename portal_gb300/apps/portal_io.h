@@ -24,16 +24,30 @@ public:
     bool read_doubles(std::vector<double> &out, size_t n);
     bool read_ints(std::vector<int> &out, size_t n);
     const std::string &path() const { return path_; }
+    // Up to n_rec consecutive reads of n values each into out (n_rec * n):
+    // the same values as n_rec calls of read_doubles / read_ints.  When every
+    // record is one line of exactly n plain numbers (the form LIME and the
+    // reference's writers produce), the lines are parsed by `threads` threads
+    // at once; otherwise the records are read one by one.  Returns the number
+    // of records read (fewer than n_rec only at the end of the file).
+    size_t read_block_doubles(double *out, size_t n_rec, size_t n, int threads);
+    size_t read_block_ints(int *out, size_t n_rec, size_t n, int threads);
 
 private:
     bool next_record();
+    template <typename T>
+    size_t read_block(T *out, size_t n_rec, size_t n, int threads);
     std::string path_;
-    std::vector<std::string> lines_;
+    std::string buf_;                   // the whole file
+    std::vector<size_t> lbeg_, lend_;   // line extents in buf_ (no line end characters)
     size_t line_ = 0;
     std::vector<std::string> toks_;
     size_t pos_ = 0;
     bool ok_ = false;
 };
+
+// threads for the bulk readers: PORTAL_THREADS, else the hardware's
+int io_threads();
 
 double to_double(const std::string &tok);
 int to_int(const std::string &tok);

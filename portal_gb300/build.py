@@ -78,7 +78,7 @@ def build_apps() -> list:
             # no FMA contraction: the ingestion must round exactly as the
             # reference's expressions (and the Python restatement) do on
             # every architecture
-            cmd = [os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-std=c++17",
+            cmd = [os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-std=c++17", "-pthread",
                    "-I", os.path.join(ROOT, "include"),
                    "-I", APPS, src, io_src, "-o", exe, "-L", OUT, "-lportal_gb300", "-Wl,-rpath,$ORIGIN"]
             r = subprocess.run(cmd, capture_output=True, text=True)

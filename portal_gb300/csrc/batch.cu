@@ -26,7 +26,7 @@ struct portal_batch {
     std::string err;
 
     bool prepared = false;
-    int nch = 0, n_depth = 0, kmax = 0;
+    int nch = 0, n_depth = 0, kmax = 0, max_lines = 0;
     bool dust = false;
     std::vector<RFArgs> rf;
     std::vector<SEArgs> se;
@@ -76,7 +76,7 @@ int enqueue_pass(portal_batch *b, const int2 *items, long long n_items) {
             return bfail(b, rc, "model " + std::to_string(m) + ": " + b->models[m]->err);
     BCHECK(b, cudaMemsetAsync(b->queue.p, 0, 2 * sizeof(unsigned long long), b->stream));
     RFBatch rb{b->d_rf.p, items, n_items, b->queue.p, b->walk.p, b->n_depth};
-    if ((rc = rf_batch_launch(b->stream, b->rf_bps * b->sm_count, b->nch, b->dust, b->nlg, rb)))
+    if ((rc = rf_batch_launch(b->stream, b->rf_bps * b->sm_count, b->nch, b->dust, b->nlg, b->max_lines, rb)))
         return bfail(b, rc, "radiation-field launch failed");
     for (size_t m = 0; m < b->models.size(); m++)
         if ((rc = se_pass(b->models[m], b->stream)))
@@ -160,6 +160,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
     b->rf.assign(M, RFArgs{});
     b->se.assign(M, SEArgs{});
     b->dust = false;
+    b->max_lines = 0;
     size_t wb = 0;
     std::vector<double> cost(M);
     for (int m = 0; m < M; m++) {
@@ -172,6 +173,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
             return bfail(b, rc, "model " + std::to_string(m) + ": " + c->err);
         wb = std::max(wb, w);
         b->dust = b->dust || c->has_dust;
+        b->max_lines = std::max(b->max_lines, c->r_num);
         // per-node cost ~ lines x cells per ray ~ L N^(1/3)
         cost[m] = (double)c->r_num * std::cbrt((double)c->N);
     }
@@ -203,7 +205,8 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
     std::vector<RFC> rfc;
     for (int nlg : {5, 10}) {
         int mx = 0;
-        if (rf_batch_blocks_per_sm(b->nch, b->dust, nlg, &mx)) return bfail(b, PORTAL_ERR_CUDA, "occupancy query");
+        if (rf_batch_blocks_per_sm(b->nch, b->dust, nlg, b->max_lines, &mx))
+            return bfail(b, PORTAL_ERR_CUDA, "occupancy query");
         for (int bps = 1; bps <= std::min(mx, 2); bps++) rfc.push_back({nlg, bps});
     }
     if (rfc.empty()) return bfail(b, PORTAL_ERR_CUDA, "radiation-field kernel does not fit on an SM");
@@ -229,7 +232,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
             RFBatch rb{b->d_rf.p, b->sample.p, b->n_sample, b->queue.p, b->walk.p, n_depth};
             double ms = 0.0;
             int rc = time_launch(b, [&]() { return rf_batch_launch(b->stream, c.bps * b->sm_count, b->nch, b->dust,
-                                                                  c.nlg, rb); }, &ms);
+                                                                  c.nlg, b->max_lines, rb); }, &ms);
             if (rc) return rc;
             b->tune.insert(b->tune.end(), {(double)c.nlg, (double)c.bps, ms});
             if (ms < best) { best = ms; b->nlg = c.nlg; b->rf_bps = c.bps; }

@@ -86,8 +86,8 @@ struct SEBatch {
 int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, double dx, int n_depth,
                bool split, RFArgs *a);
 int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s);
-int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int *blocks);
-int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, const RFBatch &bw);
+int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int max_lines, int *blocks);
+int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, int max_lines, const RFBatch &bw);
 // se.cu
 int se_prepare(portal_ctx *c, int kmax, SEArgs *a, size_t *warp_bytes);
 int se_pass(portal_ctx *c, cudaStream_t s);

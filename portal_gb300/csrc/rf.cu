@@ -116,6 +116,8 @@ __global__ void k_line_table(int N, int L, double dxp, const LineConst *__restri
 template <int NLG, bool DUST>
 struct CellRec {
     float q0[32], dq[32];
+    int cell[32];        // cell id and trace steps (the remainder channel's pass)
+    float fst[32];
     float As[32][NLG];   // A * steps
     float Ss[32][NLG];   // S (no dust) or E * steps (dust)
     float Ad[32][DUST ? NLG : 1];   // dust tau per cell (dust only)
@@ -130,11 +132,16 @@ struct RayBatch {
     int K[32];           // segments per ray (-1: n_depth overflow)
 };
 
-// NS channel slots per lane (nch <= 32 NS), NLG lines per register group.
+// NS channel slots per lane, NLG lines per register group.
+// RT = 0: nch <= 32 NS, every channel in a slot.  RT = 1: nch = 32 NS + 1
+// (the reference's 2 nvel + 1 channels with nvel a multiple of 16): the
+// last channel (nv = +nvel) is integrated lanes-over-lines (lane = line,
+// L <= 32) in the first line-group pass instead of costing a whole slot of
+// 32 lanes for one channel.
 // BATCH: the work items are (model, node) pairs of many models (RFBatch);
 // each warp copies the argument block of its current model into shared
 // memory.  Otherwise the nodes of the one model a0.
-template <int NS, int NLG, bool DUST, bool BATCH>
+template <int NS, int NLG, bool DUST, bool BATCH, int RT>
 __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiation_field(RFArgs a0, RFBatch bw) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -270,6 +277,10 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                     const float wgt = (float)dr[4], wgt2 = (float)dr[5];
                     nseg += (unsigned long long)Kr;
                     const int2 w0 = wl[0];
+                    // the remainder channel of this lane's line (RT): intensity, and
+                    // its central-cell contributions to J0 (and J_eff, L*)
+                    float Irem = 0.f, remJ = 0.f, remE = 0.f, remL = 0.f;
+                    if (RT && lane < a.L) Irem = a.bb[lane];
                     for (int l0 = 0; l0 < a.L; l0 += NLG) {
                         // intensities of the lane's channels: slot pairs (s, s+1) in one
                         // float2 (packed FP32x2 arithmetic), an odd last slot in .x
@@ -292,6 +303,10 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 R.q0[lane] = (d4.w - vp) * ib;
                                 R.dq[lane] = dqfac * ib;
                                 const float fst = (float)wc.y;
+                                if (RT) {
+                                    R.cell[lane] = wc.x;
+                                    R.fst[lane] = fst;
+                                }
                                 const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
 #pragma unroll
                                 for (int l = 0; l < NLG; l++) {
@@ -324,6 +339,19 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 }
                             }
                             __syncwarp();
+                            if (RT && l0 == 0 && lane < a.L) {
+                                // the remainder channel, lane = line, the same cells inward
+                                const float chr = (float)(32 * NS - a.nvel);
+                                for (int u = 0; u < nc; u++) {
+                                    const float4 v = a.ltab[(size_t)R.cell[u] * a.L + lane];
+                                    const float q = fmaf(R.dq[u], chr, R.q0[u]);
+                                    const float gr = ex2(-q * q * LOG2E_F);
+                                    const float As = (v.x > 0.f) ? v.x * R.fst[u] * LOG2E_F : 0.f;
+                                    const float Ss = (v.x > 0.f) ? v.y : 0.f;
+                                    const float x = As * gr;
+                                    Irem = fmaf(one_minus_exp(x, ex2(-x)), Ss - Irem, Irem);
+                                }
+                            }
                             for (int u = 0; u < nc; u++) {
                                 const float q0 = R.q0[u], dq = R.dq[u];
                                 float g[NS];
@@ -382,6 +410,19 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                         // central cell (inverse_rt.f90:320-339): no gate, profile at
                         // the node's own b, then the weighted channel sum
                         const float fst0 = (float)w0.y;
+                        if (RT && l0 == 0 && lane < a.L) {
+                            const int ch = 32 * NS;
+                            const float4 v = a.ltab[(size_t)node * a.L + lane];
+                            const float q0c = a.chq[ch];
+                            const float g0 = ex2(-q0c * q0c * LOG2E_F);
+                            const float x = v.x * g0 * fst0 * LOG2E_F;
+                            const float om = one_minus_exp(x, ex2(-x));
+                            remJ = a.chw[ch] * fmaf(om, v.y - Irem, Irem);
+                            if (split) {
+                                remE = a.chw[ch] * fmaf(om, -Irem, Irem);
+                                remL = a.chw[ch] * om;
+                            }
+                        }
                         float part[NLG], pe[NLG], pl[NLG];
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
@@ -428,6 +469,7 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                             const int line = l0 + l;
                             if (line < a.L && (line & 31) == lane) {
                                 if (line < 32) {
+                                    if (RT) v += remJ;   // this lane's line: its remainder channel
                                     acc0a.add(wgt * v);
                                     acc2a.add(wgt2 * v);
                                 } else {
@@ -448,6 +490,10 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 const int line = l0 + l;
                                 if (line < a.L && (line & 31) == lane) {
                                     if (line < 32) {
+                                        if (RT) {
+                                            ve += remE;
+                                            vl += remL;
+                                        }
                                         accEa.add(wgt * ve);
                                         accLa.add(wgt * vl);
                                     } else {
@@ -522,9 +568,9 @@ int upload_lines(portal_ctx *c) {
     return PORTAL_OK;
 }
 
-template <int NS, int NLG, bool DUST>
+template <int NS, int NLG, bool DUST, int RT>
 int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
-    auto kern = k_radiation_field<NS, NLG, DUST, false>;
+    auto kern = k_radiation_field<NS, NLG, DUST, false, RT>;
     int nb = 0;
     PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, 0));
     if (nb < 1) nb = 1;
@@ -552,28 +598,78 @@ inline int line_group(int L) {
     return 5;
 }
 
-template <int NS>
-int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
-    if (line_group(a.L) == 5)
-        return c->has_dust ? launch_rf<NS, 5, true>(c, a, n_depth) : launch_rf<NS, 5, false>(c, a, n_depth);
-    return c->has_dust ? launch_rf<NS, 10, true>(c, a, n_depth) : launch_rf<NS, 10, false>(c, a, n_depth);
+// Channel layout: (slots per lane, remainder channel).  2 nvel + 1 channels
+// with nvel a multiple of 16 take 2 nvel / 32 full slots plus the
+// lanes-over-lines remainder channel (no dust, at most 32 lines); any other
+// count is padded to whole slots.
+struct ChanLayout {
+    int ns, rt;
+};
+inline ChanLayout chan_layout(int nch, bool dust, int max_lines) {
+    if (!dust && max_lines <= 32 && nch > 32 && nch % 32 == 1) {
+        const int k = nch / 32;
+        if (k == 1 || k == 2 || k == 4 || k == 8) return {k, 1};
+    }
+    if (nch <= 32) return {1, 0};
+    if (nch <= 64) return {2, 0};
+    if (nch <= 96) return {3, 0};
+    if (nch <= 160) return {5, 0};
+    return {9, 0};
 }
 
-// the batched kernel for a channel count and line group
-template <int NS>
-const void *batch_kernel_ns(bool dust, int nlg) {
-    if (nlg == 10)
-        return dust ? (const void *)k_radiation_field<NS, 10, true, true>
-                    : (const void *)k_radiation_field<NS, 10, false, true>;
-    return dust ? (const void *)k_radiation_field<NS, 5, true, true>
-                : (const void *)k_radiation_field<NS, 5, false, true>;
+template <int NS, int RT>
+int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
+    if (RT || line_group(a.L) == 5)
+        return c->has_dust ? launch_rf<NS, 5, true, 0>(c, a, n_depth) : launch_rf<NS, 5, false, RT>(c, a, n_depth);
+    return c->has_dust ? launch_rf<NS, 10, true, 0>(c, a, n_depth) : launch_rf<NS, 10, false, 0>(c, a, n_depth);
 }
-const void *batch_kernel(int nch, bool dust, int nlg) {
-    if (nch <= 32) return batch_kernel_ns<1>(dust, nlg);
-    if (nch <= 64) return batch_kernel_ns<2>(dust, nlg);
-    if (nch <= 96) return batch_kernel_ns<3>(dust, nlg);
-    if (nch <= 160) return batch_kernel_ns<5>(dust, nlg);
-    return batch_kernel_ns<9>(dust, nlg);
+
+int dispatch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
+    const ChanLayout cl = chan_layout(a.nch, c->has_dust, a.L);
+    if (cl.rt) {
+        switch (cl.ns) {
+        case 1: return dispatch_nlg<1, 1>(c, a, n_depth);
+        case 2: return dispatch_nlg<2, 1>(c, a, n_depth);
+        case 4: return dispatch_nlg<4, 1>(c, a, n_depth);
+        default: return dispatch_nlg<8, 1>(c, a, n_depth);
+        }
+    }
+    switch (cl.ns) {
+    case 1: return dispatch_nlg<1, 0>(c, a, n_depth);
+    case 2: return dispatch_nlg<2, 0>(c, a, n_depth);
+    case 3: return dispatch_nlg<3, 0>(c, a, n_depth);
+    case 5: return dispatch_nlg<5, 0>(c, a, n_depth);
+    default: return dispatch_nlg<9, 0>(c, a, n_depth);
+    }
+}
+
+// the batched kernel for a channel layout and line group
+template <int NS, int RT>
+const void *batch_kernel_ns(bool dust, int nlg) {
+    if (RT) return (const void *)k_radiation_field<NS, 5, false, true, RT>;
+    if (nlg == 10)
+        return dust ? (const void *)k_radiation_field<NS, 10, true, true, 0>
+                    : (const void *)k_radiation_field<NS, 10, false, true, 0>;
+    return dust ? (const void *)k_radiation_field<NS, 5, true, true, 0>
+                : (const void *)k_radiation_field<NS, 5, false, true, 0>;
+}
+const void *batch_kernel(int nch, bool dust, int nlg, int max_lines) {
+    const ChanLayout cl = chan_layout(nch, dust, max_lines);
+    if (cl.rt) {
+        switch (cl.ns) {
+        case 1: return batch_kernel_ns<1, 1>(dust, nlg);
+        case 2: return batch_kernel_ns<2, 1>(dust, nlg);
+        case 4: return batch_kernel_ns<4, 1>(dust, nlg);
+        default: return batch_kernel_ns<8, 1>(dust, nlg);
+        }
+    }
+    switch (cl.ns) {
+    case 1: return batch_kernel_ns<1, 0>(dust, nlg);
+    case 2: return batch_kernel_ns<2, 0>(dust, nlg);
+    case 3: return batch_kernel_ns<3, 0>(dust, nlg);
+    case 5: return batch_kernel_ns<5, 0>(dust, nlg);
+    default: return batch_kernel_ns<9, 0>(dust, nlg);
+    }
 }
 
 }  // namespace
@@ -667,15 +763,15 @@ int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s) {
     return PORTAL_OK;
 }
 
-int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int *blocks) {
-    const void *k = batch_kernel(nch, dust, nlg);
+int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int max_lines, int *blocks) {
+    const void *k = batch_kernel(nch, dust, nlg, max_lines);
     *blocks = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 256, 0);
     return e == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
 }
 
-int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, const RFBatch &bw) {
-    const void *k = batch_kernel(nch, dust, nlg);
+int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, int max_lines, const RFBatch &bw) {
+    const void *k = batch_kernel(nch, dust, nlg, max_lines);
     RFArgs a0{};
     RFBatch b = bw;
     void *args[] = {&a0, &b};
@@ -694,13 +790,7 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     timer_start(c, T_LINETAB);
     if ((rc = rf_pass(c, a, c->stream))) return rc;
     timer_stop(c, T_LINETAB);
-    const int nch = a.nch;
-    if (nch <= 32) rc = dispatch_nlg<1>(c, a, n_depth);
-    else if (nch <= 64) rc = dispatch_nlg<2>(c, a, n_depth);
-    else if (nch <= 96) rc = dispatch_nlg<3>(c, a, n_depth);
-    else if (nch <= 160) rc = dispatch_nlg<5>(c, a, n_depth);
-    else rc = dispatch_nlg<9>(c, a, n_depth);
-    if (rc) return rc;
+    if ((rc = dispatch_rf(c, a, n_depth))) return rc;
     unsigned long long cnt[8];
     PCHECK(c, cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
