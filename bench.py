@@ -247,6 +247,11 @@ def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
     return out
 
 
+def ctx_cdim(mol, kmax):
+    """Order of the SE system: components K = 0, 2, .. min(2J, kmax) per level."""
+    return int(sum(min(2 * int(j), kmax) // 2 + 1 for j in mol.j_lev))
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import portal_gb300 as pg
@@ -304,7 +309,7 @@ def gpu_arm(args, rank, world, local_rank):
     if dist:
         dist.barrier()
     clocks.start()
-    times, rf_ms, launches, nseg_tot = [], [], 0, 0
+    times, rf_ms, se_ms, launches, nseg_tot = [], [], [], 0, 0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -317,6 +322,7 @@ def gpu_arm(args, rank, world, local_rank):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
         rf_ms.append(kt_rf["radiation_field"][0])
+        se_ms.append(kt_se["solve_se"][0])
         launches += kt_rf["line_table"][1] + kt_rf["radiation_field"][1] + kt_se["solve_se"][1]
         nseg_tot += nseg
     torch.cuda.synchronize()
@@ -351,6 +357,21 @@ def gpu_arm(args, rank, world, local_rank):
         t_e2e = float(ev.item())
     e2e_val = nseg_step * world / t_e2e
 
+    # ---- the other two stages' throughput: SE node solves, Stokes image ----
+    se_launch_ms = statistics.median(se_ms)
+    stages = {"se": {"node_solves_per_s": cloud.bulk_node_num / (se_launch_ms * 1e-3), "launch_ms": se_launch_ms,
+                     "system": "%d x %d (kmax %d)" % (ctx_cdim(mol, rc.kmax), ctx_cdim(mol, rc.kmax), rc.kmax)}}
+    if not args.no_image:
+        im_pix, im_nvel = 256, 64
+        ctx.image([1], [2], 0.78539816339, 0.0, im_nvel, 50.0, 0.0, im_pix, 0.7, quantities=4)   # warm-up
+        ctx.image([1], [2], 0.78539816339, 0.0, im_nvel, 50.0, 0.0, im_pix, 0.7, quantities=4)
+        kt = ctx.kernel_times()
+        im_ms = kt["emcoefs"][0] + kt["image_walk"][0] + kt["image_rt"][0]
+        npx = 2 * im_pix + 1
+        stages["image"] = {"pixel_channels_per_s": npx * npx * (2 * im_nvel + 1) / (im_ms * 1e-3),
+                           "kernel_ms": im_ms, "cube": "%dx%d pixels x %d channels, line 1-0, inclination 45 deg"
+                                                       % (npx, npx, 2 * im_nvel + 1)}
+
     # ---- roofline of the dominant kernel (radiation field) ----
     deg = float(np.diff(cloud.nb_off).mean())
     b_seg = 4 + deg * (4 + 12) + 12 + 4 + 4 + 4 + 4 * nlev
@@ -369,7 +390,7 @@ def gpu_arm(args, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 ray integration, f32 LU + f64 refinement",
             "data": "synthetic", "config": workload_config(cloud, mol, rc, N),
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "clocks": clk}
+            "gpu_launches": launches, "roofline": roof, "clocks": clk, "stages": stages}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rates, cores = cpu_port_rate(cloud, mol, rc, args.cpu_seconds, repeats=1)
         line["cpu_baseline"] = {"value": rates[0][0], "unit": UNIT, "cores": cores, "kind": "port",
@@ -396,6 +417,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-image", action="store_true", help="skip the Stokes-image throughput leg")
     ap.add_argument("--no-convergence", action="store_true",
                     help="skip the time-to-converged comparison (plain / accelerated / warm-started)")
     ap.add_argument("--n-depth", type=int, default=10000,

@@ -183,16 +183,33 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
             // the oracle's FP64 arithmetic, without FMA contraction, throughout the march
             const double z0 = -1.0 * __dsqrt_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(x, x)), __dmul_rn(y, y)));
             int2 *dl = wbase + (size_t)lane * a.n_depth;
-            // nearest node (raytrace.f90:126-134; strict <, so the lowest index wins)
-            int c = -1;
-            double best = 10.0;  // rsave = 10 (raytrace.f90:126)
-            for (int i = 0; i < a.N; i++) {
-                const double dx0 = x - a.xyz[3 * (size_t)i], dy0 = y - a.xyz[3 * (size_t)i + 1],
-                             dz0 = z0 - a.xyz[3 * (size_t)i + 2];
-                const double r = __dsqrt_rn(dsum3sq(dx0, dy0, dz0));  // norm2(start - X)
-                if (r < best) { best = r; c = i; }
+            // nearest node to the start point (raytrace.f90:126-134 scans all
+            // nodes; strict <, so the lowest index wins).  The same argmin by
+            // greedy descent on the Delaunay graph: a node that is not the
+            // nearest has a neighbour at most as far (the segment to the point
+            // leaves its Voronoi cell through a face shared with that
+            // neighbour), so descending in (distance, index) order from node 0
+            // ends at the nearest node with the lowest index; distances are
+            // computed exactly as the reference's norm2.
+            auto dist = [&](int i) {
+                return __dsqrt_rn(dsum3sq(x - a.xyz[3 * (size_t)i], y - a.xyz[3 * (size_t)i + 1],
+                                          z0 - a.xyz[3 * (size_t)i + 2]));
+            };
+            int c = 0;
+            double best = dist(0);
+            for (int hop = 0; hop < a.N; hop++) {
+                int nbest = c;
+                double dbest = best;
+                for (int q = a.off[c]; q < a.off[c + 1]; q++) {
+                    const int nb = a.idx[q];
+                    const double d = dist(nb);
+                    if (d < dbest || (d == dbest && nb < nbest)) { dbest = d; nbest = nb; }
+                }
+                if (nbest == c) break;
+                c = nbest;
+                best = dbest;
             }
-            if (c < 0) st = 3;  // start point outside the unit sphere (NaN)
+            if (!(best < 10.0)) { c = -1; st = 3; }  // start point outside the unit sphere (NaN; rsave = 10)
             double z = z0;
             int k = 0;
             const double zexit = -z0;

@@ -354,11 +354,22 @@ __global__ void __launch_bounds__(256, (NLG == 5 && NS <= 5) ? 2 : 1) k_radiatio
                             }
                             for (int u = 0; u < nc; u++) {
                                 const float q0 = R.q0[u], dq = R.dq[u];
+                                // Gaussian profile of the cell at the lane's channels,
+                                // slot pairs on the packed pipe (the same roundings as
+                                // ex2(-q q log2 e) per slot)
                                 float g[NS];
 #pragma unroll
-                                for (int s2 = 0; s2 < NS; s2++) {
-                                    const float q = fmaf(dq, (float)(lane + 32 * s2 - a.nvel), q0);
-                                    g[s2] = ex2(-q * q * LOG2E_F);
+                                for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
+                                    const float2 ch2 = make_float2((float)(lane + 32 * s2 - a.nvel),
+                                                                   (float)(lane + 32 * (s2 + 1) - a.nvel));
+                                    const float2 q = __ffma2_rn(make_float2(dq, dq), ch2, make_float2(q0, q0));
+                                    const float2 t = __fmul2_rn(__fmul2_rn(q, q), make_float2(-LOG2E_F, -LOG2E_F));
+                                    g[s2] = ex2(t.x);
+                                    g[s2 + 1] = ex2(t.y);
+                                }
+                                if (NS & 1) {
+                                    const float q = fmaf(dq, (float)(lane + 32 * (NS - 1) - a.nvel), q0);
+                                    g[NS - 1] = ex2(-q * q * LOG2E_F);
                                 }
 #pragma unroll
                                 for (int l = 0; l < NLG; l++) {
