@@ -247,6 +247,20 @@ def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
     return out
 
 
+def reduce_replicas(t, units, dist=None):
+    """Whole-job figures of N independent replicas: the slowest rank's time
+    (max over ranks) and the units all ranks processed (sum).  dist is
+    torch.distributed (gloo here) or None for one rank."""
+    if dist is None:
+        return float(t), float(units)
+    import torch
+    tt = torch.tensor([float(t)], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    uu = torch.tensor([float(units)], dtype=torch.float64)
+    dist.all_reduce(uu, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(uu.item())
+
+
 def ctx_cdim(mol, kmax):
     """Order of the SE system: components K = 0, 2, .. min(2J, kmax) per level."""
     return int(sum(min(2 * int(j), kmax) // 2 + 1 for j in mol.j_lev))
@@ -328,15 +342,7 @@ def gpu_arm(args, rank, world, local_rank):
     torch.cuda.synchronize()
     clk = clocks.stop()
     t_total_ms = sum(times)
-    if dist:
-        tt = torch.tensor([t_total_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total_ms = float(tt.item())
-        ns = torch.tensor([nseg_tot], dtype=torch.float64)
-        dist.all_reduce(ns, op=dist.ReduceOp.SUM)
-        nseg_all = float(ns.item())
-    else:
-        nseg_all = float(nseg_tot)
+    t_total_ms, nseg_all = reduce_replicas(t_total_ms, nseg_tot, dist)
     value = nseg_all / (t_total_ms * 1e-3)
     nseg_step = nseg_tot / args.steps
 
@@ -351,10 +357,7 @@ def gpu_arm(args, rank, world, local_rank):
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
     t_e2e = statistics.median(e2e_times)
-    if dist:
-        ev = torch.tensor([t_e2e], dtype=torch.float64)
-        dist.all_reduce(ev, op=dist.ReduceOp.MAX)
-        t_e2e = float(ev.item())
+    t_e2e, _ = reduce_replicas(t_e2e, 0, dist)
     e2e_val = nseg_step * world / t_e2e
 
     # ---- the other two stages' throughput: SE node solves, Stokes image ----
