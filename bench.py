@@ -70,7 +70,7 @@ def peaks():
 def traffic_per_segment():
     """DRAM bytes per ray segment of the radiation-field kernel, from the ncu
     summary committed under profiles/ (None when absent)."""
-    p = os.path.join(ROOT, "profiles", "radiation_field_cfg2.md")
+    p = os.path.join(ROOT, "profiles", "radiation_field_sphere262k.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -159,7 +159,7 @@ def cpu_port_rate(cloud, mol, rc, target_s, repeats=1):
 
 def build_workload(n_points, n_depth=10000):
     from portal_gb300 import synth
-    cloud, mol, rc = synth.config_cloud("cfg2", n_points=n_points)
+    cloud, mol, rc = synth.config_cloud("sphere262k", n_points=n_points)
     rc.n_depth = n_depth
     return cloud, mol, rc
 

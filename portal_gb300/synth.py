@@ -440,23 +440,25 @@ def gauge_vector(seed: int) -> tuple:
 def config_cloud(name: str, n_points: int | None = None):
     """(cloud, molecule, run config) for a named configuration.
 
-    "cfg1": 4,096 points, seed 0, 5-level rotor, T = 20 K, B along z,
+    "sphere4k": 4,096 points, seed 0, 5-level rotor, T = 20 K, B along z,
             16x16 directions, 65 channels (nvel = 32);
-    "cfg2": 262,144 points, seed 1, 10-level rotor, T 10-40 K linear in
+    "sphere262k": 262,144 points, seed 1, 10-level rotor, T 10-40 K linear in
             log r, B along z + 30% Gaussian component, 24x24 directions,
-            129 channels (nvel = 64).
+            129 channels (nvel = 64);
+    "cube1m": 1,048,576 points of the turbulent cube (seed 4), 20-level
+            rotor, 32x32 directions, 129 channels, kmax 2.
     n_points overrides the point count (smaller parity cases)."""
-    if name == "cfg1":
+    if name == "sphere4k":
         mol = linear_rotor(5)
         n = n_points or 4096
         cloud = power_law_sphere(n, 0, mol, t_law="uniform", t_uniform=20.0)
         rc = RunConfig(nth=16, nph=16, nvel=32, kmax=6, gvec=gauge_vector(0))
-    elif name == "cfg2":
+    elif name == "sphere262k":
         mol = linear_rotor(10)
         n = n_points or 262144
         cloud = power_law_sphere(n, 1, mol, t_law="loglinear", b_random=0.3)
         rc = RunConfig(nth=24, nph=24, nvel=64, kmax=6, gvec=gauge_vector(1))
-    elif name == "cfg4":
+    elif name == "cube1m":
         mol = linear_rotor(20)
         n = n_points or 1048576
         cloud = turbulent_cube(n, 4, mol, grid=128 if n > 200000 else 64)

@@ -19,16 +19,16 @@ def built_lib():
 
 
 @pytest.fixture(scope="session")
-def cfg1():
+def sphere4k():
     from portal_gb300 import synth
-    return synth.config_cloud("cfg1")
+    return synth.config_cloud("sphere4k")
 
 
 @pytest.fixture(scope="session")
-def cfg1_oracle(cfg1):
-    """Oracle radiation field + SE of all cfg1 nodes (FP64, OpenMP)."""
+def sphere4k_oracle(sphere4k):
+    """Oracle radiation field + SE of all sphere4k nodes (FP64, OpenMP)."""
     import oracle
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     P = oracle.OracleProblem(cloud, mol)
     J0, J2, st, nseg, nfail = P.radiation_field(rc)
     pp, st2, nf2 = P.solve_se(rc.kmax, J0, J2)

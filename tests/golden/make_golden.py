@@ -116,7 +116,7 @@ def lapack():
     from portal_gb300 import synth
     from scipy.linalg import lapack as la
 
-    cloud, mol, rc = synth.config_cloud("cfg1")
+    cloud, mol, rc = synth.config_cloud("sphere4k")
     P = oracle.OracleProblem(cloud, mol)
     J0, J2, _, _, _ = P.radiation_field(rc, 1, 4)
     out = {"source": "scipy.linalg.lapack dgetrf + dgetri", "cases": []}

@@ -25,10 +25,10 @@ def test_ng_solves_two_mode_linear_iteration():
 
 
 @pytest.mark.gpu
-def test_device_ng_step_matches_restatement(built_lib, cfg1):
+def test_device_ng_step_matches_restatement(built_lib, sphere4k):
     import portal_gb300 as pg
 
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     n_mol = cloud.lev_p.sum(axis=1)
     g = np.sqrt(2 * mol.j_lev + 1.0)
     with pg.Context(0) as ctx:
@@ -49,10 +49,10 @@ def test_device_ng_step_matches_restatement(built_lib, cfg1):
 
 
 @pytest.mark.gpu
-def test_ng_reaches_the_plain_fixed_point_sooner(built_lib, cfg1):
+def test_ng_reaches_the_plain_fixed_point_sooner(built_lib, sphere4k):
     import portal_gb300 as pg
 
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     with pg.Context(0) as ctx:
         ctx.set_molecule(mol)
         ctx.set_cloud(cloud)
@@ -67,12 +67,12 @@ def test_ng_reaches_the_plain_fixed_point_sooner(built_lib, cfg1):
 
 
 @pytest.mark.gpu
-def test_split_field_matches_oracle(built_lib, cfg1):
+def test_split_field_matches_oracle(built_lib, sphere4k):
     """J_eff and L* of the radiation-field kernel against the FP64 oracle."""
     import portal_gb300 as pg
     import oracle
 
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     P = oracle.OracleProblem(cloud, mol)
     oJ0, _, oJE, oLS, _ = P.radiation_field_split(rc)
     with pg.Context(0) as ctx:
@@ -95,10 +95,10 @@ def test_split_field_matches_oracle(built_lib, cfg1):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("ng", [0, 4])
-def test_local_operator_reaches_the_plain_fixed_point(built_lib, cfg1, ng):
+def test_local_operator_reaches_the_plain_fixed_point(built_lib, sphere4k, ng):
     import portal_gb300 as pg
 
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     with pg.Context(0) as ctx:
         ctx.set_molecule(mol)
         ctx.set_cloud(cloud)

@@ -45,22 +45,22 @@ def _check_J(J0, J2, oJ0, oJ2, mask=None):
     assert r2.max() < J2_MAX, r2.max()
 
 
-def test_radiation_field_cfg1(ctx, cfg1, cfg1_oracle):
-    cloud, mol, rc = cfg1
+def test_radiation_field_sphere4k(ctx, sphere4k, sphere4k_oracle):
+    cloud, mol, rc = sphere4k
     J0, J2, st, nseg = _rf(ctx, cloud, mol, rc)
     assert not st.any()
-    assert abs(nseg - cfg1_oracle["nseg"]) <= 1e-4 * cfg1_oracle["nseg"]
-    _check_J(J0, J2, cfg1_oracle["J0"], cfg1_oracle["J2"])
+    assert abs(nseg - sphere4k_oracle["nseg"]) <= 1e-4 * sphere4k_oracle["nseg"]
+    _check_J(J0, J2, sphere4k_oracle["J0"], sphere4k_oracle["J2"])
 
 
-def test_solve_se_same_J_cfg1(ctx, cfg1, cfg1_oracle):
+def test_solve_se_same_J_sphere4k(ctx, sphere4k, sphere4k_oracle):
     import portal_gb300 as pg
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     ctx.set_molecule(mol)
     ctx.set_cloud(cloud)
-    pops, st = ctx.solve_se(rc.kmax, cfg1_oracle["J0"], cfg1_oracle["J2"])
+    pops, st = ctx.solve_se(rc.kmax, sphere4k_oracle["J0"], sphere4k_oracle["J2"])
     assert not (st & pg.NODE_SINGULAR).any()
-    opp = cfg1_oracle["P"].solve_se(rc.kmax, cfg1_oracle["J0"], cfg1_oracle["J2"])[0]
+    opp = sphere4k_oracle["P"].solve_se(rc.kmax, sphere4k_oracle["J0"], sphere4k_oracle["J2"])[0]
     scale = np.abs(opp[:, 0::2]).max(axis=1, keepdims=True)
     assert (np.abs(pops[:, 0::2] - opp[:, 0::2]) / np.abs(opp[:, 0::2])).max() < 1e-10
     assert (np.abs(pops[:, 1::2] - opp[:, 1::2]) / scale).max() < 1e-10
@@ -68,42 +68,42 @@ def test_solve_se_same_J_cfg1(ctx, cfg1, cfg1_oracle):
     np.testing.assert_allclose((pops[:, 0::2] * g).sum(1), 1.0, rtol=1e-12)
 
 
-def test_extra_info_rates_cfg1(ctx, cfg1, cfg1_oracle):
+def test_extra_info_rates_sphere4k(ctx, sphere4k, sphere4k_oracle):
     """The extra_info rates (spontaneous, radiative, collisional per
     component, em_coefs.f90:188-198 packed like the populations) and
     J2/J0 from the same J as the oracle."""
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     ctx.set_molecule(mol)
     ctx.set_cloud(cloud)
     for kmax in (2, rc.kmax):
-        pops, st, jj, rt = ctx.solve_se(kmax, cfg1_oracle["J0"], cfg1_oracle["J2"], jj20=True, rates=True)
-        _, _, _, ort = cfg1_oracle["P"].solve_se(kmax, cfg1_oracle["J0"], cfg1_oracle["J2"], rates=True)
+        pops, st, jj, rt = ctx.solve_se(kmax, sphere4k_oracle["J0"], sphere4k_oracle["J2"], jj20=True, rates=True)
+        _, _, _, ort = sphere4k_oracle["P"].solve_se(kmax, sphere4k_oracle["J0"], sphere4k_oracle["J2"], rates=True)
         bulk = cloud.bulk_node_num
         scale = np.abs(ort[:bulk]).max(axis=2, keepdims=True) + 1e-300
         assert (np.abs(rt[:bulk] - ort[:bulk]) / scale).max() < 1e-10
         assert np.abs(ort[:bulk]).max() > 0
         assert not rt[bulk:].any()
         with np.errstate(invalid="ignore", divide="ignore"):
-            want = cfg1_oracle["J2"] / cfg1_oracle["J0"]
+            want = sphere4k_oracle["J2"] / sphere4k_oracle["J0"]
         live = cloud.ab_all[:bulk] > 0
         np.testing.assert_allclose(jj[:bulk][live], want[:bulk][live], rtol=1e-15)
 
 
-def test_node_loop_chain_cfg1(ctx, cfg1, cfg1_oracle):
+def test_node_loop_chain_sphere4k(ctx, sphere4k, sphere4k_oracle):
     """Device-resident chain radiation field -> SE against oracle -> oracle."""
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     ctx.set_molecule(mol)
     ctx.set_cloud(cloud)
     ctx.radiation_field(rc, fetch=False)
     pops, st = ctx.solve_se(rc.kmax)
-    opp = cfg1_oracle["pops"]
+    opp = sphere4k_oracle["pops"]
     assert (np.abs(pops[:, 0::2] - opp[:, 0::2]) / np.abs(opp[:, 0::2])).max() < 2e-4
     scale = np.abs(opp[:, 0::2]).max(axis=1, keepdims=True)
     assert (np.abs(pops[:, 1::2] - opp[:, 1::2]) / scale).max() < 2e-5
 
 
-def test_deterministic(ctx, cfg1):
-    cloud, mol, rc = cfg1
+def test_deterministic(ctx, sphere4k):
+    cloud, mol, rc = sphere4k
     a = _rf(ctx, cloud, mol, rc)
     b = ctx.radiation_field(rc)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[3] == b[3]
@@ -184,13 +184,13 @@ def test_dust_path(ctx):
     _check_J(J0[:128], J2[:128], oJ0[:128], oJ2[:128])
 
 
-def test_cfg2_shape_subset():
+def test_sphere262k_shape_subset():
     """The 10-level / 24x24 / 129-channel shape on a 16,384-point cloud:
     first 64 nodes against the oracle."""
     import oracle
     import portal_gb300 as pg
     from portal_gb300 import synth
-    cloud, mol, rc = synth.config_cloud("cfg2", n_points=16384)
+    cloud, mol, rc = synth.config_cloud("sphere262k", n_points=16384)
     with pg.Context(0) as c:
         c.set_molecule(mol)
         c.set_cloud(cloud)
@@ -204,7 +204,7 @@ def test_cfg2_shape_subset():
     assert (np.abs(pops[:64, 0::2] - opp[:64, 0::2]) / np.abs(opp[:64, 0::2])).max() < 2e-4
 
 
-def test_cfg4_shape_subset():
+def test_cube1m_shape_subset():
     """The turbulent-cube shape (20-level rotor, 32x32 directions, 129
     channels, kmax 2) on a 32,768-point cube: the full node loop on the
     device, first 24 nodes against the oracle, and the split of the
@@ -212,7 +212,7 @@ def test_cfg4_shape_subset():
     import oracle
     import portal_gb300 as pg
     from portal_gb300 import synth
-    cloud, mol, rc = synth.config_cloud("cfg4", n_points=32768)
+    cloud, mol, rc = synth.config_cloud("cube1m", n_points=32768)
     with pg.Context(0) as c:
         c.set_molecule(mol)
         c.set_cloud(cloud)
@@ -241,7 +241,7 @@ def test_cfg4_shape_subset():
 
 def _image_case(n=4096, im_pix=16, nvel=8):
     from portal_gb300 import synth
-    cloud, mol, rc = synth.config_cloud("cfg1", n_points=n)
+    cloud, mol, rc = synth.config_cloud("sphere4k", n_points=n)
     return cloud, mol, rc, dict(l1=[1], l2=[2], th_inc=0.78539816339, ph_az=0.0, nvel=nvel, dvel=50.0,
                                 v0=0.0, im_pix=im_pix, im_size=0.7)
 

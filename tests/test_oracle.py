@@ -67,10 +67,10 @@ def test_se_solution_against_lapack():
         np.testing.assert_allclose(x, rho, rtol=1e-9, atol=1e-12 * np.abs(rho).max())
 
 
-def test_se_oracle_matches_lapack_pipeline(cfg1):
+def test_se_oracle_matches_lapack_pipeline(sphere4k):
     """orc_solve_se (assembly + LU solve + packing) against the fixture's
     dgetri column for the same J."""
-    cloud, mol, rc = cfg1
+    cloud, mol, rc = sphere4k
     g = _load("lapack.json")
     P = oracle.OracleProblem(cloud, mol)
     N, R = cloud.node_num, mol.r_num

@@ -33,7 +33,7 @@ def test_static_scratch_entry_point_matches_context_path(built_lib):
     L.portal_radiation_field_static_limits(C.byref(max_depth), None, None, None, C.byref(scratch))
     assert scratch.value == 64 << 20 and max_depth.value >= 512
 
-    cloud, mol, rc = synth.config_cloud("cfg1")
+    cloud, mol, rc = synth.config_cloud("sphere4k")
     rc.n_depth = max_depth.value
     with pg.Context(0) as ctx:
         ctx.set_molecule(mol)
