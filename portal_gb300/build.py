@@ -16,8 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libportal_gb300.so")
-SOURCES = ["ctx.cu", "rf.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "mlp.cu", "warmstart.cu",
-           "batch.cu", "wigner.cpp"]
+SOURCES = ["ctx.cu", "rf.cu", "rf_batch.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "mlp.cu",
+           "warmstart.cu", "batch.cu", "wigner.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

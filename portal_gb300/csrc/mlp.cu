@@ -4,8 +4,10 @@
 // Network: n_in -> width (SiLU) -> ... (depth hidden layers) -> n_out
 // (linear).  Parameters are FP32 master copies; every GEMM rounds its
 // operands to BF16 (weights and activations) and accumulates in FP32 on the
-// tensor cores (mma.sync m16n8k16).  Inputs and targets are standardised
-// with statistics stored in the model.
+// tensor cores: the forward GEMMs (inference and training) with tcgen05
+// (k_gemm_tc, accumulator in tensor memory), the backward GEMMs, whose
+// operands are transposed, with mma.sync m16n8k16 (k_gemm).  Inputs and
+// targets are standardised with statistics stored in the model.
 //
 // GEMM kernel: C(M,N) = A(M,K) B(K,N) with 64x64 block tiles, 4 warps of
 // 32x32, K steps of 32 staged in shared memory as BF16 (K-contiguous rows,
@@ -25,6 +27,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "umma.cuh"
 
 using namespace portal;
 
@@ -133,6 +136,131 @@ __global__ void __launch_bounds__(128) k_gemm(int M, int N, int K, const float *
             }
 }
 
+// ---- the forward GEMMs on the 5th-generation tensor cores ------------------
+// C(M, N) = A(M, K) W(N, K)^T with the fused epilogues above, for K, N <= 256.
+// Persistent CTAs of 4 warps (one per SM, the grid at most the SM count):
+// each converts all of W to BF16 in shared memory once, then for each of its
+// 128-row tiles of A converts the rows to BF16 beside it, one thread issues
+// the Kp/16 MMAs of shape 128 x Np x 16 into an FP32 accumulator in tensor
+// memory and commits them to an mbarrier, and each warp reads its 32 rows
+// back with tcgen05.ld for the epilogue.  Shared-memory operands use the
+// canonical no-swizzle K-major layout: 8-row x 16-byte core matrices,
+// K-adjacent ones 128 B apart, row groups Kp/8 x 128 B apart (K and N
+// zero-padded to multiples of 16).  Waits are bounded: a timeout sets *err,
+// the CTA stops and still frees its tensor memory.
+constexpr int TC_M = 128;
+
+__host__ __device__ inline size_t tc_smem_bytes(int Np, int Kp) {
+    return (size_t)TC_M * Kp * 2 + (size_t)Np * Kp * 2 + 16;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// rows [r0, r0 + rows) of the row-major src (ld floats per row, K valid
+// columns, nrow_valid valid rows) into the canonical BF16 tile
+__device__ __forceinline__ void tc_stage(unsigned char *tile, int rows, int Kp, const float *__restrict__ src,
+                                         int r0, int nrow_valid, int K, int ld, int tid) {
+    const int kc = Kp / 8;
+    const uint32_t sbo = (uint32_t)kc * 128;
+    for (int i = tid; i < rows * kc; i += 128) {
+        const int r = i / kc, c = i - r * kc;
+        const int k0 = c * 8;
+        float v[8];
+        const float *p = src + (size_t)(r0 + r) * ld + k0;
+        if (r < nrow_valid && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+            const float4 y = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+            v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+            v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = (r < nrow_valid && k0 + j < K) ? p[j] : 0.f;
+        }
+        uint4 q;
+        q.x = pack_bf16x2(v[0], v[1]);
+        q.y = pack_bf16x2(v[2], v[3]);
+        q.z = pack_bf16x2(v[4], v[5]);
+        q.w = pack_bf16x2(v[6], v[7]);
+        *reinterpret_cast<uint4 *>(tile + (size_t)(r >> 3) * sbo + (size_t)c * 128 + (size_t)(r & 7) * 16) = q;
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, int Np, int Kp, uint32_t tcols,
+                                                    const float *__restrict__ A, const float *__restrict__ W,
+                                                    EpiArgs e, int *err) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    unsigned char *As = tsm;
+    unsigned char *Bs = tsm + (size_t)TC_M * Kp * 2;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + (size_t)Np * Kp * 2);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    tc_stage(Bs, Np, Kp, W, 0, N, K, K, tid);
+    if (warp == 0) umma::tmem_alloc(tslot, tcols);
+    if (tid == 0) {
+        umma::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t taddr = *tslot;
+    const uint32_t idesc = umma::idesc_bf16_f32(TC_M, Np);
+    const uint32_t sbo = (uint32_t)(Kp / 8) * 128;
+    const int ntiles = (M + TC_M - 1) / TC_M;
+    int iter = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, iter++) {
+        const int m0 = t * TC_M;
+        tc_stage(As, TC_M, Kp, A, m0, min(TC_M, M - m0), K, K, tid);
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        __syncthreads();   // A staged; the previous tile's accumulator reads are done
+        umma::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t a0 = umma::smem_addr(As), b0 = umma::smem_addr(Bs);
+            for (int ks = 0; ks < Kp / 16; ks++)
+                umma::mma_bf16(taddr, umma::smem_desc(a0 + ks * 256, 128, sbo),
+                               umma::smem_desc(b0 + ks * 256, 128, sbo), idesc, ks > 0);
+            umma::mma_commit(bar);
+        }
+        bool done = false;
+        for (int it = 0; it < (1 << 24) && !done; it++) done = umma::mbar_try_wait(bar, (uint32_t)(iter & 1));
+        ok = __syncthreads_and(done);
+        umma::fence_after_sync();
+        if (!ok) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < Np; c0 += 32) {
+            float v[32];
+            umma::tmem_ld32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int c = c0 + j;
+                    if (c >= N) break;
+                    const size_t o = (size_t)row * e.ldc + c;
+                    if (e.kind == EPI_BIAS) {
+                        e.C[o] = v[j] + e.bias[c];
+                    } else if (e.kind == EPI_BIAS_SILU) {
+                        const float z = v[j] + e.bias[c];
+                        e.Z[o] = z;
+                        e.C[o] = z * sigm(z);
+                    } else {
+                        e.C[o] = v[j];
+                    }
+                }
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(taddr, tcols);
+}
+
 // column sums of dZ (B x n) -> db (n): deterministic, one thread per column
 __global__ void k_colsum(int B, int n, const float *__restrict__ dZ, float *__restrict__ db) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -208,6 +336,7 @@ struct portal_mlp {
     DevBuf<float> act;   // activations / pre-activations for one batch
     DevBuf<float> xbuf, ybuf, part;
     DevBuf<int> idx;
+    DevBuf<int> tc_err;  // set by a tensor-core GEMM whose completion wait timed out
     int cap_batch = 0;
     long long step = 0;
     std::string err;
@@ -226,10 +355,42 @@ int mlp_fail(portal_mlp *m, int code, const std::string &msg) {
         if (_e != cudaSuccess) return mlp_fail((m), PORTAL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
     } while (0)
 
+// after a stream synchronize: did a tensor-core GEMM give up waiting?
+int tc_status(portal_mlp *m) {
+    int e = 0;
+    if (cudaMemcpy(&e, m->tc_err.p, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return mlp_fail(m, PORTAL_ERR_CUDA, "tensor-core status read");
+    if (e) return mlp_fail(m, PORTAL_ERR_CUDA, "a tensor-core GEMM timed out waiting for its MMAs");
+    return PORTAL_OK;
+}
+
 template <bool AK, bool BK>
 void gemm(cudaStream_t s, int M, int N, int K, const float *A, int lda, const float *B, int ldb, EpiArgs e) {
     dim3 grid((N + 63) / 64, (M + 63) / 64);
     k_gemm<AK, BK><<<grid, 128, 0, s>>>(M, N, K, A, lda, B, ldb, e);
+}
+
+// A(M,K) row-major times W(N,K)^T on the tensor cores (N, K <= 256)
+bool gemm_tc_fits(int N, int K) { return N >= 1 && K >= 1 && N <= 256 && K <= 256; }
+void gemm_tc(cudaStream_t s, int M, int N, int K, const float *A, const float *W, EpiArgs e, int *err) {
+    const int Np = (N + 15) / 16 * 16, Kp = (K + 15) / 16 * 16;
+    uint32_t tcols = 32;
+    while ((int)tcols < Np) tcols <<= 1;
+    const size_t smem = tc_smem_bytes(Np, Kp);
+    static size_t raised = 0;
+    if (smem > raised) {
+        cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(256, 256));
+        raised = tc_smem_bytes(256, 256);
+    }
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm < 1) nsm = 1;
+    }
+    const int ntiles = (M + TC_M - 1) / TC_M;
+    k_gemm_tc<<<std::min(ntiles, nsm), 128, smem, s>>>(M, N, K, Np, Kp, tcols, A, W, e, err);
 }
 
 // activation workspace layout for a batch of B rows:
@@ -282,7 +443,10 @@ void forward(portal_mlp *m, int B, Work &w) {
     for (int l = 0; l < m->n_layers; l++) {
         const bool last = (l == m->n_layers - 1);
         EpiArgs e{last ? EPI_BIAS : EPI_BIAS_SILU, m->fout[l], w.H[l], w.Z[l], m->params.p + m->boff[l]};
-        gemm<true, true>(m->stream, B, m->fout[l], nin, in, nin, m->params.p + m->woff[l], nin, e);
+        if (gemm_tc_fits(m->fout[l], nin))
+            gemm_tc(m->stream, B, m->fout[l], nin, in, m->params.p + m->woff[l], e, m->tc_err.p);
+        else
+            gemm<true, true>(m->stream, B, m->fout[l], nin, in, nin, m->params.p + m->woff[l], nin, e);
         in = w.H[l];
         nin = m->fout[l];
     }
@@ -332,10 +496,11 @@ extern "C" int portal_mlp_create(portal_mlp **out, int device, int n_in, int wid
     m->n_params = off;
     if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
         m->params.reserve(off) || m->grads.reserve(off) || m->adam_m.reserve(off) || m->adam_v.reserve(off) ||
-        m->stats.reserve(2 * (size_t)(n_in + n_out))) {
+        m->stats.reserve(2 * (size_t)(n_in + n_out)) || m->tc_err.reserve(1)) {
         delete m;
         return PORTAL_ERR_NOMEM;
     }
+    cudaMemset(m->tc_err.p, 0, sizeof(int));
     // He-uniform weights, zero biases, identity standardisation
     std::mt19937_64 rng(seed);
     std::vector<float> h(off, 0.f);
@@ -409,6 +574,7 @@ extern "C" int portal_mlp_gradients(portal_mlp *m, const float *X, const float *
     if (grads)
         MCHECK(m, cudaMemcpyAsync(grads, m->grads.p, m->n_params * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
     MCHECK(m, cudaStreamSynchronize(m->stream));
+    if (int rc2 = tc_status(m)) return rc2;
     if (loss) {
         double s = 0.0;
         for (float p : parts) s += p;
@@ -484,7 +650,7 @@ extern "C" int portal_mlp_train(portal_mlp *m, const float *X, const float *Y, i
         if (loss_per_epoch) loss_per_epoch[ep] = (float)(eloss / std::max(nbatch, 1));
     }
     MCHECK(m, cudaStreamSynchronize(m->stream));
-    return PORTAL_OK;
+    return tc_status(m);
 }
 
 // Predict raw-unit outputs for raw inputs X (host or device pointers as
@@ -517,5 +683,5 @@ extern "C" int portal_mlp_predict(portal_mlp *m, const float *X, int B, float *Y
         MCHECK(m, cudaStreamSynchronize(m->stream));
     }
     MCHECK(m, cudaGetLastError());
-    return PORTAL_OK;
+    return tc_status(m);
 }

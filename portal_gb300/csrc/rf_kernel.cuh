@@ -1,0 +1,535 @@
+// The radiation-field kernel (the template shared by the single-model calls
+// in rf.cu and the batched launch in rf_batch.cu) and the line-table kernel.
+// See rf.cu for the algorithm.
+#pragma once
+
+#include <cmath>
+
+#include "internal.cuh"
+
+using namespace portal;
+
+namespace {
+
+constexpr float LOG2E_F = 1.4426950408889634f;
+// Face crossings closer than this (in units of r_max) are not taken.  The
+// reference uses 1e-10 (miscellaneous.f90:1048) against FP64 noise ~1e-16;
+// the FP32 walk's noise in t is ~1e-9, and a crossing shorter than 2e-8 is
+// 0.02 trace steps, i.e. it contributes nint(...) = 0 steps either way.
+constexpr float FACE_EPS = 2e-8f;
+
+struct LineConst {
+    double nu, A, B, kd, glo, gup, bb_cmb;
+    int lo, up;
+};
+constexpr int MAX_LINES = 64;
+
+// Compensated (Kahan) FP32 sum: J of one node is a sum of a few hundred ray
+// contributions; the compensation keeps it to ~1e-7 of the sum of magnitudes
+// without the FP64 pipe.
+struct KahanF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Line table: one thread per (node, line).
+__global__ void k_line_table(int N, int L, double dxp, const LineConst *__restrict__ lines,
+                             const double *__restrict__ levp, int nlev, const double *__restrict__ b,
+                             const double *__restrict__ dustp, const double *__restrict__ tdust,
+                             float4 *__restrict__ ltab) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * L) return;
+    int n = (int)(t / L), l = (int)(t - (long long)n * L);
+    const LineConst lc = lines[l];
+    double p1 = levp[(size_t)nlev * n + lc.lo];
+    double p2 = levp[(size_t)nlev * n + lc.up];
+    // ray_in inverse_rt.f90:263-266, 293-294, 298-301
+    double c1 = 2.2102191e-42 * lc.nu;
+    double c2 = 5.272859e-35 * lc.nu;
+    double cnu = 299792458.0 / lc.nu;
+    double kv = c1 * lc.B * (p1 - lc.glo * p2 / lc.gup);
+    double ev = c2 * lc.A * p2;
+    double phif = cnu / (1.7724538509055160273 * b[n]) * dxp;
+    double Ad = lc.kd * dustp[n] * dxp;
+    double Td = tdust[n];
+    double Ibb = 0.0;
+    if (Td != 0.0) {  // black_body miscellaneous.f90:263-285
+        double c2b = 4.79924e-11 / Td;
+        Ibb = 1.4744995e-50 * lc.nu * lc.nu * lc.nu / (exp(c2b * lc.nu) - 1.0);
+    }
+    // (optical depth per trace step at unit profile, line source function
+    // ev/kv, dust optical depth per step, dust emissivity per step): the
+    // source function is stored as the FP64 ratio, not the emissivity, so a
+    // weak line's S keeps full FP32 precision where kv and ev alone would be
+    // FP32 denormals
+    ltab[t] = make_float4((float)(kv * phif), (float)(kv != 0.0 ? ev / kv : 0.0), (float)Ad, (float)(Ad * Ibb));
+}
+
+template <int NLG, bool DUST>
+struct CellRec {
+    float q0[32], dq[32];
+    int cell[32];        // cell id and trace steps (the remainder channel's pass)
+    float fst[32];
+    float As[32][NLG];   // A * steps
+    float Ss[32][NLG];   // S (no dust) or E * steps (dust)
+    float Ad[32][DUST ? NLG : 1];   // dust tau per cell (dust only)
+    float Jd[32][DUST ? NLG : 1];   // dust emissivity * steps (dust only)
+};
+
+// Per-warp shared state of the node being processed and its current batch of
+// (up to) 32 rays.
+struct RayBatch {
+    double frame[13];    // b(3), x(3), w(3), node position(3), |p|^2
+    float4 dir[32];      // (d_x, d_y, d_z, v_node . d) per ray
+    int K[32];           // segments per ray (-1: n_depth overflow)
+};
+
+// NS channel slots per lane, NLG lines per register group.
+// RT = 0: nch <= 32 NS, every channel in a slot.  RT = 1: nch = 32 NS + 1
+// (the reference's 2 nvel + 1 channels with nvel a multiple of 16): the
+// last channel (nv = +nvel) is integrated lanes-over-lines (lane = line,
+// L <= 32) in the first line-group pass instead of costing a whole slot of
+// 32 lanes for one channel.
+// BATCH: the work items are (model, node) pairs of many models (RFBatch);
+// each warp copies the argument block of its current model into shared
+// memory.  Otherwise the nodes of the one model a0.
+template <int NS, int NLG, bool DUST, bool BATCH, int RT>
+__global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiation_field(RFArgs a0, RFBatch bw) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    const int n_depth = BATCH ? bw.n_depth : a0.n_depth;
+    int2 *const wbase = (BATCH ? bw.walk : a0.walk) + (size_t)gw * 32 * (size_t)n_depth;
+    __shared__ CellRec<NLG, DUST> recs[8];
+    __shared__ RayBatch rbs[8];
+    __shared__ RFArgs margs[BATCH ? 8 : 1];
+    CellRec<NLG, DUST> &R = recs[wib];
+    RayBatch &B = rbs[wib];
+
+    unsigned long long nseg = 0;
+    int cur_model = -1;
+    for (;;) {
+        int node = 0;
+        if (BATCH) {
+            long long item = 0;
+            if (lane == 0) item = (long long)atomicAdd(&bw.queue[0], 1ULL);
+            item = __shfl_sync(FULL, item, 0);
+            if (item >= bw.n_items) break;
+            const int2 wi = bw.items[item];
+            if (wi.x != cur_model) {
+                __syncwarp();
+                const int *src = reinterpret_cast<const int *>(bw.models + wi.x);
+                int *dst = reinterpret_cast<int *>(&margs[wib]);
+                for (int k = lane; k < (int)(sizeof(RFArgs) / sizeof(int)); k += 32) dst[k] = src[k];
+                __syncwarp();
+                cur_model = wi.x;
+            }
+            node = wi.y;
+        } else {
+            if (lane == 0) node = (int)atomicAdd(&a0.counters[0], 1ULL);
+            node = __shfl_sync(FULL, node, 0);
+            if (node >= a0.bulk) break;
+        }
+        const RFArgs &a = BATCH ? margs[wib] : a0;
+        KahanF acc0a, acc0b, acc2a, acc2b;  // lines lane and lane+32, compensated FP32
+        KahanF accEa, accEb, accLa, accLb;  // J_eff and L* of the same lines (split field only)
+        const bool split = (a.JE != nullptr);
+        int st = 0;
+        if (a.ab[node] > 0.0) {
+            if (lane == 0) {
+                // node frame (find_dir miscellaneous.f90:48-82): x = b x g / |b x g|,
+                // dir = R(b,ph) R(x,th) b = cos th b + sin th (cos ph (x x b) + sin ph x)
+                const double bx = a.bvec[3 * (size_t)node], by = a.bvec[3 * (size_t)node + 1],
+                             bz = a.bvec[3 * (size_t)node + 2];
+                double xx = by * a.gz - bz * a.gy, xy = bz * a.gx - bx * a.gz, xz = bx * a.gy - by * a.gx;
+                const double xn = sqrt(xx * xx + xy * xy + xz * xz);
+                xx /= xn; xy /= xn; xz /= xn;
+                const double px = a.pos[3 * (size_t)node], py = a.pos[3 * (size_t)node + 1],
+                             pz = a.pos[3 * (size_t)node + 2];
+                double *f = B.frame;
+                f[0] = bx; f[1] = by; f[2] = bz; f[3] = xx; f[4] = xy; f[5] = xz;
+                f[6] = xy * bz - xz * by; f[7] = xz * bx - xx * bz; f[8] = xx * by - xy * bx;
+                f[9] = px; f[10] = py; f[11] = pz; f[12] = px * px + py * py + pz * pz;
+            }
+            __syncwarp();
+            const float4 cvn = a.cellv[node];
+            const float dqfac = 2.f * cvn.w / (float)a.nvel;
+
+            for (int k0 = 0; k0 < a.ndir && st == 0; k0 += 32) {
+                const int nr = min(32, a.ndir - k0);
+                // ---- (1)+(2) set-up and walk, one lane per ray ----
+                int K = 0;
+                bool over = false;
+                if (lane < nr) {
+                    const double *dr = a.dirs + 6 * (size_t)(k0 + lane);
+                    const double *f = B.frame;
+                    const double mu = dr[0], sth = dr[1], cph = dr[2], sph = dr[3];
+                    const double dx = mu * f[0] + sth * (cph * f[6] + sph * f[3]);
+                    const double dy = mu * f[1] + sth * (cph * f[7] + sph * f[4]);
+                    const double dz = mu * f[2] + sth * (cph * f[8] + sph * f[5]);
+                    const double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
+                    const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+                    B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
+                    int2 *wl = wbase + (size_t)lane * n_depth;
+                    // distance left to the sphere exit as an unevaluated float pair
+                    // (rh + rl), decremented exactly by each step
+                    float rh = (float)sexit, rl = (float)(sexit - (double)rh);
+                    float rx = 0.f, ry = 0.f, rz = 0.f;
+                    int c = node;
+                    for (;;) {
+                        const float tsph = rh + rl;
+                        const int o = a.off[c], deg = a.off[c + 1] - o;
+                        // check_neigh_fast's scan: best starts at the sphere exit, a
+                        // neighbour replaces it when FACE_EPS < t <= best (so among equal
+                        // t the later neighbour wins).  t = num/den compared by cross
+                        // multiplication (den > 0).
+                        float bnum = tsph, bden = 1.f;
+                        int bj = -1;
+                        for (int j = 0; j < deg; j++) {
+                            const float4 e = a.edge[o + j];
+                            const float den = e.x * fdx + e.y * fdy + e.z * fdz;
+                            const float num = e.w - (e.x * rx + e.y * ry + e.z * rz);
+                            if (den > 0.f && num > FACE_EPS * den && num * bden <= bnum * den) {
+                                bnum = num;
+                                bden = den;
+                                bj = j;
+                            }
+                        }
+                        const float delta = (bj < 0) ? tsph : bnum / bden;
+                        if (K >= n_depth) { over = true; break; }
+                        wl[K] = make_int2(c, (int)roundf(delta / a.dx32));  // nint(delta_x/dx)
+                        K++;
+                        if (bj < 0) break;
+                        const float4 e = a.edge[o + bj];
+                        {   // (rh, rl) -= delta: two-sum, then renormalise
+                            const float t = rh - delta;
+                            const float bv = t - rh;
+                            const float err = (rh - (t - bv)) - (delta + bv);
+                            const float lo = rl + err;
+                            rh = t + lo;
+                            rl = lo - (rh - t);
+                        }
+                        rx = fmaf(delta, fdx, rx) - e.x;
+                        ry = fmaf(delta, fdy, ry) - e.y;
+                        rz = fmaf(delta, fdz, rz) - e.z;
+                        c = a.idx[o + bj];
+                    }
+                }
+                B.K[lane] = over ? -1 : K;
+                if (__any_sync(FULL, over)) { st |= PORTAL_NODE_DEPTH; break; }
+                __syncwarp();
+
+                // ---- (3)+(4) channel integration of each ray of the batch ----
+                for (int rr = 0; rr < nr; rr++) {
+                    const int Kr = B.K[rr];
+                    const int2 *wl = wbase + (size_t)rr * n_depth;
+                    const float4 d4 = B.dir[rr];
+                    const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
+                    const float wgt = (float)dr[4], wgt2 = (float)dr[5];
+                    nseg += (unsigned long long)Kr;
+                    const int2 w0 = wl[0];
+                    // the remainder channel of this lane's line (RT): intensity, and
+                    // its central-cell contributions to J0 (and J_eff, L*)
+                    float Irem = 0.f, remJ = 0.f, remE = 0.f, remL = 0.f;
+                    if (RT && lane < a.L) Irem = a.bb[lane];
+                    for (int l0 = 0; l0 < a.L; l0 += NLG) {
+                        // intensities of the lane's channels: slot pairs (s, s+1) in one
+                        // float2 (packed FP32x2 arithmetic), an odd last slot in .x
+                        float2 I2[(NS + 1) / 2][NLG];
+#define IV(s, l) (((s) & 1) ? I2[(s) >> 1][l].y : I2[(s) >> 1][l].x)
+#pragma unroll
+                        for (int l = 0; l < NLG; l++) {
+                            const float bb = (l0 + l < a.L) ? a.bb[l0 + l] : 0.f;
+#pragma unroll
+                            for (int s2 = 0; s2 < NS; s2++) IV(s2, l) = bb;
+                        }
+                        for (int hi = Kr - 1; hi >= 1; hi -= 32) {
+                            const int nc = min(32, hi);
+                            __syncwarp();
+                            if (lane < nc) {
+                                const int2 wc = wl[hi - lane];
+                                const float4 cv = a.cellv[wc.x];
+                                const float vp = cv.x * d4.x + cv.y * d4.y + cv.z * d4.z;
+                                const float ib = 1.f / cv.w;
+                                R.q0[lane] = (d4.w - vp) * ib;
+                                R.dq[lane] = dqfac * ib;
+                                const float fst = (float)wc.y;
+                                if (RT) {
+                                    R.cell[lane] = wc.x;
+                                    R.fst[lane] = fst;
+                                }
+                                const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
+#pragma unroll
+                                for (int l = 0; l < NLG; l++) {
+                                    if (DUST) {
+                                        if (l0 + l < a.L) {
+                                            const float4 v = lt[l];
+                                            R.As[lane][l] = v.x * fst;
+                                            R.Ss[lane][l] = v.y * v.x * fst;   // emissivity x steps
+                                            R.Ad[lane][DUST ? l : 0] = v.z * fst;
+                                            R.Jd[lane][DUST ? l : 0] = v.w * fst;
+                                        }
+                                    } else {
+                                        // optical depth at unit profile in log2 units (ex2
+                                        // takes it as is) and the source function.  A cell
+                                        // line with kv <= 0 fails ray_in's gate tau > 1e-30
+                                        // in every channel (inverse_rt.f90:308), and so does
+                                        // a padding line of the last group: both get A = S
+                                        // = 0, which leaves I unchanged exactly.
+                                        float As = 0.f, Ss = 0.f;
+                                        if (l0 + l < a.L) {
+                                            const float4 v = lt[l];
+                                            if (v.x > 0.f) {
+                                                As = v.x * fst * LOG2E_F;
+                                                Ss = v.y;
+                                            }
+                                        }
+                                        R.As[lane][l] = As;
+                                        R.Ss[lane][l] = Ss;
+                                    }
+                                }
+                            }
+                            __syncwarp();
+                            if (RT && l0 == 0 && lane < a.L) {
+                                // the remainder channel, lane = line, the same cells inward
+                                const float chr = (float)(32 * NS - a.nvel);
+                                for (int u = 0; u < nc; u++) {
+                                    const float4 v = a.ltab[(size_t)R.cell[u] * a.L + lane];
+                                    const float q = fmaf(R.dq[u], chr, R.q0[u]);
+                                    const float gr = ex2(-q * q * LOG2E_F);
+                                    const float As = (v.x > 0.f) ? v.x * R.fst[u] * LOG2E_F : 0.f;
+                                    const float Ss = (v.x > 0.f) ? v.y : 0.f;
+                                    const float x = As * gr;
+                                    Irem = fmaf(one_minus_exp(x, ex2(-x)), Ss - Irem, Irem);
+                                }
+                            }
+                            for (int u = 0; u < nc; u++) {
+                                const float q0 = R.q0[u], dq = R.dq[u];
+                                // Gaussian profile of the cell at the lane's channels,
+                                // slot pairs on the packed pipe (the same roundings as
+                                // ex2(-q q log2 e) per slot)
+                                float g[NS];
+#pragma unroll
+                                for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
+                                    const float2 ch2 = make_float2((float)(lane + 32 * s2 - a.nvel),
+                                                                   (float)(lane + 32 * (s2 + 1) - a.nvel));
+                                    const float2 q = __ffma2_rn(make_float2(dq, dq), ch2, make_float2(q0, q0));
+                                    const float2 t = __fmul2_rn(__fmul2_rn(q, q), make_float2(-LOG2E_F, -LOG2E_F));
+                                    g[s2] = ex2(t.x);
+                                    g[s2 + 1] = ex2(t.y);
+                                }
+                                if (NS & 1) {
+                                    const float q = fmaf(dq, (float)(lane + 32 * (NS - 1) - a.nvel), q0);
+                                    g[NS - 1] = ex2(-q * q * LOG2E_F);
+                                }
+#pragma unroll
+                                for (int l = 0; l < NLG; l++) {
+                                    const float Au = R.As[u][l];
+                                    const float Su = R.Ss[u][l];
+                                    if (DUST) {
+                                        if (l0 + l < a.L) {
+                                            const float Adu = R.Ad[u][DUST ? l : 0], Jdu = R.Jd[u][DUST ? l : 0];
+#pragma unroll
+                                            for (int s2 = 0; s2 < NS; s2++) {
+                                                // tau = (kv phi + alpha) dx n, S = (ev phi + j)/(kv phi + alpha)
+                                                const float tau = fmaf(Au, g[s2], Adu);
+                                                const float Sv = fmaf(Su, g[s2], Jdu) / tau;
+                                                const float x = tau * LOG2E_F;
+                                                const float om = one_minus_exp(x, ex2(-x));
+                                                const float In = fmaf(om, Sv - IV(s2, l), IV(s2, l));
+                                                IV(s2, l) = (tau > 1e-30f) ? In : IV(s2, l);
+                                            }
+                                        }
+                                    } else {
+                                        // I' = I + (1 - e^-tau)(S - I) with 1 - e^-tau accurate
+                                        // down to tau = 0 and rounded as the reference's FP64
+                                        // (one_minus_exp).  ray_in's gate tau > 1e-30
+                                        // (inverse_rt.f90:308) needs no test: lines with kv <= 0
+                                        // carry A = S = 0 and leave I unchanged exactly, and
+                                        // 0 < tau < 2^-54 rounds to a zero weight as in FP64.
+                                        // Branch-free, so the NS x NLG update chains of a cell
+                                        // interleave (a uniform thin-line branch measured 7 %
+                                        // slower).  Channel-slot pairs go through the packed
+                                        // FP32x2 pipe (one issue slot for two updates).
+                                        const float2 A2 = make_float2(Au, Au), S2 = make_float2(Su, Su);
+#pragma unroll
+                                        for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
+                                            const float2 x = __fmul2_rn(A2, make_float2(g[s2], g[s2 + 1]));
+                                            const float2 om = one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
+                                            float2 &Ip = I2[s2 >> 1][l];
+                                            Ip = __ffma2_rn(om, __ffma2_rn(Ip, make_float2(-1.f, -1.f), S2), Ip);
+                                        }
+                                        if (NS & 1) {
+                                            const float x = Au * g[NS - 1];
+                                            const float om = one_minus_exp(x, ex2(-x));
+                                            float &Is = I2[NS >> 1][l].x;
+                                            Is = fmaf(om, Su - Is, Is);
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                        // central cell (inverse_rt.f90:320-339): no gate, profile at
+                        // the node's own b, then the weighted channel sum
+                        const float fst0 = (float)w0.y;
+                        if (RT && l0 == 0 && lane < a.L) {
+                            const int ch = 32 * NS;
+                            const float4 v = a.ltab[(size_t)node * a.L + lane];
+                            const float q0c = a.chq[ch];
+                            const float g0 = ex2(-q0c * q0c * LOG2E_F);
+                            const float x = v.x * g0 * fst0 * LOG2E_F;
+                            const float om = one_minus_exp(x, ex2(-x));
+                            remJ = a.chw[ch] * fmaf(om, v.y - Irem, Irem);
+                            if (split) {
+                                remE = a.chw[ch] * fmaf(om, -Irem, Irem);
+                                remL = a.chw[ch] * om;
+                            }
+                        }
+                        float part[NLG], pe[NLG], pl[NLG];
+#pragma unroll
+                        for (int l = 0; l < NLG; l++) {
+                            part[l] = 0.f;
+                            pe[l] = 0.f;
+                            pl[l] = 0.f;
+                            if (l0 + l < a.L) {
+                                const float4 v = a.ltab[(size_t)node * a.L + l0 + l];
+#pragma unroll
+                                for (int s2 = 0; s2 < NS; s2++) {
+                                    const int ch = lane + 32 * s2;
+                                    if (ch < a.nch) {
+                                        const float q0c = a.chq[ch];
+                                        const float g0 = ex2(-q0c * q0c * LOG2E_F);
+                                        float tau, Sv, lf = 1.f, Sd = 0.f;
+                                        if (DUST) {
+                                            const float kap = fmaf(v.x, g0, v.z);
+                                            tau = kap * fst0;
+                                            Sv = fmaf(v.y * v.x, g0, v.w) / kap;
+                                            lf = v.x * g0 / kap;   // line share of the opacity
+                                            Sd = v.w / kap;        // dust emission share of S
+                                        } else {
+                                            tau = v.x * g0 * fst0;
+                                            Sv = v.y;
+                                        }
+                                        const float x = tau * LOG2E_F;
+                                        const float e = ex2(-x);
+                                        const float om = one_minus_exp(x, e);
+                                        const float Io = fmaf(om, Sv - IV(s2, l), IV(s2, l));
+                                        part[l] = fmaf(a.chw[ch], Io, part[l]);
+                                        if (split) {
+                                            pe[l] = fmaf(a.chw[ch], fmaf(om, Sd - IV(s2, l), IV(s2, l)), pe[l]);
+                                            pl[l] = fmaf(a.chw[ch], lf * om, pl[l]);
+                                        }
+                                    }
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int l = 0; l < NLG; l++) {
+                            float v = part[l];
+#pragma unroll
+                            for (int o2 = 16; o2 >= 1; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
+                            const int line = l0 + l;
+                            if (line < a.L && (line & 31) == lane) {
+                                if (line < 32) {
+                                    if (RT) v += remJ;   // this lane's line: its remainder channel
+                                    acc0a.add(wgt * v);
+                                    acc2a.add(wgt2 * v);
+                                } else {
+                                    acc0b.add(wgt * v);
+                                    acc2b.add(wgt2 * v);
+                                }
+                            }
+                        }
+                        if (split) {
+#pragma unroll
+                            for (int l = 0; l < NLG; l++) {
+                                float ve = pe[l], vl = pl[l];
+#pragma unroll
+                                for (int o2 = 16; o2 >= 1; o2 >>= 1) {
+                                    ve += __shfl_xor_sync(FULL, ve, o2);
+                                    vl += __shfl_xor_sync(FULL, vl, o2);
+                                }
+                                const int line = l0 + l;
+                                if (line < a.L && (line & 31) == lane) {
+                                    if (line < 32) {
+                                        if (RT) {
+                                            ve += remE;
+                                            vl += remL;
+                                        }
+                                        accEa.add(wgt * ve);
+                                        accLa.add(wgt * vl);
+                                    } else {
+                                        accEb.add(wgt * ve);
+                                        accLb.add(wgt * vl);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+#undef IV
+        if (lane < a.L) {
+            a.J0[(size_t)node * a.L + lane] = (st == 0) ? acc0a.value() : 0.0;
+            a.J2[(size_t)node * a.L + lane] = (st == 0) ? acc2a.value() : 0.0;
+        }
+        if (lane + 32 < a.L) {
+            a.J0[(size_t)node * a.L + lane + 32] = (st == 0) ? acc0b.value() : 0.0;
+            a.J2[(size_t)node * a.L + lane + 32] = (st == 0) ? acc2b.value() : 0.0;
+        }
+        if (split) {
+            if (lane < a.L) {
+                a.JE[(size_t)node * a.L + lane] = (st == 0) ? accEa.value() : 0.0;
+                a.LS[(size_t)node * a.L + lane] = (st == 0) ? accLa.value() : 0.0;
+            }
+            if (lane + 32 < a.L) {
+                a.JE[(size_t)node * a.L + lane + 32] = (st == 0) ? accEb.value() : 0.0;
+                a.LS[(size_t)node * a.L + lane + 32] = (st == 0) ? accLb.value() : 0.0;
+            }
+        }
+        if (lane == 0) a.status[node] = st;
+        __syncwarp();
+    }
+    // segment count (every lane holds the same count)
+    if (lane == 0) atomicAdd(BATCH ? &bw.queue[1] : &a0.counters[1], nseg);
+}
+
+}  // namespace
+
+namespace {
+
+// Channel layout: (slots per lane, remainder channel).  2 nvel + 1 channels
+// with nvel a multiple of 16 take 2 nvel / 32 full slots plus the
+// lanes-over-lines remainder channel (no dust, at most 32 lines); any other
+// count is padded to whole slots.
+struct ChanLayout {
+    int ns, rt;
+};
+inline ChanLayout chan_layout(int nch, bool dust, int max_lines) {
+    if (!dust && max_lines <= 32 && nch > 32 && nch % 32 == 1) {
+        const int k = nch / 32;
+        if (k == 1 || k == 2 || k == 4 || k == 8) return {k, 1};
+    }
+    if (nch <= 32) return {1, 0};
+    if (nch <= 64) return {2, 0};
+    if (nch <= 96) return {3, 0};
+    if (nch <= 160) return {5, 0};
+    return {9, 0};
+}
+
+}  // namespace
