@@ -150,8 +150,14 @@ __global__ void __launch_bounds__(128) k_gemm(int M, int N, int K, const float *
 // the CTA stops and still frees its tensor memory.
 constexpr int TC_M = 128;
 
+// the A tile's region doubles as the epilogue's transpose buffer (4 KB per
+// warp of 512 threads) once a tile's MMAs are complete
+constexpr int TC_EPI_BYTES = 16 * 32 * 32 * 4;
+__host__ __device__ inline size_t tc_a_bytes(int Kp) {
+    return (size_t)TC_M * Kp * 2 > (size_t)TC_EPI_BYTES ? (size_t)TC_M * Kp * 2 : (size_t)TC_EPI_BYTES;
+}
 __host__ __device__ inline size_t tc_smem_bytes(int Np, int Kp) {
-    return (size_t)TC_M * Kp * 2 + (size_t)Np * Kp * 2 + 16;
+    return tc_a_bytes(Kp) + (size_t)Np * Kp * 2 + 16;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -160,43 +166,62 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 }
 
 // rows [r0, r0 + rows) of the row-major src (ld floats per row, K valid
-// columns, nrow_valid valid rows) into the canonical BF16 tile
+// columns, nrow_valid valid rows) into the canonical BF16 tile; each thread
+// first loads TC_U chunks (two float4 each) and then converts them, so that
+// many loads are in flight per thread
+constexpr int TC_THREADS = 512;
+constexpr int TC_U = 4;
+
+__device__ __forceinline__ void tc_load8(const float *p, bool valid, int nk, float *v) {
+    if (valid && nk >= 8 && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+        const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+        const float4 y = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+        v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = (valid && j < nk) ? p[j] : 0.f;
+    }
+}
+
 __device__ __forceinline__ void tc_stage(unsigned char *tile, int rows, int Kp, const float *__restrict__ src,
                                          int r0, int nrow_valid, int K, int ld, int tid) {
     const int kc = Kp / 8;
     const uint32_t sbo = (uint32_t)kc * 128;
-    for (int i = tid; i < rows * kc; i += 128) {
-        const int r = i / kc, c = i - r * kc;
-        const int k0 = c * 8;
-        float v[8];
-        const float *p = src + (size_t)(r0 + r) * ld + k0;
-        if (r < nrow_valid && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
-            const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
-            const float4 y = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-            v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
-            v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
-        } else {
+    const int total = rows * kc;
+    for (int base = tid; base < total; base += TC_THREADS * TC_U) {
+        float v[TC_U][8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) v[j] = (r < nrow_valid && k0 + j < K) ? p[j] : 0.f;
+        for (int u = 0; u < TC_U; u++) {
+            const int i = base + u * TC_THREADS;
+            const int r = i / kc, c = i - r * kc;
+            tc_load8(src + (size_t)(r0 + r) * ld + c * 8, i < total && r < nrow_valid, K - c * 8, v[u]);
         }
-        uint4 q;
-        q.x = pack_bf16x2(v[0], v[1]);
-        q.y = pack_bf16x2(v[2], v[3]);
-        q.z = pack_bf16x2(v[4], v[5]);
-        q.w = pack_bf16x2(v[6], v[7]);
-        *reinterpret_cast<uint4 *>(tile + (size_t)(r >> 3) * sbo + (size_t)c * 128 + (size_t)(r & 7) * 16) = q;
+#pragma unroll
+        for (int u = 0; u < TC_U; u++) {
+            const int i = base + u * TC_THREADS;
+            if (i >= total) break;
+            const int r = i / kc, c = i - r * kc;
+            uint4 q;
+            q.x = pack_bf16x2(v[u][0], v[u][1]);
+            q.y = pack_bf16x2(v[u][2], v[u][3]);
+            q.z = pack_bf16x2(v[u][4], v[u][5]);
+            q.w = pack_bf16x2(v[u][6], v[u][7]);
+            *reinterpret_cast<uint4 *>(tile + (size_t)(r >> 3) * sbo + (size_t)c * 128 + (size_t)(r & 7) * 16) = q;
+        }
     }
 }
 
-__global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, int Np, int Kp, uint32_t tcols,
-                                                    const float *__restrict__ A, const float *__restrict__ W,
-                                                    EpiArgs e, int *err) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_gemm_tc(int M, int N, int K, int Np, int Kp, uint32_t tcols,
+                                                           const float *__restrict__ A, const float *__restrict__ W,
+                                                           EpiArgs e, int *err) {
     extern __shared__ __align__(1024) unsigned char tsm[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     unsigned char *As = tsm;
-    unsigned char *Bs = tsm + (size_t)TC_M * Kp * 2;
+    unsigned char *Bs = tsm + tc_a_bytes(Kp);
     uint64_t *bar = reinterpret_cast<uint64_t *>(Bs + (size_t)Np * Kp * 2);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    float *T = reinterpret_cast<float *>(As) + (size_t)warp * 32 * 32;  // this warp's 32 x 32 transpose buffer
     tc_stage(Bs, Np, Kp, W, 0, N, K, K, tid);
     if (warp == 0) umma::tmem_alloc(tslot, tcols);
     if (tid == 0) {
@@ -209,6 +234,9 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, int Np,
     const uint32_t idesc = umma::idesc_bf16_f32(TC_M, Np);
     const uint32_t sbo = (uint32_t)(Kp / 8) * 128;
     const int ntiles = (M + TC_M - 1) / TC_M;
+    // epilogue split: warp w reads the lane quarter w % 4 (tcgen05.ld's rule)
+    // and every (TC_THREADS / 128)-th 32-column chunk from chunk w / 4
+    const int quarter = warp & 3, cgroup = warp >> 2, ngroups = TC_THREADS / 128;
     int iter = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, iter++) {
@@ -233,24 +261,28 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, int Np,
             if (tid == 0) atomicExch(err, 1);
             break;
         }
-        const int row = m0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < Np; c0 += 32) {
+        // epilogue: thread t of the warp holds row (rbase + t), columns c0..c0+31;
+        // through the warp's transpose buffer (XOR-swizzled, no bank
+        // conflicts) each store instruction then writes 32 consecutive
+        // columns of one row
+        const int rbase = m0 + quarter * 32;
+        for (int c0 = cgroup * 32; c0 < Np; c0 += 32 * ngroups) {
             float v[32];
-            umma::tmem_ld32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (row < M) {
+            umma::tmem_ld32(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
+            const int cl = c0 + lane;                  // the column this lane stores
+            const float bl = (e.kind != EPI_STORE && cl < N) ? e.bias[cl] : 0.f;
+            __syncwarp();
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int c = c0 + j;
-                    if (c >= N) break;
-                    const size_t o = (size_t)row * e.ldc + c;
-                    if (e.kind == EPI_BIAS) {
-                        e.C[o] = v[j] + e.bias[c];
-                    } else if (e.kind == EPI_BIAS_SILU) {
-                        const float z = v[j] + e.bias[c];
-                        e.Z[o] = z;
-                        e.C[o] = z * sigm(z);
-                    } else {
-                        e.C[o] = v[j];
+            for (int j = 0; j < 32; j++) T[lane * 32 + (j ^ lane)] = v[j];
+            __syncwarp();
+            for (int pass = 0; pass < (e.kind == EPI_BIAS_SILU ? 2 : 1); pass++) {
+                float *dst = (pass == 0 && e.kind == EPI_BIAS_SILU) ? e.Z : e.C;
+                for (int r = 0; r < 32; r++) {
+                    const int row = rbase + r;
+                    if (row >= M) break;
+                    if (cl < N) {
+                        const float z = T[r * 32 + (lane ^ r)] + bl;
+                        dst[(size_t)row * e.ldc + cl] = (e.kind == EPI_BIAS_SILU && pass == 1) ? z * sigm(z) : z;
                     }
                 }
             }
@@ -390,7 +422,7 @@ void gemm_tc(cudaStream_t s, int M, int N, int K, const float *A, const float *W
         if (nsm < 1) nsm = 1;
     }
     const int ntiles = (M + TC_M - 1) / TC_M;
-    k_gemm_tc<<<std::min(ntiles, nsm), 128, smem, s>>>(M, N, K, Np, Kp, tcols, A, W, e, err);
+    k_gemm_tc<<<std::min(ntiles, nsm), TC_THREADS, smem, s>>>(M, N, K, Np, Kp, tcols, A, W, e, err);
 }
 
 // activation workspace layout for a batch of B rows:
