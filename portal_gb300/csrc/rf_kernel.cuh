@@ -306,15 +306,27 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             if (RT && l0 == 0 && lane < a.L) {
                                 // the remainder channel, lane = line, the same cells inward
                                 const float chr = (float)(32 * NS - a.nvel);
-                                for (int u = 0; u < nc; u++) {
-                                    const float4 v = a.ltab[(size_t)R.cell[u] * a.L + lane];
+                                auto step = [&](const float4 v, int u) {
                                     const float q = fmaf(R.dq[u], chr, R.q0[u]);
                                     const float gr = ex2(-q * q * LOG2E_F);
                                     const float As = (v.x > 0.f) ? v.x * R.fst[u] * LOG2E_F : 0.f;
                                     const float Ss = (v.x > 0.f) ? v.y : 0.f;
                                     const float x = As * gr;
                                     Irem = fmaf(one_minus_exp(x, ex2(-x)), Ss - Irem, Irem);
+                                };
+                                // four cells' line-table reads are issued together
+                                int u = 0;
+                                for (; u + 4 <= nc; u += 4) {
+                                    const float4 v0 = a.ltab[(size_t)R.cell[u] * a.L + lane];
+                                    const float4 v1 = a.ltab[(size_t)R.cell[u + 1] * a.L + lane];
+                                    const float4 v2 = a.ltab[(size_t)R.cell[u + 2] * a.L + lane];
+                                    const float4 v3 = a.ltab[(size_t)R.cell[u + 3] * a.L + lane];
+                                    step(v0, u);
+                                    step(v1, u + 1);
+                                    step(v2, u + 2);
+                                    step(v3, u + 3);
                                 }
+                                for (; u < nc; u++) step(a.ltab[(size_t)R.cell[u] * a.L + lane], u);
                             }
                             for (int u = 0; u < nc; u++) {
                                 const float q0 = R.q0[u], dq = R.dq[u];

@@ -17,11 +17,13 @@ def _models():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("autotune", [True, False])
-def test_batch_matches_single_models(built_lib, autotune):
+@pytest.mark.parametrize("autotune,nvel", [(True, 12), (False, 12), (True, 16)])
+def test_batch_matches_single_models(built_lib, autotune, nvel):
+    """nvel 12: 25 channels in one padded slot; nvel 16: 33 channels, one
+    full slot plus the remainder channel integrated lanes-over-lines."""
     import portal_gb300 as pg
 
-    rc = synth.RunConfig(nth=8, nph=8, nvel=12, kmax=2, gvec=synth.gauge_vector(3))
+    rc = synth.RunConfig(nth=8, nph=8, nvel=nvel, kmax=2, gvec=synth.gauge_vector(3))
     models = _models()
     ctxs = []
     for cl, mol in models:
