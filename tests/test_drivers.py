@@ -137,3 +137,42 @@ def test_main_and_finish_portal_end_to_end(case):
     np.testing.assert_array_equal(dtau, cube[3, 0])
     h, ddust = lime.read_fits(os.path.join(d, "inc01-trans01-dust_i.fits"))
     assert ddust.shape == (1, 25, 25)
+
+
+def test_parallel_reader_matches_list_directed_forms(case, tmp_path):
+    """The bulk readers' fast path (one plain record per line, many threads)
+    and their list-directed fallback (records across lines, D exponents,
+    repeat counts) ingest the same arrays; so do 1 and many threads."""
+    p = case["paths"]
+    alt = dict(p)
+    # .pop: one row split over two lines, a D exponent, a repeat count
+    lines = open(p["pop"]).read().splitlines()
+    r = lines[5].split()
+    lines[5] = " ".join(r[:7]) + "\n" + " ".join(r[7:])
+    r = lines[9].split()
+    r[6] = r[6].replace("e", "D") if "e" in r[6] else r[6] + "D0"
+    lines[9] = " ".join(r)
+    r = lines[12].split()
+    assert float(r[11]) == float(r[12]) == 0.0
+    lines[12] = " ".join(r[:11] + ["2*0"] + r[13:])
+    alt["pop"] = str(tmp_path / "alt.pop")
+    open(alt["pop"], "w").write("\n".join(lines) + "\n")
+    # grid.vtk: one point record over two lines
+    g = open(p["grid"]).read().splitlines()
+    k = next(i for i, l in enumerate(g) if l.startswith("POINTS")) + 3
+    x = g[k].split()
+    g[k] = x[0] + "\n" + " ".join(x[1:])
+    alt["grid"] = str(tmp_path / "alt.vtk")
+    open(alt["grid"], "w").write("\n".join(g) + "\n")
+    dumps = []
+    for paths, threads in ((p, "1"), (p, "8"), (alt, "8")):
+        dd = tmp_path / ("dump_%d" % len(dumps))
+        dd.mkdir()
+        c2 = dict(case, paths=paths)
+        r = _run(MAIN, c2, dict(PORTAL_DUMP_INGESTED=str(dd), PORTAL_BVEC_FILE=p["bvec"], PORTAL_THREADS=threads))
+        assert r.returncode == 0, r.stderr
+        dumps.append({n: np.load(dd / (n + ".npy")) for n in ("xyz", "vel", "b_all", "lev_p", "del_ne",
+                                                               "del_num_ne", "h2_dens", "temp_all")})
+    for d in dumps[1:]:
+        for n, v in d.items():
+            np.testing.assert_array_equal(v, dumps[0][n], err_msg=n)
