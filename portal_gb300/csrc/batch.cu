@@ -203,7 +203,13 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
     // SE (warps per block; blocks per SM from the occupancy)
     struct RFC { int nlg, bps; };
     std::vector<RFC> rfc;
+    const void *seen = nullptr;
     for (int nlg : {5, 10}) {
+        // layouts with the lanes-over-lines remainder channel have one line
+        // group; do not time the same kernel twice
+        const void *k = rf_batch_kernel_ptr(b->nch, b->dust, nlg, b->max_lines);
+        if (k == seen) continue;
+        seen = k;
         int mx = 0;
         if (rf_batch_blocks_per_sm(b->nch, b->dust, nlg, b->max_lines, &mx))
             return bfail(b, PORTAL_ERR_CUDA, "occupancy query");

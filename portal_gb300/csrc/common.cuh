@@ -201,13 +201,15 @@ __device__ __forceinline__ float one_minus_exp(float x, float e) {
     return (fabsf(x) < OM_TAYLOR_X) ? om_taylor(x) : 1.f - e;
 }
 // The same for two optical depths at once on the packed FP32x2 pipe (the
-// same operations and roundings per element as one_minus_exp).
-__device__ __forceinline__ float2 one_minus_exp2(float2 x, float e0, float e1) {
+// same operations and roundings per element as om_taylor / one_minus_exp).
+__device__ __forceinline__ float2 om_taylor2(float2 x) {
     const float2 h = __ffma2_rn(x, __ffma2_rn(x, make_float2(0.0555041087f, 0.0555041087f),
                                               make_float2(-0.240226507f, -0.240226507f)),
                                 make_float2(0.693147181f, 0.693147181f));
-    const float2 t = __fadd2_rn(__ffma2_rn(x, h, make_float2(OM_MAGIC, OM_MAGIC)),
-                                make_float2(-OM_MAGIC, -OM_MAGIC));
+    return __fadd2_rn(__ffma2_rn(x, h, make_float2(OM_MAGIC, OM_MAGIC)), make_float2(-OM_MAGIC, -OM_MAGIC));
+}
+__device__ __forceinline__ float2 one_minus_exp2(float2 x, float e0, float e1) {
+    const float2 t = om_taylor2(x);
     const float2 b = __ffma2_rn(make_float2(e0, e1), make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     return make_float2((fabsf(x.x) < OM_TAYLOR_X) ? t.x : b.x, (fabsf(x.y) < OM_TAYLOR_X) ? t.y : b.y);
 }

@@ -87,6 +87,7 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
                bool split, RFArgs *a);
 int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s);
 int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int max_lines, int *blocks);
+const void *rf_batch_kernel_ptr(int nch, bool dust, int nlg, int max_lines);  // identity of the variant
 int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, int max_lines, const RFBatch &bw);
 // se.cu
 int se_prepare(portal_ctx *c, int kmax, SEArgs *a, size_t *warp_bytes);

@@ -38,6 +38,10 @@ const void *batch_kernel(int nch, bool dust, int nlg, int max_lines) {
 
 namespace portal {
 
+const void *rf_batch_kernel_ptr(int nch, bool dust, int nlg, int max_lines) {
+    return batch_kernel(nch, dust, nlg, max_lines);
+}
+
 int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int max_lines, int *blocks) {
     const void *k = batch_kernel(nch, dust, nlg, max_lines);
     *blocks = 0;

@@ -373,9 +373,12 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                         // carry A = S = 0 and leave I unchanged exactly, and
                                         // 0 < tau < 2^-54 rounds to a zero weight as in FP64.
                                         // Branch-free, so the NS x NLG update chains of a cell
-                                        // interleave (a uniform thin-line branch measured 7 %
-                                        // slower).  Channel-slot pairs go through the packed
-                                        // FP32x2 pipe (one issue slot for two updates).
+                                        // interleave: a warp-uniform branch to a Taylor-only
+                                        // path for lines thin in the whole cell measured 24 %
+                                        // slower in spite of skipping the ex2 (1.45e9 against
+                                        // 1.90e9 segments/s).  Channel-slot pairs go through
+                                        // the packed FP32x2 pipe (one issue slot for two
+                                        // updates).
                                         const float2 A2 = make_float2(Au, Au), S2 = make_float2(Su, Su);
 #pragma unroll
                                         for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
