@@ -191,6 +191,25 @@ int portal_image(portal_ctx *ctx, const double *pol_pops, int nlines, const int 
                  float *U, float *tau, float *dust_I, float *dust_Q, float *dust_U,
                  float *dust_tau, int *status);
 
+/* Per-node maps of one inclination: the pix_mod = 0 mode of finish_portal.x
+ * (para_finish.f90:245-350).  As portal_image, but one ray per bulk node,
+ * started at the node's rotated sky position (x, y) = XYZ_inc(1:2, node)
+ * (:292), and every line's Einstein A taken as t_Aji(l1(j)) -- the radiative
+ * transition whose index equals the line's lower level (:303; the pixel mode
+ * matches (l1, l2) against r_trans), so l1 must not exceed the number of
+ * radiative transitions.  A node whose (x, y) lies outside the unit circle
+ * has no start point (the reference leaves its start node undefined): its
+ * status is 3 and its outputs NaN.
+ * Outputs (any may be NULL): xy(2, n_bulk) = tx * the rotated (x, y), the
+ * rows of inc%02d-xy.dat (:266-271); I, Q, U, tau and the dust I, Q, U, tau,
+ * each (n_bulk, 2*nvel+1, nlines) column-major and unscaled (the files
+ * inc%02d-trans%02d-vel%02d-im.dat hold I_to_T I, I_to_T Q, I_to_T U, tau,
+ * :331-349); status(n_bulk). */
+int portal_image_nodes(portal_ctx *ctx, const double *pol_pops, int nlines, const int *l1, const int *l2,
+                       double th_inc, double ph_az, int nvel, double dvel, double v0, double alpha, double dx,
+                       int n_depth_rt, double *xy, float *I, float *Q, float *U, float *tau, float *dust_I,
+                       float *dust_Q, float *dust_U, float *dust_tau, int *status);
+
 /* Radiation field for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  It serves callers that must not call

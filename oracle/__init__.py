@@ -178,6 +178,27 @@ class OracleProblem:
                                 n_depth_rt, pix_lo, pix_hi, nthreads, _p(out), _p(st, P_I))
         return out, st, nfail
 
+    def image_nodes(self, lines_l1, lines_l2, pol_pops, th_inc, ph_az, nvel, dvel, v0, alpha=0.15,
+                    n_depth_rt=10000, node_lo=0, node_hi=None, nthreads=0):
+        """Per-node mode (pix_mod = 0): raw cube (8, n_bulk, nlines, nchan) for
+        the bulk nodes node_lo..node_hi (the others stay 0), the xy rows
+        (n_bulk, 2) and the status per node."""
+        nb = self.cloud.bulk_node_num
+        nl = len(lines_l1)
+        l1 = np.ascontiguousarray(lines_l1, dtype=np.int32)
+        l2 = np.ascontiguousarray(lines_l2, dtype=np.int32)
+        ppF = np.ascontiguousarray(np.asarray(pol_pops, dtype=np.float64).T)
+        nch = 2 * nvel + 1
+        out = np.zeros((8, nb, nl, nch))
+        xy = np.zeros((nb, 2))
+        st = np.zeros(nb, dtype=np.int32)
+        node_hi = nb - 1 if node_hi is None else node_hi
+        nfail = lib().orc_image_nodes(C.byref(self.c), C.byref(self.m), nl, _p(l1, P_I), _p(l2, P_I), _p(ppF),
+                                      C.c_double(th_inc), C.c_double(ph_az), nvel, C.c_double(dvel),
+                                      C.c_double(v0), C.c_double(alpha), n_depth_rt, node_lo, node_hi, nthreads,
+                                      _p(xy), _p(out), _p(st, P_I))
+        return out, xy, st, nfail
+
 
 def legendre_all(nth, nph):
     xth = np.zeros((nth * nph, 3))

@@ -1269,16 +1269,21 @@ void orc_ray_in_raytrace(double vel_obs, int node_count, const int *depth_list,
     out[4] = I_dust; out[5] = Q_dust; out[6] = U_dust; out[7] = tau_d;
 }
 
-/* Pixel mode of finish_portal.x for one inclination: para_finish.f90:170-185
+/* Both modes of finish_portal.x for one inclination: para_finish.f90:170-185
  * (line data, including the nu0_all whole-array assignment of :173-175),
- * :222-240 (population read-back), :369-376 (pixel grid) and :382-448. */
-int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *l1,
-              const int *l2, const double *pol_pops_in, double th_inc, double ph_az, int nvel,
-              double dvel, double v0, int im_pix, double im_size, double alpha, int n_depth_rt,
-              int pix_lo, int pix_hi, int nthreads, double *out, int *status)
+ * :222-240 (population read-back), then either the pixel mode (:369-376 pixel
+ * grid, :382-448 loops; node_mode 0) or the per-node mode (:261-320; node_mode
+ * 1: one ray per bulk node from its rotated (x, y), the emission coefficients
+ * with t_Aji(l1(j)) as the Einstein A, :303). */
+static int image_impl(const orc_cloud *c, const orc_molecule *m, int nlines, const int *l1,
+                      const int *l2, const double *pol_pops_in, double th_inc, double ph_az,
+                      int nvel, double dvel, double v0, int node_mode, int im_pix, double im_size,
+                      double alpha, int n_depth_rt, int pix_lo, int pix_hi, int nthreads,
+                      double *xy, double *out, int *status)
 {
     int N = c->node_num, nlev = c->nlev;
-    int npx = 2 * im_pix + 1, n_rt = npx * npx, nchan = 2 * nvel + 1;
+    int npx = 2 * im_pix + 1, nchan = 2 * nvel + 1;
+    int n_rt = node_mode ? c->bulk_node_num : npx * npx;
     double *nu0_all = (double *)malloc(sizeof(double) * nlines);
     double *Aji_all = (double *)calloc(nlines, sizeof(double));
     double *kd_all = (double *)calloc(nlines, sizeof(double));
@@ -1292,6 +1297,8 @@ int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *
                 kd_all[i] = m->kd_v[j];
                 break;
             }
+    if (node_mode)  /* para_finish.f90:303 passes t_Aji(l1(j)) */
+        for (int i = 0; i < nlines; i++) Aji_all[i] = (l1[i] <= m->r_num) ? m->A[l1[i] - 1] : 0.0;
     /* population read-back para_finish.f90:226-239 */
     double *pp = (double *)malloc(sizeof(double) * (size_t)N * 2 * nlev);
     memcpy(pp, pol_pops_in, sizeof(double) * (size_t)N * 2 * nlev);
@@ -1327,6 +1334,11 @@ int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *
     }
 #undef PP
 #undef LP
+    if (node_mode && xy)  /* the rows of inc%02d-xy.dat, para_finish.f90:269-271 */
+        for (int n = 0; n < n_rt; n++) {
+            xy[2 * n] = c->tx * xyz_inc[3 * n];
+            xy[2 * n + 1] = c->tx * xyz_inc[3 * n + 1];
+        }
     double dx = F4(1e-4);
     int nfail = 0;
     if (pix_lo < 0) pix_lo = 0;
@@ -1339,8 +1351,15 @@ int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *
         int *dl = (int *)malloc(sizeof(int) * 2 * (size_t)(n_depth_rt + 2));
 #pragma omp for schedule(static)
         for (int p = pix_lo; p <= pix_hi; p++) {
-            int i = p / npx - im_pix, j = p % npx - im_pix;
-            double x = i * im_size / im_pix, y = j * im_size / im_pix;
+            double x, y;
+            if (node_mode) {
+                x = xyz_inc[3 * p];
+                y = xyz_inc[3 * p + 1];
+            } else {
+                int i = p / npx - im_pix, j = p % npx - im_pix;
+                x = i * im_size / im_pix;
+                y = j * im_size / im_pix;
+            }
             int nc = 0;
             int st = orc_trace_out_raytrace(x, y, N, xyz_inc, c->del_ne, c->del_num_ne, c->maxne,
                                             dx, n_depth_rt, dl, &nc);
@@ -1363,4 +1382,22 @@ int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *
     free(nu0_all); free(Aji_all); free(kd_all); free(pp); free(vel_inc); free(bvec_inc);
     free(xyz_inc); free(velz); free(pol_rayt);
     return nfail;
+}
+
+int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *l1,
+              const int *l2, const double *pol_pops_in, double th_inc, double ph_az, int nvel,
+              double dvel, double v0, int im_pix, double im_size, double alpha, int n_depth_rt,
+              int pix_lo, int pix_hi, int nthreads, double *out, int *status)
+{
+    return image_impl(c, m, nlines, l1, l2, pol_pops_in, th_inc, ph_az, nvel, dvel, v0, 0, im_pix,
+                      im_size, alpha, n_depth_rt, pix_lo, pix_hi, nthreads, NULL, out, status);
+}
+
+int orc_image_nodes(const orc_cloud *c, const orc_molecule *m, int nlines, const int *l1,
+                    const int *l2, const double *pol_pops_in, double th_inc, double ph_az,
+                    int nvel, double dvel, double v0, double alpha, int n_depth_rt, int node_lo,
+                    int node_hi, int nthreads, double *xy, double *out, int *status)
+{
+    return image_impl(c, m, nlines, l1, l2, pol_pops_in, th_inc, ph_az, nvel, dvel, v0, 1, 1, 0.0,
+                      alpha, n_depth_rt, node_lo, node_hi, nthreads, xy, out, status);
 }

@@ -158,6 +158,15 @@ int orc_image(const orc_cloud *c, const orc_molecule *m, int nlines, const int *
               int nvel, double dvel, double v0, int im_pix, double im_size,
               double alpha, int n_depth_rt, int pix_lo, int pix_hi, int nthreads,
               double *out, int *status);
+/* Per-node mode of finish_portal.x (pix_mod = 0, para_finish.f90:245-350) for
+ * one inclination: one ray per bulk node started at its rotated (x, y), the
+ * line's Einstein A taken as t_Aji(l1(j)) (:303).  xy(2, n_bulk) = tx * the
+ * rotated (x, y) (:269-271), or NULL; out as orc_image with p the bulk node,
+ * computed for nodes node_lo..node_hi. */
+int orc_image_nodes(const orc_cloud *c, const orc_molecule *m, int nlines, const int *l1,
+                    const int *l2, const double *pol_pops, double th_inc, double ph_az,
+                    int nvel, double dvel, double v0, double alpha, int n_depth_rt, int node_lo,
+                    int node_hi, int nthreads, double *xy, double *out, int *status);
 
 #ifdef __cplusplus
 }

@@ -30,7 +30,7 @@ KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_w
 EXPORTS = (
     "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
     "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
-    "portal_radiation_field", "portal_radiation_field_split", "portal_solve_se", "portal_image", "portal_last_kernel_times",
+    "portal_radiation_field", "portal_radiation_field_split", "portal_solve_se", "portal_image", "portal_image_nodes", "portal_last_kernel_times",
     "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
     "portal_radiation_field_static", "portal_radiation_field_static_limits",
@@ -80,6 +80,9 @@ def lib() -> C.CDLL:
     P_F = C.POINTER(C.c_float)
     L.portal_image.argtypes = [C.c_void_p, P_D, C.c_int, P_I, P_I, C.c_double, C.c_double, C.c_int, C.c_double,
                                C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int] + [P_F] * 8 + [P_I]
+    L.portal_image_nodes.argtypes = [C.c_void_p, P_D, C.c_int, P_I, P_I, C.c_double, C.c_double, C.c_int,
+                                     C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, P_D] + \
+        [C.POINTER(C.c_float)] * 8 + [P_I]
     L.portal_wigner3j.restype = C.c_double
     L.portal_wigner3j.argtypes = [C.c_int] * 6
     L.portal_wigner6j.restype = C.c_double
@@ -143,7 +146,7 @@ class Context:
         rc = lib().portal_create(C.byref(self._h), device)
         if rc != PORTAL_OK:
             raise PortalError(rc, lib().portal_last_error(None).decode())
-        self.nlev = self.r_num = self.N = 0
+        self.nlev = self.r_num = self.N = self.bulk = 0
 
     def close(self):
         if self._h:
@@ -193,7 +196,7 @@ class Context:
         self._check(lib().portal_set_cloud(self._h, N, cloud.bulk_node_num, cloud.nlev,
                                            *[_p(a) for a in arrs], dn.shape[0], _p(dn, P_I), _p(dnn, P_I),
                                            float(cloud.tx)))
-        self.N = N
+        self.N, self.bulk = N, cloud.bulk_node_num
 
     def set_cloud_arrays(self, N, bulk, nlev, xyz, vel, b_all, temp_all, dust_p, h2_dens, ab_all, lev_p,
                          bvec, del_ne, del_num_ne, tx):
@@ -202,7 +205,7 @@ class Context:
         self._check(lib().portal_set_cloud(self._h, N, bulk, nlev, _p(xyz), _p(vel), _p(b_all), _p(temp_all),
                                            _p(dust_p), _p(h2_dens), _p(ab_all), _p(lev_p), _p(bvec),
                                            del_ne.shape[0], _p(del_ne, P_I), _p(del_num_ne, P_I), float(tx)))
-        self.N = N
+        self.N, self.bulk = N, bulk
 
     def set_populations(self, lev_p):
         self._check(lib().portal_set_populations(self._h, _p(_f64(lev_p))))
@@ -274,6 +277,25 @@ class Context:
                                        nvel, float(dvel), float(v0), im_pix, float(im_size), float(alpha), float(dx),
                                        n_depth_rt, *ptrs, _p(st, P_I)))
         return out, st
+
+    def image_nodes(self, l1, l2, th_inc, ph_az, nvel, dvel, v0, alpha=0.15, dx=float(np.float32(1e-4)),
+                    n_depth_rt=10000, pol_pops=None, quantities=4):
+        """Per-node maps of one inclination (pix_mod = 0).  Returns an (8,
+        nlines, nchan, n_bulk) float32 array (I, Q, U, tau, dust I, Q, U, tau;
+        the first `quantities` filled), the xy rows (n_bulk, 2) and the
+        per-node status."""
+        l1 = _i32(l1); l2 = _i32(l2)
+        nl, nch, nb = len(l1), 2 * nvel + 1, self.bulk
+        out = np.zeros((8, nl, nch, nb), dtype=np.float32)
+        xy = np.zeros((nb, 2))
+        st = np.zeros(nb, dtype=np.int32)
+        pp = None if pol_pops is None else np.ascontiguousarray(np.asarray(pol_pops, dtype=np.float64).T)
+        P_F = C.POINTER(C.c_float)
+        ptrs = [out[q].ctypes.data_as(P_F) if q < quantities else None for q in range(8)]
+        self._check(lib().portal_image_nodes(self._h, _p(pp), nl, _p(l1, P_I), _p(l2, P_I), float(th_inc),
+                                             float(ph_az), nvel, float(dvel), float(v0), float(alpha), float(dx),
+                                             n_depth_rt, _p(xy), *ptrs, _p(st, P_I)))
+        return out, xy, st
 
     def lambda_iterate(self, rc, tol=1e-6, max_iter=100, start_pops=None, fetch=True, ng_period=0,
                        local_operator=False):

@@ -1,6 +1,7 @@
 // finish_portal.x on GB300: the same command line, input file and outputs as
-// the reference program (para_finish.f90), pixel mode, with the pixel loops
-// (para_finish.f90:382-448) run by the library.
+// the reference program (para_finish.f90), with the pixel loops
+// (para_finish.f90:382-448) or the per-node loops (:287-320) run by the
+// library.
 //
 //   finish_portal.x <input_file> <output_map> <pop> <grid> <mol> <dust>
 //
@@ -9,6 +10,10 @@
 // centre-channel dust maps inc{j}-trans{i}-dust_{i,q,u,tau}.fits
 // (para_finish.f90:460-616), I, Q and U scaled by I_to_T = 3.255e39/nu0^2.
 // With fits = 0 the .dat maps of the same routine are written instead.
+// pix_mod = 0 (para_finish.f90:245-350): per inclination j the node positions
+// inc{j}-xy.dat, then per line i, inclination j and channel k the per-node
+// rows inc{j}-trans{i}-vel{k}-im.dat (I_to_T I, I_to_T Q, I_to_T U, tau); the
+// numbers in the names are written like Fortran's i2.2 ("**" above 99).
 // PORTAL_BVEC_FILE and PORTAL_DEVICE as for main_portal.x.
 #include <cmath>
 #include <cstdio>
@@ -26,6 +31,54 @@ static int fail(const std::string &m) {
     return 1;
 }
 
+// Fortran's i2.2 edit descriptor: two digits, "**" when the value needs more
+static std::string i2(int v) {
+    if (v < 0 || v > 99) return "**";
+    char b[4];
+    snprintf(b, sizeof b, "%02d", v);
+    return b;
+}
+
+// pix_mod = 0: para_finish.f90:245-350
+static int node_maps(portal_ctx *ctx, const FinishInput &in, const std::string &out, const Cloud &c,
+                     const std::vector<double> &pops, double nu0, double dx) {
+    const int nb = c.bulk_node_num, nch = 2 * in.nvel + 1, nl = in.nlevels;
+    const double I_to_T = 3.255e39 / (nu0 * nu0);  // :333
+    const size_t cube = (size_t)nb * nch * nl;
+    std::vector<float> q[4];
+    for (auto &v : q) v.assign(cube, 0.f);
+    std::vector<double> xy(2 * (size_t)nb), rows;
+    for (int j = 0; j < in.nincs; j++) {
+        const int r = portal_image_nodes(ctx, pops.data(), nl, in.l1.data(), in.l2.data(), in.th_inc[j], in.ph_az[j],
+                                         in.nvel, in.dvel, in.v0, 0.15, dx, in.n_depth_rt, xy.data(), q[0].data(),
+                                         q[1].data(), q[2].data(), q[3].data(), nullptr, nullptr, nullptr, nullptr,
+                                         nullptr);
+        if (r) return fail(std::string("portal_image_nodes: ") + portal_strerror(r) + " (" + portal_last_error(ctx) + ")");
+        rows.resize(2 * (size_t)nb);
+        for (int n = 0; n < nb; n++) {
+            rows[n] = xy[2 * (size_t)n];
+            rows[(size_t)nb + n] = xy[2 * (size_t)n + 1];
+        }
+        std::string name = out + "/inc" + i2(j + 1) + "-xy.dat";
+        if (!write_rows(name, rows, nb, 2)) return fail("cannot write " + name);
+        rows.resize(4 * (size_t)nb);
+        for (int i = 0; i < nl; i++)
+            for (int k = 0; k < nch; k++) {
+                const size_t base = (size_t)nb * ((size_t)k + (size_t)nch * i);
+                for (int n = 0; n < nb; n++) {
+                    rows[n] = I_to_T * (double)q[0][base + n];
+                    rows[(size_t)nb + n] = I_to_T * (double)q[1][base + n];
+                    rows[2 * (size_t)nb + n] = I_to_T * (double)q[2][base + n];
+                    rows[3 * (size_t)nb + n] = (double)q[3][base + n];
+                }
+                name = out + "/inc" + i2(j + 1) + "-trans" + i2(i + 1) + "-vel" + i2(k + 1) + "-im.dat";
+                if (!write_rows(name, rows, nb, 4)) return fail("cannot write " + name);
+            }
+    }
+    printf("finish_portal: %d inclinations, %d lines, %d nodes, %d channels\n", in.nincs, nl, nb, nch);
+    return 0;
+}
+
 int main(int argc, char **argv) {
     if (argc < 7)
         return fail("usage: finish_portal.x <input_file> <output_map> <pop> <grid> <mol> <dust>");
@@ -35,7 +88,6 @@ int main(int argc, char **argv) {
     FinishInput in;
     if (!read_finish_input(input, in, err)) return fail(err);
     if (in.star_mod == 1) return fail("star mode (star_mod = 1) is not supported");
-    if (in.pix != 1) return fail("only the pixel mode (pix_mod = 1) is supported");
     Molecule m;
     Cloud c;
     if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err)) return fail(err);
@@ -71,15 +123,20 @@ int main(int argc, char **argv) {
                          bvec.data(), c.maxne, c.del_ne.data(), c.del_num_ne.data(), c.tx),
         "portal_set_cloud");
     const int npx = 2 * in.im_pix + 1, nch = 2 * in.nvel + 1, nl = in.nlevels;
+    // every line takes the frequency of the last (l1, l2) pair (para_finish.f90:173-175)
+    const double nu0 = m.e_levs[in.l2[nl - 1] - 1] - m.e_levs[in.l1[nl - 1] - 1];
+    const double dx = (double)1e-4f;  // para_finish.f90:201
+    if (in.pix == 0) {
+        const int r = node_maps(ctx, in, out, c, pops, nu0, dx);
+        portal_destroy(ctx);
+        return r;
+    }
     const size_t cube = (size_t)npx * npx * nch * nl;
     std::vector<float> q[8];
     for (auto &v : q) v.assign(cube, 0.f);
-    // every line takes the frequency of the last (l1, l2) pair (para_finish.f90:173-175)
-    const double nu0 = m.e_levs[in.l2[nl - 1] - 1] - m.e_levs[in.l1[nl - 1] - 1];
     const double I_to_T = 3.255e39 / (nu0 * nu0);
     const double pi = std::acos(-1.0);
     const double ang = -180.0 * std::asin(2.0 * in.im_size * c.tx / in.distance) / (pi * (in.im_pix * 2 + 1));
-    const double dx = (double)1e-4f;  // para_finish.f90:201
     for (int j = 0; j < in.nincs; j++) {
         chk(portal_image(ctx, pops.data(), nl, in.l1.data(), in.l2.data(), in.th_inc[j], in.ph_az[j], in.nvel,
                          in.dvel, in.v0, in.im_pix, in.im_size, 0.15, dx, in.n_depth_rt, q[0].data(), q[1].data(),

@@ -19,6 +19,11 @@
 //                            dipole_magfield, for clouds whose field those
 //                            models cannot express (e.g. a uniform field)
 //   PORTAL_DEVICE=n          CUDA device (default 0)
+//   PORTAL_LAMBDA="tol [n]"  iterate the node loop to convergence (largest
+//                            relative change of rho^0_0 per pass below tol,
+//                            at most n passes, accelerated) before the pass
+//                            whose results are written (no reference
+//                            counterpart: the reference makes one pass)
 //   PORTAL_DUMP_INGESTED=dir write the ingested arrays (what the library
 //                            receives) as .npy files into dir and stop
 //                            before any device work
@@ -132,6 +137,24 @@ int main(int argc, char **argv) {
         "portal_set_cloud");
     long long nseg = 0;
     const double dx = (double)1e-6f;  // main_para.f90:135
+    if (const char *li = getenv("PORTAL_LAMBDA")) {
+        // iterate the node loop to convergence first (accelerated: local
+        // operator + Ng every 4 passes); the pass below then starts from the
+        // converged populations, so its outputs are those of the fixed point
+        double tol = 1e-6;
+        int max_iter = 500;
+        if (sscanf(li, "%lf %d", &tol, &max_iter) < 1 || !(tol > 0.0) || max_iter < 1)
+            return fail("PORTAL_LAMBDA: \"tol [max_iter]\"");
+        int iters = 0;
+        long long ns = 0;
+        std::vector<double> res((size_t)max_iter);
+        chk(portal_lambda_iterate(ctx, in.nth, in.nph, in.nvel, g, dx, in.n_depth, in.kmax, tol, max_iter, 4, 1,
+                                  nullptr, nullptr, nullptr, &iters, res.data(), &ns),
+            "portal_lambda_iterate");
+        const double last = iters ? res[iters - 1] : 0.0;
+        printf("main_portal: Lambda iteration, %d passes, last change %.3e%s\n", iters, last,
+               last < tol ? "" : " (not converged)");
+    }
     chk(portal_radiation_field(ctx, in.nth, in.nph, in.nvel, g, dx, in.n_depth, nullptr, nullptr, nullptr, &nseg),
         "portal_radiation_field");
     const int N = c.node_num, nlev = m.nlev;

@@ -3,6 +3,7 @@
 #include "portal_io.h"
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -548,14 +549,47 @@ void gauge_vector(unsigned long long seed, double g[3]) {
     for (int k = 0; k < 3; k++) g[k] /= n;
 }
 
+// One value as printf's " %24.17E": std::to_chars in scientific notation
+// with 17 digits is correctly rounded like glibc's printf, so the digits are
+// the same; the exponent letter and inf / nan are upper-cased and the field
+// right-aligned to 24 characters.  Returns the characters written (<= 40).
+static size_t format_e17(char *p, double v) {
+    char b[40];
+    const auto r = std::to_chars(b, b + sizeof b, v, std::chars_format::scientific, 17);
+    const size_t n = (size_t)(r.ptr - b);
+    for (size_t i = 0; i < n; i++)
+        if (b[i] >= 'a' && b[i] <= 'z') b[i] = (char)(b[i] - 'a' + 'A');
+    const size_t pad = n < 24 ? 24 - n : 0;
+    p[0] = ' ';
+    memset(p + 1, ' ', pad);
+    memcpy(p + 1 + pad, b, n);
+    return 1 + pad + n;
+}
+
 bool write_rows(const std::string &path, const std::vector<double> &cm, int rows, int cols) {
     FILE *f = fopen(path.c_str(), "w");
     if (!f) return false;
-    for (int r = 0; r < rows; r++) {
-        for (int k = 0; k < cols; k++) fprintf(f, " %24.17E", cm[(size_t)r + (size_t)rows * k]);
-        fputc('\n', f);
-    }
-    return fclose(f) == 0;
+    // rows formatted by all host threads into per-thread buffers, written in order
+    const int nth = std::max(1, std::min(io_threads(), rows / 4096 + 1));
+    std::vector<std::string> buf((size_t)nth);
+    auto work = [&](int t) {
+        const int r0 = (int)((long long)rows * t / nth), r1 = (int)((long long)rows * (t + 1) / nth);
+        std::string &s = buf[(size_t)t];
+        s.resize((size_t)(r1 - r0) * ((size_t)cols * 40 + 1));
+        char *p = &s[0];
+        for (int r = r0; r < r1; r++) {
+            for (int k = 0; k < cols; k++) p += format_e17(p, cm[(size_t)r + (size_t)rows * k]);
+            *p++ = '\n';
+        }
+        s.resize((size_t)(p - &s[0]));
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+    bool ok = true;
+    for (const auto &s : buf) ok = ok && fwrite(s.data(), 1, s.size(), f) == s.size();
+    return (fclose(f) == 0) && ok;
 }
 
 bool read_rows(const std::string &path, std::vector<double> &cm, int rows, int cols, std::string &err) {

@@ -104,7 +104,9 @@ void magfield(const Cloud &c, double x1, double x2, double x3, double x_dip, std
 // a seeded generator
 void gauge_vector(unsigned long long seed, double g[3]);
 
-// pol_pops.dat: one line per node, 2*nlev values (main_para.f90:271-275)
+// pol_pops.dat: one line per node, 2*nlev values (main_para.f90:271-275),
+// each as printf's " %24.17E" (17 significant digits: read back, the same
+// doubles); formatted in parallel, byte-identical to the printf loop
 bool write_rows(const std::string &path, const std::vector<double> &colmajor, int rows, int cols);
 bool read_rows(const std::string &path, std::vector<double> &colmajor, int rows, int cols, std::string &err);
 

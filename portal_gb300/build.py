@@ -35,7 +35,8 @@ def _compile(src: str, verbose: bool) -> str:
     deps.append(os.path.join(ROOT, "include", "portal_gb300.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    # host code uncontracted like the oracle (aarch64 g++ fuses a*b+c by default)
+    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", path, "-o", obj]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]

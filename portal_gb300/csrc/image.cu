@@ -72,9 +72,11 @@ __global__ void k_im_nodes(ImNodeArgs a) {
     for (int j = 0; j < 3; j++) {
         double sx = 0.0, sv = 0.0, sb = 0.0;
         for (int k = 0; k < 3; k++) {
-            sv = sv + a.R[j + 3 * k] * a.vel[3 * (size_t)n + k];
-            sb = sb + a.R[j + 3 * k] * a.bvec[3 * (size_t)n + k];
-            sx = sx + a.R[j + 3 * k] * a.xyz[3 * (size_t)n + k];
+            // uncontracted, as the reference's sums (the per-node mode starts
+            // its rays at these positions)
+            sv = __dadd_rn(sv, __dmul_rn(a.R[j + 3 * k], a.vel[3 * (size_t)n + k]));
+            sb = __dadd_rn(sb, __dmul_rn(a.R[j + 3 * k], a.bvec[3 * (size_t)n + k]));
+            sx = __dadd_rn(sx, __dmul_rn(a.R[j + 3 * k], a.xyz[3 * (size_t)n + k]));
         }
         x[j] = sx; v[j] = sv; bb[j] = sb;
     }
@@ -132,7 +134,12 @@ __global__ void k_im_nodes(ImNodeArgs a) {
             // trace step: * tx dx (raytrace.f90:221, 239, 250-258)
             const double cnu = (double)2.99792e8f / L.nu0;
             const double f = cnu / spi_b * a.tdx;
-            o = make_float4((float)(nI * f), (float)(nQ * f), (float)(eI * f), (float)(eQ * f));
+            // eta_Q exactly 0 (no alignment, sin(theta) = 0, or a line whose
+            // w^(2) vanish) makes polarize_prop's eta_I/eta_Q * sinh(0) a NaN
+            // (raytrace.f90:41-53): carried as a NaN coefficient, so I, Q, U
+            // turn NaN wherever the reference's do, tau stays finite
+            o = make_float4((float)(nI * f), nQ == 0.0 ? __int_as_float(0x7fc00000) : (float)(nQ * f),
+                            (float)(eI * f), (float)(eQ * f));
         }
         a.coef[(size_t)j * N + n] = o;
     }
@@ -140,6 +147,7 @@ __global__ void k_im_nodes(ImNodeArgs a) {
 
 struct ImArgs {
     int N, npx, im_pix, nlines, nvel, nch, n_depth;
+    int mode, nrays;         // 0: pixel grid, nrays = npx^2; 1: one ray per bulk node
     double im_size, dx, tdx, alpha, dvel, v0;
     const double *xyz;       // rotated (3,N)
     const int *off, *idx;    // neighbour CSR
@@ -148,7 +156,7 @@ struct ImArgs {
     int2 *walk;              // per warp: 32 pixels x n_depth
     unsigned long long *counters;
     int *status;
-    float *out[8];           // (npx, npx, nch, nlines) each, or null
+    float *out[8];           // (npx, npx, nch, nlines) or (nrays, nch, nlines) each, or null
 };
 
 __device__ __forceinline__ float phi1(float x) {  // (1 - e^-x)/x, stable near 0
@@ -168,7 +176,7 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
     const int lane = threadIdx.x & 31;
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int2 *const wbase = a.walk + (size_t)gw * 32 * (size_t)a.n_depth;
-    const int npix = a.npx * a.npx;
+    const int npix = a.nrays;
     for (;;) {
         int p0 = 0;
         if (lane == 0) p0 = (int)atomicAdd(&a.counters[0], 32ULL);
@@ -178,8 +186,15 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
         const int p = p0 + lane;
         int nc = 0, st = 0;
         if (p < npix) {
-            const int ia = p / a.npx - a.im_pix, ib = p % a.npx - a.im_pix;
-            const double x = ia * a.im_size / a.im_pix, y = ib * a.im_size / a.im_pix;
+            double x, y;
+            if (a.mode == 1) {  // the node's rotated sky position (para_finish.f90:292)
+                x = a.xyz[3 * (size_t)p];
+                y = a.xyz[3 * (size_t)p + 1];
+            } else {
+                const int ia = p / a.npx - a.im_pix, ib = p % a.npx - a.im_pix;
+                x = ia * a.im_size / a.im_pix;
+                y = ib * a.im_size / a.im_pix;
+            }
             // the oracle's FP64 arithmetic, without FMA contraction, throughout the march
             const double z0 = -1.0 * __dsqrt_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(x, x)), __dmul_rn(y, y)));
             int2 *dl = wbase + (size_t)lane * a.n_depth;
@@ -317,6 +332,12 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                                 const float tk = tau[s] + yk;
                                 tauc[s] = (tk - tau[s]) - yk;
                                 tau[s] = tk;
+                            } else if (cv.z != cv.z) {
+                                // the reference rotates Q, U into the node frame and back at
+                                // every cell; a field along the line of sight has no frame
+                                // (NaN angle), which makes them NaN there too
+                                Q[s] = cv.z;
+                                U[s] = cv.z;
                             }
                         }
                     }
@@ -348,9 +369,14 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 for (int s = 0; s < NS; s++) {
                     const int ch = lane + 32 * s;
                     if (ch < a.nch) {
-                        const int ia = pix / a.npx, ib = pix % a.npx;
-                        const size_t o = (size_t)ia + (size_t)a.npx * ((size_t)ib + (size_t)a.npx *
-                                                                       ((size_t)ch + (size_t)a.nch * j));
+                        size_t o;
+                        if (a.mode == 1) {
+                            o = (size_t)pix + (size_t)a.nrays * ((size_t)ch + (size_t)a.nch * j);
+                        } else {
+                            const int ia = pix / a.npx, ib = pix % a.npx;
+                            o = (size_t)ia + (size_t)a.npx * ((size_t)ib + (size_t)a.npx *
+                                                              ((size_t)ch + (size_t)a.nch * j));
+                        }
                         const bool bad = (str != 0);
                         const float vals[8] = {bad ? NAN : (float)((double)I[s] - Ic), bad ? NAN : Q[s],
                                                bad ? NAN : U[s], bad ? NAN : tau[s],
@@ -369,30 +395,34 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
 
 }  // namespace
 
-extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, const int *l1,
-                            const int *l2, double th_inc, double ph_az, int nvel, double dvel,
-                            double v0, int im_pix, double im_size, double alpha, double dx,
-                            int n_depth_rt, float *I, float *Q, float *U, float *tau, float *dust_I,
-                            float *dust_Q, float *dust_U, float *dust_tau, int *status) {
-    if (!c) return PORTAL_ERR_ARG;
+// mode 0: the pixel grid (2 im_pix + 1)^2; mode 1: one ray per bulk node
+static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const int *l1, const int *l2,
+                      double th_inc, double ph_az, int nvel, double dvel, double v0, int mode, int im_pix,
+                      double im_size, double alpha, double dx, int n_depth_rt, double *xy, float *const *dout,
+                      int *status) {
+    const char *fn = mode ? "portal_image_nodes" : "portal_image";
     if (!c->have_cloud || !c->have_mol) return set_err(c, PORTAL_ERR_STATE, "no cloud or molecule");
     if (nlines < 1 || nlines > IM_MAX_LINES || !l1 || !l2 || nvel < 0 || 2 * nvel + 1 > 288 ||
         im_pix < 1 || !(im_size > 0.0) || !(dx > 0.0) || n_depth_rt < 1)
-        return set_err(c, PORTAL_ERR_ARG, "portal_image: bad arguments");
-    if (im_size * im_size * 2.0 >= 1.0)
+        return set_err(c, PORTAL_ERR_ARG, std::string(fn) + ": bad arguments");
+    if (mode == 0 && im_size * im_size * 2.0 >= 1.0)
         return set_err(c, PORTAL_ERR_ARG, "portal_image: im_size must keep the image corners inside "
                                           "the unit sphere (im_size < 1/sqrt(2))");
     if (!pol_pops && !c->pops.p)
-        return set_err(c, PORTAL_ERR_STATE, "portal_image: no pol_pops (pass them or run portal_solve_se)");
+        return set_err(c, PORTAL_ERR_STATE, std::string(fn) + ": no pol_pops (pass them or run portal_solve_se)");
     cudaSetDevice(c->device);
     timers_reset(c);
     const int N = c->N, nlev = c->nlev, nch = 2 * nvel + 1, npx = 2 * im_pix + 1;
+    const int nrays = mode ? c->bulk : npx * npx;
     // line data (para_finish.f90:173-185): every line takes the frequency of the
     // last (l1, l2) pair, as the whole-array assignment there does
     ImLine h[IM_MAX_LINES];
     for (int i = 0; i < nlines; i++) {
         if (l1[i] < 1 || l1[i] > nlev || l2[i] < 1 || l2[i] > nlev)
-            return set_err(c, PORTAL_ERR_ARG, "portal_image: line level out of range");
+            return set_err(c, PORTAL_ERR_ARG, std::string(fn) + ": line level out of range");
+        if (mode && l1[i] > c->r_num)
+            return set_err(c, PORTAL_ERR_ARG, "portal_image_nodes: t_Aji(l1) needs l1 <= the number of "
+                                              "radiative transitions");
     }
     const double nu_last = c->e_levs[l2[nlines - 1] - 1] - c->e_levs[l1[nlines - 1] - 1];
     for (int i = 0; i < nlines; i++) {
@@ -404,6 +434,7 @@ extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, c
                 L.A = c->A[r]; L.kd = c->kd_v[r];
                 break;
             }
+        if (mode) L.A = c->A[l1[i] - 1];  // para_finish.f90:303 passes t_Aji(l1(j))
         L.lo = l1[i] - 1; L.up = l2[i] - 1;
         L.j1 = c->j_lev[L.lo]; L.j2 = c->j_lev[L.up];
         L.w1 = wigner6j(2, 2, 4, 2 * L.j1, 2 * L.j1, 2 * L.j2);
@@ -438,10 +469,10 @@ extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, c
     DevBuf<float4> cellv, cellb, coef;
     DevBuf<float> outd;
     DevBuf<int> stat;
-    const size_t cube = (size_t)npx * npx * nch * nlines;
+    const size_t cube = (size_t)nrays * nch * nlines;
     if (xyz_r.reserve(3 * (size_t)N) || cellv.reserve(N) || cellb.reserve(N) ||
-        coef.reserve((size_t)nlines * N) || jl.reserve(nlev) || stat.reserve((size_t)npx * npx))
-        return set_err(c, PORTAL_ERR_NOMEM, "portal_image buffers");
+        coef.reserve((size_t)nlines * N) || jl.reserve(nlev) || stat.reserve((size_t)(nrays > 0 ? nrays : 1)))
+        return set_err(c, PORTAL_ERR_NOMEM, "image buffers");
     const double *pops_src = c->pops.p;
     if (pol_pops) {
         if (pops_d.reserve((size_t)N * 2 * nlev)) return set_err(c, PORTAL_ERR_NOMEM, "pol_pops");
@@ -459,12 +490,12 @@ extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, c
     timer_stop(c, T_EMCOEF);
     PCHECK(c, cudaGetLastError());
     // outputs on the device
-    float *dout[8] = {I, Q, U, tau, dust_I, dust_Q, dust_U, dust_tau};
     int nout = 0;
     for (int q = 0; q < 8; q++) nout += dout[q] ? 1 : 0;
     if (outd.reserve(cube * (nout ? nout : 1))) return set_err(c, PORTAL_ERR_NOMEM, "image outputs");
     ImArgs ia;
     ia.N = N; ia.npx = npx; ia.im_pix = im_pix; ia.nlines = nlines; ia.nvel = nvel; ia.nch = nch;
+    ia.mode = mode; ia.nrays = nrays;
     ia.n_depth = n_depth_rt; ia.im_size = im_size; ia.dx = dx; ia.tdx = c->tx * dx; ia.alpha = alpha; ia.dvel = dvel; ia.v0 = v0;
     ia.xyz = xyz_r.p; ia.off = c->nb_off.p; ia.idx = c->nb_idx.p; ia.cellv = cellv.p; ia.cellb = cellb.p;
     ia.coef = coef.p; ia.dust_p = c->dustp.p; ia.tdust = c->tdust.p; ia.status = stat.p;
@@ -490,14 +521,48 @@ extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, c
     for (int q = 0; q < 8; q++)
         if (dout[q])
             PCHECK(c, cudaMemcpyAsync(dout[q], ia.out[q], cube * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    std::vector<int> sth((size_t)npx * npx);
+    std::vector<int> sth((size_t)nrays);
+    std::vector<double> xyz_h;
+    if (xy) {
+        xyz_h.resize(3 * (size_t)N);
+        PCHECK(c, cudaMemcpyAsync(xyz_h.data(), xyz_r.p, xyz_h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+    }
     PCHECK(c, cudaMemcpyAsync(sth.data(), stat.p, sth.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
     timer_collect(c, T_EMCOEF);
     timer_collect(c, T_IMWALK);
     if (status) std::copy(sth.begin(), sth.end(), status);
+    if (xy)  // the rows of inc%02d-xy.dat (para_finish.f90:269-271)
+        for (int n = 0; n < nrays; n++) {
+            xy[2 * (size_t)n] = c->tx * xyz_h[3 * (size_t)n];
+            xy[2 * (size_t)n + 1] = c->tx * xyz_h[3 * (size_t)n + 1];
+        }
     for (size_t i = 0; i < sth.size(); i++)
         if (sth[i] == 1)
-            return set_err(c, PORTAL_ERR_DEPTH, "node_count > n_depth_rt for pixel " + std::to_string(i + 1));
+            return set_err(c, PORTAL_ERR_DEPTH, std::string("node_count > n_depth_rt for ") +
+                                                    (mode ? "node " : "pixel ") + std::to_string(i + 1));
     return PORTAL_OK;
+}
+
+extern "C" int portal_image(portal_ctx *c, const double *pol_pops, int nlines, const int *l1,
+                            const int *l2, double th_inc, double ph_az, int nvel, double dvel,
+                            double v0, int im_pix, double im_size, double alpha, double dx,
+                            int n_depth_rt, float *I, float *Q, float *U, float *tau, float *dust_I,
+                            float *dust_Q, float *dust_U, float *dust_tau, int *status) {
+    if (!c) return PORTAL_ERR_ARG;
+    float *const out[8] = {I, Q, U, tau, dust_I, dust_Q, dust_U, dust_tau};
+    return image_call(c, pol_pops, nlines, l1, l2, th_inc, ph_az, nvel, dvel, v0, 0, im_pix, im_size, alpha, dx,
+                      n_depth_rt, nullptr, out, status);
+}
+
+extern "C" int portal_image_nodes(portal_ctx *c, const double *pol_pops, int nlines, const int *l1,
+                                  const int *l2, double th_inc, double ph_az, int nvel, double dvel,
+                                  double v0, double alpha, double dx, int n_depth_rt, double *xy, float *I,
+                                  float *Q, float *U, float *tau, float *dust_I, float *dust_Q, float *dust_U,
+                                  float *dust_tau, int *status) {
+    if (!c) return PORTAL_ERR_ARG;
+    float *const out[8] = {I, Q, U, tau, dust_I, dust_Q, dust_U, dust_tau};
+    return image_call(c, pol_pops, nlines, l1, l2, th_inc, ph_az, nvel, dvel, v0, 1, 1, 0.5, alpha, dx,
+                      n_depth_rt, xy, out, status);
 }

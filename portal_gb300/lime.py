@@ -84,7 +84,7 @@ def write_main_input(path, rc, kmax=None, extra_info=0, max_ne_temp=10000, dust_
 
 def write_finish_input(path, l1, l2, th_inc, ph_az, nvel, dvel, v0, im_pix, im_size, kmax=6, fits=1,
                        distance=3.086e16, max_ne_temp=10000, n_depth_rt=10000, dust_ii_gas=0.01,
-                       field=(0, 1, 0, "1.d0")):
+                       field=(0, 1, 0, "1.d0"), pix_mod=1):
     """The input file of finish_portal.x as run_portal.sh:133-152 writes it."""
     with open(path, "w") as f:
         f.write("\n%d\n%s\n%s\n\n" % (len(l1), " ".join(map(str, l1)), " ".join(map(str, l2))))
@@ -92,8 +92,8 @@ def write_finish_input(path, l1, l2, th_inc, ph_az, nvel, dvel, v0, im_pix, im_s
         f.write("%d %s %s\n\n" % (nvel, _g(dvel), _g(v0)))
         f.write("0 2.5E3 2.99196E11 0.d0 0.d0 0.d0\n%s\n" % dust_ii_gas)
         f.write("%s %s %s %s\n" % field)
-        f.write("%d 0\n1 %d %s\n%d %s\n%d %d\n\n" % (kmax, im_pix, _g(im_size), fits, _g(distance), max_ne_temp,
-                                                   n_depth_rt))
+        f.write("%d 0\n%d %d %s\n%d %s\n%d %d\n\n" % (kmax, pix_mod, im_pix, _g(im_size), fits, _g(distance),
+                                                   max_ne_temp, n_depth_rt))
 
 
 def write_case(directory, cloud, mol, dust_table=None):

@@ -139,6 +139,115 @@ def test_main_and_finish_portal_end_to_end(case):
     assert ddust.shape == (1, 25, 25)
 
 
+@pytest.mark.gpu
+def test_main_portal_lambda_mode(case):
+    """PORTAL_LAMBDA="tol n": main_portal.x iterates the node loop to
+    convergence (accelerated) before its pass; pol_pops.dat equals the same
+    library calls."""
+    import portal_gb300 as pg
+    d, cloud, mol, rc = case["d"], case["cloud"], case["mol"], case["rc"]
+    env = dict(PORTAL_BVEC_FILE=case["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec),
+               PORTAL_LAMBDA="1e-6 300")
+    r = _run(MAIN, case, env)
+    assert r.returncode == 0, r.stderr
+    assert "Lambda iteration" in r.stdout
+    pops_file = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        _, _, n, res, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=300, fetch=False, ng_period=4,
+                                             local_operator=True)
+        assert n < 300 and res[-1] < 1e-6
+        assert f"{n} passes" in r.stdout
+        ctx.radiation_field(rc, fetch=False)
+        pops, _, _, _ = ctx.solve_se(rc.kmax, jj20=True, rates=True)
+    np.testing.assert_allclose(pops_file, pops, rtol=1e-15, atol=0)
+    r = _run(MAIN, case, dict(env, PORTAL_LAMBDA="-1"))
+    assert r.returncode != 0 and "PORTAL_LAMBDA" in r.stderr
+
+
+@pytest.mark.gpu
+def test_finish_portal_node_maps(case):
+    """pix_mod = 0: finish_portal.x writes inc01-xy.dat and one
+    inc01-trans01-vel{k}-im.dat per channel from the library's per-node
+    maps (I_to_T I, I_to_T Q, I_to_T U, tau per bulk node)."""
+    import portal_gb300 as pg
+    d, cloud, mol, rc = case["d"], case["cloud"], case["mol"], case["rc"]
+    env = dict(PORTAL_BVEC_FILE=case["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec))
+    r = _run(MAIN, case, env)
+    assert r.returncode == 0, r.stderr
+    pops_file = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    nvel = 3
+    lime.write_finish_input(os.path.join(d, "finish0.dat"), [1], [2], [0.5], [0.2], nvel, 100.0, 0.0, 12, 0.7,
+                            pix_mod=0)
+    r2 = _run(FINISH, case, env, input_name="finish0.dat")
+    assert r2.returncode == 0, r2.stderr
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        cube, xy, st = ctx.image_nodes([1], [2], 0.5, 0.2, nvel, 100.0, 0.0, pol_pops=pops_file)
+    assert not st.any()
+    np.testing.assert_allclose(np.loadtxt(os.path.join(d, "inc01-xy.dat")), xy, rtol=1e-15, atol=0)
+    nu0 = mol.e_levs[1] - mol.e_levs[0]
+    I_to_T = 3.255e39 / nu0 ** 2
+    for k in range(2 * nvel + 1):
+        rows = np.loadtxt(os.path.join(d, "inc01-trans01-vel%02d-im.dat" % (k + 1)))
+        want = np.stack([I_to_T * cube[0, 0, k].astype(np.float64), I_to_T * cube[1, 0, k].astype(np.float64),
+                         I_to_T * cube[2, 0, k].astype(np.float64), cube[3, 0, k].astype(np.float64)], axis=1)
+        np.testing.assert_allclose(rows, want, rtol=1e-15, atol=0)
+    assert not os.path.exists(os.path.join(d, "inc01-trans01-vel%02d-im.dat" % (2 * nvel + 2)))
+
+
+_ROW_WRITER_CHECK = r"""
+#include <cstdio>
+#include <vector>
+#include "portal_io.h"
+int main(int argc, char **argv) {
+    FILE *f = fopen(argv[1], "rb");
+    int rows, cols;
+    if (fread(&rows, 4, 1, f) != 1 || fread(&cols, 4, 1, f) != 1) return 2;
+    std::vector<double> v((size_t)rows * cols);
+    if (fread(v.data(), 8, v.size(), f) != v.size()) return 3;
+    fclose(f);
+    return portal_io::write_rows(argv[2], v, rows, cols) ? 0 : 1;
+}
+"""
+
+
+def test_row_writer_matches_printf(tmp_path):
+    """write_rows (the pol_pops.dat writer, parallel, std::to_chars) is byte
+    for byte the " %24.17E" printf loop: signed zeros, subnormals, the
+    largest and smallest doubles, inf and NaN included, with 1 and with 8
+    threads."""
+    import shutil
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    apps = os.path.join(ROOT, "portal_gb300", "apps")
+    src = tmp_path / "check.cpp"
+    src.write_text(_ROW_WRITER_CHECK)
+    exe = str(tmp_path / "check")
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-pthread", "-I", apps, str(src),
+                        os.path.join(apps, "portal_io.cpp"), "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    rng = np.random.default_rng(5)
+    rows, cols = 9001, 7
+    v = rng.normal(size=(rows, cols)) * 10.0 ** rng.integers(-300, 300, size=(rows, cols))
+    special = [0.0, -0.0, 5e-324, -2.2250738585072014e-308, 1.7976931348623157e308, np.inf, -np.inf, np.nan,
+               1.0, 0.1, 123456789.0, 9.999999999999999e22]
+    v.flat[:len(special)] = special
+    blob = tmp_path / "in.bin"
+    with open(blob, "wb") as f:
+        f.write(np.array([rows, cols], dtype=np.int32).tobytes())
+        f.write(np.asfortranarray(v).tobytes(order="F"))
+    want = "".join("".join(" %24.17E" % x for x in row) + "\n" for row in v)
+    for threads in ("1", "8"):
+        out = tmp_path / ("rows%s.dat" % threads)
+        r = subprocess.run([exe, str(blob), str(out)], env=dict(os.environ, PORTAL_THREADS=threads))
+        assert r.returncode == 0
+        assert out.read_text() == want
+
+
 def test_parallel_reader_matches_list_directed_forms(case, tmp_path):
     """The bulk readers' fast path (one plain record per line, many threads)
     and their list-directed fallback (records across lines, D exponents,

@@ -279,6 +279,89 @@ def test_image_against_oracle(ctx):
     assert np.abs(cube[4:]).max() == 0.0 and np.abs(o[4:]).max() == 0.0
 
 
+def _reversed_transitions(mol):
+    """The same molecule with its radiative transitions listed in reverse
+    order (a LAMDA file may list them in any order)."""
+    import dataclasses
+    return dataclasses.replace(mol, r_trans=mol.r_trans[::-1].copy(), A=mol.A[::-1].copy(),
+                               freq_ghz=mol.freq_ghz[::-1].copy(), nu=mol.nu[::-1].copy(),
+                               Bij=mol.Bij[::-1].copy(), kd_v=mol.kd_v[::-1].copy())
+
+
+def _stokes_close(cube, ocube_t, lines):
+    """I, Q, U, tau of (8, nl, nch, rays) against the oracle's, NaN where the
+    oracle's are NaN; tolerances of the pixel-mode test."""
+    for j in lines:
+        I, Q, U, tau = (cube[q, j] for q in range(4))
+        oI, oQ, oU, otau = (ocube_t[q, j] for q in range(4))
+        for a, b in ((I, oI), (Q, oQ), (U, oU), (tau, otau)):
+            np.testing.assert_array_equal(np.isnan(a), np.isnan(b))
+        assert np.abs(tau - otau).max() < 1e-4 * np.abs(otau).max()
+        ok = ~np.isnan(oI)
+        if not ok.any():
+            continue
+        Ipk = np.abs(oI[ok]).max()
+        assert Ipk > 0.0
+        assert np.abs(I - oI)[ok].max() < 1e-4 * Ipk, (j, np.abs(I - oI)[ok].max() / Ipk)
+        denom = np.maximum(np.abs(oI), 1e-3 * Ipk)[ok]
+        assert (np.abs(Q - oQ)[ok] / denom).max() < 1e-4
+        assert (np.abs(U - oU)[ok] / denom).max() < 1e-4
+
+
+def test_image_nodes_against_oracle(ctx):
+    """pix_mod = 0 (one ray per bulk node from its rotated sky position)
+    against the oracle's per-node loop on the same pol_pops.  The molecule
+    lists its transitions in reverse, so the per-node mode's t_Aji(l1) is
+    another transition's A than the pixel mode's matched one; the second
+    line (1, 3) has vanishing w^(2) on both levels, eta_Q = 0 and NaN I, Q,
+    U in both (polarize_prop divides 0 by 0).  The xy rows are equal to the
+    last bit; I, Q, U, tau within the pixel mode's tolerances."""
+    import oracle
+    cloud, mol, rc, im = _image_case(n=2048)
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc)
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2)
+    rmol = _reversed_transitions(mol)
+    Pr = oracle.OracleProblem(cloud, rmol)
+    ctx.set_molecule(rmol)
+    ctx.set_cloud(cloud)
+    l1, l2 = [1, 1], [2, 3]
+    cube, xy, st = ctx.image_nodes(l1, l2, 0.6, 0.3, im["nvel"], im["dvel"], im["v0"], pol_pops=opp)
+    ocube, oxy, ost, nf = Pr.image_nodes(l1, l2, opp, 0.6, 0.3, im["nvel"], im["dvel"], im["v0"])
+    assert nf == 0 and not st.any()
+    np.testing.assert_array_equal(xy, oxy)
+    o = ocube.transpose(0, 2, 3, 1)  # (8, nb, nl, nch) -> (8, nl, nch, nb)
+    assert not np.isnan(o[0, 0]).any() and np.isnan(o[0, 1]).all()
+    _stokes_close(cube, o, [0, 1])
+    # t_Aji(1) of the reversed list is the top transition's A, not A(1 -> 2)
+    with_matched = Pr.image(l1[:1], l2[:1], opp, 0.6, 0.3, im["nvel"], im["dvel"], im["v0"], 2, 0.5)[0]
+    assert rmol.A[0] != mol.A[0] and np.isfinite(with_matched).all()
+
+
+def test_image_face_on_field_is_nan_like_the_reference(ctx):
+    """A field along the line of sight (B along z, th_inc = 0): sin(theta) =
+    0 gives eta_Q = 0 and an undefined Stokes rotation, so the reference's I,
+    Q, U are NaN wherever a line cell is crossed; the GPU image has the same
+    NaN pattern and the same tau."""
+    import oracle
+    cloud, mol, rc, im = _image_case(n=2048, im_pix=6)
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc)
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2)
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    cube, st = ctx.image([1], [2], 0.0, 0.0, im["nvel"], im["dvel"], im["v0"], im["im_pix"], im["im_size"],
+                         pol_pops=opp)
+    ocube, ost, nf = P.image([1], [2], opp, 0.0, 0.0, im["nvel"], im["dvel"], im["v0"], im["im_pix"],
+                             im["im_size"])
+    npx, nch = 2 * im["im_pix"] + 1, 2 * im["nvel"] + 1
+    o = ocube.reshape(8, npx, npx, 1, nch).transpose(0, 3, 4, 2, 1)
+    assert np.isnan(o[0]).any()
+    for q in range(3):
+        np.testing.assert_array_equal(np.isnan(cube[q]), np.isnan(o[q]))
+    assert np.abs(cube[3] - o[3]).max() < 1e-4 * np.abs(o[3]).max()
+
+
 # ---- Lambda iteration -------------------------------------------------------
 
 def test_lambda_iteration_against_oracle(ctx):

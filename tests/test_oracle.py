@@ -180,3 +180,43 @@ def test_polarize_prop_against_rk4():
             y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
         np.testing.assert_allclose([I.value, Q.value], y, rtol=1e-9)
         assert abs(U.value - 0.2 * math.exp(-eI * ds)) < 1e-14
+
+
+def test_node_maps_start_points_and_einstein_a():
+    """The per-node mode (pix_mod = 0, para_finish.f90:245-350): the xy rows
+    are tx times the rotated positions R_z(ph_az) R_x(th_inc) X of the bulk
+    nodes; with the transitions listed in reverse, line (1, 2) radiates with
+    t_Aji(1) = the top transition's A (:303), so its intensities differ from
+    the same molecule listed in order; a line (1, 3), whose w^(2) vanish on
+    both levels, has eta_Q = 0 and NaN I, Q, U (polarize_prop's 0/0) but a
+    finite tau, while the pixel mode gives it A = 0 and zeros."""
+    import dataclasses
+    cloud, mol = _tiny_problem(512)
+    rmol = dataclasses.replace(mol, r_trans=mol.r_trans[::-1].copy(), A=mol.A[::-1].copy(),
+                               freq_ghz=mol.freq_ghz[::-1].copy(), nu=mol.nu[::-1].copy(),
+                               Bij=mol.Bij[::-1].copy(), kd_v=mol.kd_v[::-1].copy())
+    pp = np.zeros((cloud.node_num, 2 * mol.nlev))
+    g = np.sqrt(2.0 * mol.j_lev + 1.0)
+    pp[:, 0::2] = cloud.lev_p / cloud.lev_p.sum(axis=1, keepdims=True) / g
+    pp[:, 1::2] = 1e-3 * pp[:, 0::2]
+    th, ph = 0.6, 0.3
+    outs = {}
+    for name, m in (("ordered", mol), ("reversed", rmol)):
+        P = oracle.OracleProblem(cloud, m)
+        out, xy, st, nf = P.image_nodes([1, 1], [2, 3], pp, th, ph, 4, 80.0, 0.0, node_lo=0, node_hi=63)
+        assert nf == 0 and not st[:64].any()
+        outs[name] = out[:, :64]
+    ct, sn = math.cos(th), math.sin(th)
+    Rx = np.array([[1, 0, 0], [0, ct, -sn], [0, sn, ct]])
+    cp, sp = math.cos(ph), math.sin(ph)
+    Rz = np.array([[cp, -sp, 0], [sp, cp, 0], [0, 0, 1]])
+    X = cloud.xyz[:cloud.bulk_node_num] @ (Rz @ Rx).T
+    np.testing.assert_allclose(xy, cloud.tx * X[:, :2], rtol=0, atol=1e-14 * cloud.tx)
+    a, b = outs["ordered"][0, :, 0], outs["reversed"][0, :, 0]
+    assert np.isfinite(a).all() and np.isfinite(b).all()
+    assert np.abs(a - b).max() > 1e-3 * np.abs(a).max()
+    line13 = outs["reversed"][:, :, 1]
+    assert np.isnan(line13[:3]).all() and np.isfinite(line13[3]).all() and line13[3].max() > 0.0
+    P = oracle.OracleProblem(cloud, mol)
+    pix, _, _ = P.image([1, 1], [2, 3], pp, th, ph, 4, 80.0, 0.0, 2, 0.5)
+    assert np.abs(pix[0, :, 1]).max() == 0.0 and np.abs(pix[0, :, 0]).max() > 0.0

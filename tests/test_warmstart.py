@@ -10,9 +10,12 @@ from portal_gb300.warmstart import start_pops, targets
 
 
 def test_targets_and_start_pops_round_trip():
+    """Populations without inversion (x_J / (2J+1) decreasing) survive the
+    round trip through the targets."""
     rng = np.random.default_rng(0)
     j = np.arange(6)
-    x = rng.dirichlet(np.ones(6), size=50)
+    x = (2 * j + 1) * np.exp(-np.cumsum(rng.uniform(0.1, 2.0, size=(50, 6)), axis=1))
+    x /= x.sum(axis=1, keepdims=True)
     rho0 = x / np.sqrt(2 * j + 1)
     pp = np.zeros((50, 12))
     pp[:, 0::2] = rho0
@@ -22,6 +25,28 @@ def test_targets_and_start_pops_round_trip():
     np.testing.assert_allclose(back, pp, rtol=1e-5, atol=1e-12)
     # the normalisation sum sqrt(2J+1) rho^0_0 = 1 of the SE solution
     np.testing.assert_allclose((back[:, 0::2] * np.sqrt(2 * j + 1)).sum(1), 1.0, rtol=1e-12)
+
+
+def test_start_pops_are_never_masers_and_stay_in_the_training_range():
+    """A prediction with an inversion (x_J / (2J+1) rising with J) or far
+    outside the training targets gives a start with non-increasing
+    populations per statistical weight, inside the targets' range."""
+    j = np.arange(4)
+    g = 2.0 * j + 1.0
+    Y = np.array([[-1.0, -0.5, -0.2, -3.0, 0.1, 0.2, 0.3, 0.4],     # J = 1, 2 inverted over J = 0
+                  [-0.3, -0.6, 32.0, -2.0, 50.0, 0.0, 0.0, -50.0]])  # far outside the training range
+    lo = np.array([-14.0, -14.0, -14.0, -14.0, -5.0, -5.0, -5.0, -5.0])
+    hi = np.array([-0.2, -0.3, -0.5, -1.0, 5.0, 5.0, 5.0, 5.0])
+    pp = start_pops(Y, j, (lo, hi))
+    x = pp[:, 0::2] * np.sqrt(g)
+    np.testing.assert_allclose(x.sum(axis=1), 1.0, rtol=1e-12)
+    per = x / g
+    assert np.all(np.diff(per, axis=1) <= 1e-15 * per[:, :-1])
+    ratio = 100.0 * pp[:, 1::2] / pp[:, 0::2]
+    assert np.all(ratio >= lo[4:] - 1e-9) and np.all(ratio <= hi[4:] + 1e-9)
+    # without a range the inversion rule alone still applies
+    per0 = start_pops(Y[:1], j)[:, 0::2] * np.sqrt(g) / g
+    assert np.all(np.diff(per0, axis=1) <= 1e-15 * per0[:, :-1])
 
 
 @pytest.mark.gpu
