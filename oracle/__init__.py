@@ -25,7 +25,8 @@ class OrcCloud(C.Structure):
                 ("maxne", C.c_int), ("xyz", P_D), ("vel", P_D), ("b_all", P_D), ("t_kin", P_D),
                 ("t_dust", P_D), ("dust_p", P_D), ("h2_dens", P_D), ("ab_all", P_D),
                 ("lev_p", P_D), ("bvec", P_D), ("del_ne", P_I), ("del_num_ne", P_I),
-                ("tx", C.c_double)]
+                ("tx", C.c_double), ("star_mod", C.c_int), ("T_star", C.c_double), ("R_star", C.c_double),
+                ("X_star", C.c_double * 3)]
 
 
 class OrcMolecule(C.Structure):
@@ -72,7 +73,9 @@ class OracleProblem:
     """Holds the reference-layout arrays of one cloud + molecule so that the
     C structs' pointers stay valid."""
 
-    def __init__(self, cloud, mol):
+    def __init__(self, cloud, mol, star=None):
+        """star: None, or (T_star [K], R_star [m], (x, y, z) as the input file
+        gives them) for star_mod = 1."""
         self.cloud, self.mol = cloud, mol
         N = cloud.node_num
         self.xyz = np.ascontiguousarray(cloud.xyz, dtype=np.float64)          # (N,3) == X(3,N)
@@ -92,6 +95,13 @@ class OracleProblem:
                           _p(self.vel), _p(self.b_all), _p(self.t_kin), _p(self.t_dust),
                           _p(self.dust_p), _p(self.h2), _p(self.ab), _p(self.lev_p), _p(self.bvec),
                           _p(self.del_ne, P_I), _p(self.del_num_ne, P_I), float(cloud.tx))
+        if star is not None:
+            T_s, R_s, X_s = star
+            self.c.star_mod = 1
+            self.c.T_star = float(T_s)
+            self.c.R_star = float(R_s) / float(cloud.tx)   # main_para.f90:122
+            for k in range(3):
+                self.c.X_star[k] = float(X_s[k])
         self.j_lev = np.ascontiguousarray(mol.j_lev, dtype=np.int32)
         self.e_levs = np.ascontiguousarray(mol.e_levs, dtype=np.float64)
         self.r_trans = np.ascontiguousarray(mol.r_trans, dtype=np.int32)      # (r,2) == r_trans(2,r)
@@ -198,6 +208,16 @@ class OracleProblem:
                                       C.c_double(v0), C.c_double(alpha), n_depth_rt, node_lo, node_hi, nthreads,
                                       _p(xy), _p(out), _p(st, P_I))
         return out, xy, st, nfail
+
+
+def star_all(nth, nph, kvec, gvec, bvec, dOm):
+    """The star-mode ray set of one node: (xth (n, 3) = cos th, ph, weight
+    relative to bvec; n_star), or None where the reference stops."""
+    xth = np.zeros((nth * nph, 3))
+    ns = C.c_int(0)
+    k, g, b = (np.ascontiguousarray(v, dtype=np.float64) for v in (kvec, gvec, bvec))
+    n = lib().orc_star_all(nth, nph, _p(k), _p(g), _p(b), C.c_double(dOm), C.byref(ns), _p(xth))
+    return None if n < 0 else (xth[:n].copy(), ns.value)
 
 
 def legendre_all(nth, nph):

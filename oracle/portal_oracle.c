@@ -237,6 +237,96 @@ static double norm2_3(const double *v)
     return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
 }
 
+/* find_angles miscellaneous.f90:86-145: (th, ph) of dir in the frame of
+ * find_dir (z = bvec, x = bvec x gvec normalised) */
+static void find_angles(const double *b, const double *g, const double *dir, double *th, double *ph)
+{
+    double xv[3] = {b[1] * g[2] - b[2] * g[1], b[2] * g[0] - b[0] * g[2], b[0] * g[1] - b[1] * g[0]};
+    double xn = sqrt(xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2]);
+    for (int k = 0; k < 3; k++) xv[k] = xv[k] / xn;
+    double bd = b[0] * dir[0] + b[1] * dir[1] + b[2] * dir[2];
+    if (bd > 1.0) *th = acos(1.0);
+    else if (bd < -1.0) *th = acos(-1.0);
+    else *th = acos(bd);
+    double cbd[3] = {b[1] * dir[2] - b[2] * dir[1], b[2] * dir[0] - b[0] * dir[2], b[0] * dir[1] - b[1] * dir[0]};
+    *ph = atan2(xv[0] * dir[0] + xv[1] * dir[1] + xv[2] * dir[2], xv[0] * cbd[0] + xv[1] * cbd[1] + xv[2] * cbd[2]);
+}
+
+/* circle_points miscellaneous.f90:1219-1265: n points on the star's cap of
+ * half-angle th_s, x(3,n) = (cos th, ph, weight).  One point keeps the
+ * reference's x(1:2,1) = cos(1): polar angle 1 rad, azimuth cos(1). */
+static void circle_points(int n, double th_s, double dth_s, double *x)
+{
+    const double pi = acos(-1.0);
+    if (n == 1) {
+        x[0] = cos(1.0);
+        x[1] = cos(1.0);
+        x[2] = 2.0 * pi * dth_s;
+    } else if (n < 10) {
+        double wph = 2.0 * pi / n, ww = wph * dth_s, xx = cos(th_s / 2.0);
+        for (int i = 1; i <= n; i++) {
+            x[3 * (i - 1)] = xx;
+            x[3 * (i - 1) + 1] = (i - 1) * wph;
+            x[3 * (i - 1) + 2] = ww;
+        }
+    } else {  /* Vogel's spiral, golden angle */
+        double ga = pi * (3.0 - sqrt(5.0)), ww = dth_s * 2.0 * pi / n;
+        for (int i = 1; i <= n; i++) {
+            x[3 * (i - 1)] = cos(th_s * sqrt(1.0 * i / n));
+            x[3 * (i - 1) + 1] = i * ga;
+            x[3 * (i - 1) + 2] = ww;
+        }
+    }
+}
+
+int orc_star_all(int nth, int nph, const double *kvec, const double *gvec, const double *bvec,
+                 double dOm_star, int *n_star_out, double *xth)
+{
+    const double pi = acos(-1.0);
+    double dth_star = dOm_star / (2.0 * pi);
+    double th_star = acos(1 - dth_star);
+    double dOm_max = 4.0 * pi / (nth * nph);
+    int n_star = (int)ceil(dOm_star / dOm_max);
+    if (n_star > nth * nph) return -1;
+    circle_points(n_star, th_star, dth_star, xth);
+    for (int i = 0; i < n_star; i++) xth[3 * i + 2] = xth[3 * i + 2] / (4.0 * pi);
+    int n_sphere = n_star;
+    double dth_rest = (pi - th_star) / nth;
+    double th_i = th_star + dth_rest / 2.0;
+    for (int i = 1; i <= nth; i++) {
+        double th = (i - 1) * dth_rest + th_i, wth;
+        if (i == 1) {
+            double th_u = (i - 0.5) * dth_rest + th_i;
+            wth = cos(th_star) - cos(th_u);
+        } else if (i == nth) {
+            double th_l = (i - 1.5) * dth_rest + th_i;
+            wth = cos(th_l) + 1.0;
+        } else {
+            double th_u = (i - 0.5) * dth_rest + th_i;
+            double th_l = (i - 1.5) * dth_rest + th_i;
+            wth = cos(th_l) - cos(th_u);
+        }
+        int np = (int)ceil(nph * sin(th));
+        double wph = 2.0 * pi / np, xx = cos(th);
+        for (int j = 1; j <= np; j++) {
+            n_sphere++;
+            if (n_sphere > nph * nth) return -1;
+            xth[3 * (n_sphere - 1)] = xx;
+            xth[3 * (n_sphere - 1) + 1] = (j - 1) * wph;
+            xth[3 * (n_sphere - 1) + 2] = wth * wph / (4.0 * pi);
+        }
+    }
+    for (int i = 0; i < n_sphere; i++) {
+        double dir[3], th, ph;
+        orc_find_dir(kvec, gvec, acos(xth[3 * i]), xth[3 * i + 1], dir);
+        find_angles(bvec, gvec, dir, &th, &ph);
+        xth[3 * i] = cos(th);
+        xth[3 * i + 1] = ph;
+    }
+    *n_star_out = n_star;
+    return n_sphere;
+}
+
 /* ------------------------------------------------------------------------ */
 /* radiation field                                                           */
 /* ------------------------------------------------------------------------ */
@@ -256,9 +346,11 @@ static int pos_quadratic(double a, double b, double c, double *x1)
     return 1;
 }
 
-/* check_neigh_fast miscellaneous.f90:1017-1076 (star_mode = 0) */
+/* check_neigh_fast miscellaneous.f90:1017-1076; star != 0 for a ray aimed
+ * at the star (trace_out's mode 1): the star's surface ends the step and
+ * the ray when it comes first */
 static void check_neigh_fast(const orc_cloud *c, double *X_phot, const double *dir, int node,
-                             double *delta_x, int *next)
+                             int star, double *delta_x, int *next)
 {
     const double *X_node = c->xyz + 3 * (node - 1);
     double nd = norm2_3(dir);
@@ -284,6 +376,16 @@ static void check_neigh_fast(const orc_cloud *c, double *X_phot, const double *d
         *delta_x = new_x;
         *next = nb;
     }
+    if (star) {
+        double ds[3] = {X_phot[0] - c->X_star[0], X_phot[1] - c->X_star[1], X_phot[2] - c->X_star[2]};
+        double nds = norm2_3(ds), sx = 0.0;
+        if (pos_quadratic(nd * nd, 2.0 * (ds[0] * dir[0] + ds[1] * dir[1] + ds[2] * dir[2]),
+                          nds * nds - c->R_star * c->R_star, &sx) == 0 &&
+            sx < *delta_x && sx > 0.0) {
+            *delta_x = sx;
+            *next = 0;
+        }
+    }
     for (int k = 0; k < 3; k++) X_phot[k] = X_phot[k] + *delta_x * dir[k];
 }
 
@@ -291,8 +393,17 @@ static void check_neigh_fast(const orc_cloud *c, double *X_phot, const double *d
  * column k = (cell id, cumulative steps).  Unlike the reference (which
  * writes past n_depth before it stops), the walk stops writing at n_depth
  * and returns ORC_ERR_DEPTH. */
+static int trace_out(const orc_cloud *c, int node, const double *dir, double dx, int n_depth,
+                     int star, int *depth_list, int *node_count);
+
 int orc_trace_out(const orc_cloud *c, int node, const double *dir, double dx, int n_depth,
                   int *depth_list, int *node_count)
+{
+    return trace_out(c, node, dir, dx, n_depth, 0, depth_list, node_count);
+}
+
+static int trace_out(const orc_cloud *c, int node, const double *dir, double dx, int n_depth,
+                     int star, int *depth_list, int *node_count)
 {
     double X_phot[3];
     int cur = node, nc = 0;
@@ -301,7 +412,7 @@ int orc_trace_out(const orc_cloud *c, int node, const double *dir, double dx, in
     depth_list[0] = node;
     for (;;) {
         int next;
-        check_neigh_fast(c, X_phot, dir, cur, &delta_x, &next);
+        check_neigh_fast(c, X_phot, dir, cur, star, &delta_x, &next);
         nc++;
         if (nc > n_depth) { *node_count = nc; return ORC_ERR_DEPTH; }
         depth_list[2 * (nc - 1) + 1] = (int)lround(delta_x / dx);  /* nint */
@@ -387,10 +498,11 @@ static double ray_in(const orc_cloud *c, const int *depth_list, int node_count, 
     return I_tot;
 }
 
-/* inverse_rt inverse_rt.f90:1-137 (star_mode = 0).  dx here is the
- * trace step (main_para.f90:135); ray_in receives tx*dx. */
+/* inverse_rt inverse_rt.f90:1-137.  dx here is the trace step
+ * (main_para.f90:135); ray_in receives tx*dx.  The first n_star rays are
+ * star rays (star mode): traced in mode 1 and started from B(T_star). */
 static int inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const double *xth,
-                      int n_sphere, const double *gvec, int nvel, double dx, int n_depth,
+                      int n_sphere, int n_star, const double *gvec, int nvel, double dx, int n_depth,
                       double *J0, double *J2, double *JE, double *LS, int64_t *n_segments)
 {
     int t_num = m->r_num;
@@ -409,7 +521,8 @@ static int inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const
         double dir[3];
         orc_find_dir(bvec, gvec, acos(mu), ph, dir);
         int node_count;
-        st = orc_trace_out(c, node, dir, dx, n_depth, depth_list, &node_count);
+        const int star_ray = (c->star_mod == 1 && i < n_star);
+        st = trace_out(c, node, dir, dx, n_depth, star_ray, depth_list, &node_count);
         if (st != ORC_OK) break;
         nseg += node_count;
         double vel_node = vn[0] * dir[0] + vn[1] * dir[1] + vn[2] * dir[2];
@@ -420,7 +533,7 @@ static int inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const
         for (int k = 0; k < t_num; k++) {
             double nu0 = m->nu[k];
             int l1 = m->r_trans[2 * k], l2 = m->r_trans[2 * k + 1];
-            double I_in = orc_black_body(2.73, nu0);
+            double I_in = star_ray ? orc_black_body(c->T_star, nu0) : orc_black_body(2.73, nu0);
             double Ie = 0.0, lam = 0.0;
             double I_out = ray_in(c, depth_list, node_count, node, vel_node, vel_ray, l1, l2,
                                   m->kd_v[k], nvel, c->tx * dx, nu0, m->A[k], m->Bij[k],
@@ -444,12 +557,19 @@ int orc_inverse_rt(const orc_cloud *c, const orc_molecule *m, int node, const do
                    int n_sphere, const double *gvec, int nvel, double dx, int n_depth,
                    double *J0, double *J2, int64_t *n_segments)
 {
-    return inverse_rt(c, m, node, xth, n_sphere, gvec, nvel, dx, n_depth, J0, J2, NULL, NULL,
+    return inverse_rt(c, m, node, xth, n_sphere, 0, gvec, nvel, dx, n_depth, J0, J2, NULL, NULL,
                       n_segments);
 }
 
-/* The node loop main_para.f90:210-257 (star_mod = 0 branch), radiation
- * field half of trace_node (main_sub.f90:82-84). */
+/* Star mode: is the node inside the star, which the node loop skips
+ * (main_para.f90:232 compares |X| with R_star, the star taken as centred) */
+static int inside_star(const orc_cloud *c, int node)
+{
+    return c->star_mod == 1 && !(norm2_3(c->xyz + 3 * (node - 1)) > c->R_star);
+}
+
+/* The node loop main_para.f90:210-257, radiation field half of trace_node
+ * (main_sub.f90:56-85; star mode: the node's own ray set from star_all). */
 int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth, int nph,
                               int nvel, const double *gvec, double dx, int n_depth, int node_lo,
                               int node_hi, int nthreads, double *J0, double *J2, double *JE,
@@ -473,8 +593,25 @@ int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth
         double *ls = JE ? LS + (size_t)t_num * (node - 1) : NULL;
         int st = ORC_OK;
         int64_t ns = 0;
-        if (c->ab_all[node - 1] > 0.0) {
-            st = inverse_rt(c, m, node, xth, n_sphere, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
+        if (c->ab_all[node - 1] > 0.0 && c->star_mod == 1 && !inside_star(c, node)) {
+            const double *X = c->xyz + 3 * (node - 1);
+            double kv[3] = {c->X_star[0] - X[0], c->X_star[1] - X[1], c->X_star[2] - X[2]};
+            double d = norm2_3(kv);
+            double q = c->R_star / d;
+            double dOm = acos(-1.0) * (q * q);
+            for (int k = 0; k < 3; k++) kv[k] = kv[k] / d;
+            double *xs = (double *)malloc(sizeof(double) * 3 * (size_t)nth * nph);
+            int n_star = 0;
+            int n_var = orc_star_all(nth, nph, kv, gvec, c->bvec + 3 * (node - 1), dOm, &n_star, xs);
+            if (n_var < 0) {
+                st = ORC_ERR_ARG;
+                for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
+            } else {
+                st = inverse_rt(c, m, node, xs, n_var, n_star, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
+            }
+            free(xs);
+        } else if (c->ab_all[node - 1] > 0.0 && c->star_mod != 1) {
+            st = inverse_rt(c, m, node, xth, n_sphere, 0, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
         } else {
             for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
             if (je)
@@ -1002,7 +1139,7 @@ int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const doub
 #pragma omp for schedule(static)
         for (int node = node_lo; node <= node_hi; node++) {
             int st = ORC_OK;
-            if (c->ab_all[node - 1] > 0.0) {
+            if (c->ab_all[node - 1] > 0.0 && !inside_star(c, node)) {
                 orc_make_AC(m, c->h2_dens[node - 1], c->t_kin[node - 1], n_trans, all_trans,
                             J0 + (size_t)m->r_num * (node - 1), J2 + (size_t)m->r_num * (node - 1),
                             AC);
@@ -1132,12 +1269,40 @@ static int check_neigh(const double *X_phot, int node, const double *xyz, const 
 
 /* trace_out_raytrace raytrace.f90:58-177 (star_mod = 0, dir = +z).
  * depth_list is (2, n_depth_rt) = (cell id, step index). */
+static int trace_out_raytrace(double x_co, double y_co, int node_num, const double *xyz,
+                              const int *del_ne, const int *del_num_ne, double dx, int n_depth_rt,
+                              int star_mod, double R_star, const double *XYZ_star, int *from_star,
+                              int *depth_list, int *node_count);
+
 int orc_trace_out_raytrace(double x_co, double y_co, int node_num, const double *xyz,
                            const int *del_ne, const int *del_num_ne, int maxne, double dx,
                            int n_depth_rt, int *depth_list, int *node_count)
 {
     (void)maxne;
+    int from_star = 0;
+    return trace_out_raytrace(x_co, y_co, node_num, xyz, del_ne, del_num_ne, dx, n_depth_rt, 0, 0.0, NULL,
+                              &from_star, depth_list, node_count);
+}
+
+/* trace_out_raytrace raytrace.f90:58-177.  Star mode (:103-115): a start
+ * point within R_star of the star's sky position starts at the star's
+ * front, z = z_star + R_star, and *from_star tells the caller to start
+ * from B(T_star). */
+static int trace_out_raytrace(double x_co, double y_co, int node_num, const double *xyz,
+                              const int *del_ne, const int *del_num_ne, double dx, int n_depth_rt,
+                              int star_mod, double R_star, const double *XYZ_star, int *from_star,
+                              int *depth_list, int *node_count)
+{
     double z_co = -1.0 * sqrt(1.0 - x_co * x_co - y_co * y_co);
+    *from_star = 0;
+    if (star_mod == 1) {
+        double xc = x_co - XYZ_star[0], yc = y_co - XYZ_star[1];
+        double rc = sqrt(xc * xc + yc * yc);
+        if (rc < R_star) {
+            z_co = XYZ_star[2] + R_star;
+            *from_star = 1;
+        }
+    }
     double start[3] = {x_co, y_co, z_co};
     int k_cur = 0, nc = 0, node = 0;
     double rsave = 10.0;
@@ -1317,6 +1482,21 @@ static int image_impl(const orc_cloud *c, const orc_molecule *m, int nlines, con
     double *bvec_inc = (double *)malloc(sizeof(double) * 3 * (size_t)N);
     double *xyz_inc = (double *)malloc(sizeof(double) * 3 * (size_t)N);
     orc_rotate_all_save(N, th_inc, ph_az, c->vel, c->bvec, c->xyz, vel_inc, bvec_inc, xyz_inc);
+    /* the star's position rotated with the nodes (miscellaneous.f90:899-904) */
+    double star_inc[3] = {0.0, 0.0, 0.0};
+    if (c->star_mod == 1) {
+        double xv[3] = {1, 0, 0}, zv[3] = {0, 0, 1}, Rth[9], Rph[9], R[9];
+        rotmat(xv, th_inc, Rth);
+        rotmat(zv, ph_az, Rph);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double sm = 0.0;
+                for (int k = 0; k < 3; k++) sm += Rph[i + 3 * k] * Rth[k + 3 * j];
+                R[i + 3 * j] = sm;
+            }
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) star_inc[j] = star_inc[j] + R[j + 3 * k] * c->X_star[k];
+    }
     double *velz = (double *)malloc(sizeof(double) * (size_t)N);
     for (int n = 0; n < N; n++) velz[n] = vel_inc[3 * n + 2];
     double *pol_rayt = (double *)calloc((size_t)nlines * 4 * N, sizeof(double));
@@ -1360,13 +1540,13 @@ static int image_impl(const orc_cloud *c, const orc_molecule *m, int nlines, con
                 x = i * im_size / im_pix;
                 y = j * im_size / im_pix;
             }
-            int nc = 0;
-            int st = orc_trace_out_raytrace(x, y, N, xyz_inc, c->del_ne, c->del_num_ne, c->maxne,
-                                            dx, n_depth_rt, dl, &nc);
+            int nc = 0, from_star = 0;
+            int st = trace_out_raytrace(x, y, N, xyz_inc, c->del_ne, c->del_num_ne, dx, n_depth_rt,
+                                        c->star_mod, c->R_star, star_inc, &from_star, dl, &nc);
             if (status) status[p] = st;
             if (st != ORC_OK) { nfail++; continue; }
             for (int jl = 0; jl < nlines; jl++) {
-                double I_in = orc_black_body(2.73, nu0_all[jl]);
+                double I_in = orc_black_body(from_star ? c->T_star : 2.73, nu0_all[jl]);
                 for (int k = -nvel; k <= nvel; k++) {
                     double o[8];
                     orc_ray_in_raytrace(k * dvel + v0, nc, dl, pol_rayt, nlines, jl, c->b_all,

@@ -47,6 +47,12 @@ typedef struct {
     const int *del_ne;     /* (N,maxne) column-major, 1-based, 0 = unused      */
     const int *del_num_ne; /* (N)                                              */
     double tx;             /* r_max in metres                                  */
+    /* star mode (star_mod = 1, main_para.f90:75, :122, :216-246): 0 = off.
+     * R_star is R_star / tx; X_star is used as read, unscaled, as the
+     * reference does (only a centred star is meaningful there). */
+    int star_mod;
+    double T_star, R_star;
+    double X_star[3];
 } orc_cloud;
 
 /* Molecule after main_para.f90:119-120 (nu, e_levs in Hz) and
@@ -80,6 +86,15 @@ double orc_wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3);
 double orc_wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
 void   orc_find_dir(const double *bvec, const double *gvec, double th, double ph,
                     double *dir);
+
+/* star_all miscellaneous.f90:1139-1217 with circle_points :1219-1265: the
+ * ray set of a node outside the star -- n_star rays into the star's cone
+ * around kvec (the node-to-star direction) with solid angle dOm, then nth
+ * bands over the rest of the sphere -- as (cos th, ph, weight) relative to
+ * bvec (find_angles miscellaneous.f90:86-145).  xth holds nth*nph columns;
+ * returns the ray count, or -1 where the reference would run past them. */
+int orc_star_all(int nth, int nph, const double *kvec, const double *gvec, const double *bvec,
+                 double dOm_star, int *n_star, double *xth);
 
 /* ---- radiation field (main_portal.x hot loop, first half) ---- */
 int orc_trace_out(const orc_cloud *c, int node, const double *dir, double dx,
