@@ -49,8 +49,10 @@ enum {
     PORTAL_NODE_OK = 0,
     PORTAL_NODE_DEPTH = 1,     /* inverse_rt.f90:206-210 would have stopped        */
     PORTAL_NODE_SINGULAR = 2,  /* em_coefs.f90:170-178 would have stopped          */
-    PORTAL_NODE_REFINE = 4     /* FP32 LU + FP64 refinement did not converge; the
+    PORTAL_NODE_REFINE = 4,    /* FP32 LU + FP64 refinement did not converge; the
                                   node was solved by the FP64 LU instead           */
+    PORTAL_NODE_STAR = 8       /* star mode: star_all's rays exceed nth*nph
+                                  (miscellaneous.f90:1181-1184 would have stopped) */
 };
 
 const char *portal_strerror(int code);
@@ -107,7 +109,8 @@ int portal_set_populations(portal_ctx *ctx, const double *lev_p);
  *                             non-bulk nodes);
  *   status(N)                 PORTAL_NODE_* bits;
  *   n_segments                ray segments walked (sum of node_count).
- * Star mode (star_mod = 1) is not supported. */
+ * In star mode (portal_set_star) nodes inside the star are skipped too and
+ * every other node uses its own star_all ray set instead. */
 int portal_radiation_field(portal_ctx *ctx, int nth, int nph, int nvel, const double *gvec,
                            double dx, int n_depth, double *J0, double *J2, int *status,
                            long long *n_segments);
@@ -171,7 +174,7 @@ int portal_lambda_iterate(portal_ctx *ctx, int nth, int nph, int nvel, const dou
  * the population read-back (para_finish.f90:222-240), comp_emcoefs
  * (em_coefs.f90:1-113) per bulk node and line, trace_out_raytrace
  * (raytrace.f90:58-177) per pixel and ray_in_raytrace (:179-323) per pixel,
- * line and channel.  star_mod = 0 only.
+ * line and channel; star mode as set by portal_set_star.
  *   pol_pops(N, 2*nlev) as main_portal.x wrote it, or NULL for the
  *   device-resident result of portal_solve_se;
  *   lines l1(nlines), l2(nlines) 1-based levels (at most 16 lines; as in
@@ -190,6 +193,29 @@ int portal_image(portal_ctx *ctx, const double *pol_pops, int nlines, const int 
                  double im_size, double alpha, double dx, int n_depth_rt, float *I, float *Q,
                  float *U, float *tau, float *dust_I, float *dust_Q, float *dust_U,
                  float *dust_tau, int *status);
+
+/* Star mode (star_mod = 1 of both input files; main_para.f90:75,
+ * para_finish.f90:116).  R_star in metres as the input file gives it
+ * (divided by the cloud's r_max here, main_para.f90:122); X_star(3) as given
+ * -- the reference uses it without scaling, so only a centred star
+ * (X_star = 0) is meaningful there and here alike.  star_mod = 0 turns it
+ * off.  While on:
+ *   - the node loop skips nodes with |X| <= R_star (main_para.f90:232): zero
+ *     J and populations;
+ *   - every other node integrates over its own ray set from star_all
+ *     (miscellaneous.f90:1139-1217; main_sub.f90:56-79): ceil(dOm / (4 pi /
+ *     (nth nph))) rays into the star's cone of solid angle
+ *     dOm = pi (R_star / |X_star - X|)^2, then nth bands of
+ *     ceil(nph sin th) rays over the rest of the sphere; the star rays end
+ *     on the star's surface when they meet it (check_neigh_fast
+ *     miscellaneous.f90:1056-1069) and start from B(T_star)
+ *     (inverse_rt.f90:113-115).  A node whose rays would exceed nth*nph
+ *     (the reference stops there) fails with PORTAL_ERR_ARG and status bit
+ *     PORTAL_NODE_STAR;
+ *   - image rays whose sky position lies on the star's disc start at the
+ *     star's front, z = z_star + R_star, from B(T_star) (raytrace.f90:103-115).
+ * portal_radiation_field_static has no context and is star_mod = 0 only. */
+int portal_set_star(portal_ctx *ctx, int star_mod, double T_star, double R_star, const double *X_star);
 
 /* Per-node maps of one inclination: the pix_mod = 0 mode of finish_portal.x
  * (para_finish.f90:245-350).  As portal_image, but one ray per bulk node,

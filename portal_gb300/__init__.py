@@ -30,7 +30,7 @@ KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_w
 EXPORTS = (
     "portal_strerror", "portal_last_error", "portal_create", "portal_destroy",
     "portal_set_molecule", "portal_set_cloud", "portal_set_populations",
-    "portal_radiation_field", "portal_radiation_field_split", "portal_solve_se", "portal_image", "portal_image_nodes", "portal_last_kernel_times",
+    "portal_radiation_field", "portal_radiation_field_split", "portal_solve_se", "portal_image", "portal_image_nodes", "portal_set_star", "portal_last_kernel_times",
     "portal_set_stream",
     "portal_wigner3j", "portal_wigner6j", "portal_coupling_constant",
     "portal_radiation_field_static", "portal_radiation_field_static_limits",
@@ -80,6 +80,7 @@ def lib() -> C.CDLL:
     P_F = C.POINTER(C.c_float)
     L.portal_image.argtypes = [C.c_void_p, P_D, C.c_int, P_I, P_I, C.c_double, C.c_double, C.c_int, C.c_double,
                                C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int] + [P_F] * 8 + [P_I]
+    L.portal_set_star.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, P_D]
     L.portal_image_nodes.argtypes = [C.c_void_p, P_D, C.c_int, P_I, P_I, C.c_double, C.c_double, C.c_int,
                                      C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, P_D] + \
         [C.POINTER(C.c_float)] * 8 + [P_I]
@@ -206,6 +207,16 @@ class Context:
                                            _p(dust_p), _p(h2_dens), _p(ab_all), _p(lev_p), _p(bvec),
                                            del_ne.shape[0], _p(del_ne, P_I), _p(del_num_ne, P_I), float(tx)))
         self.N, self.bulk = N, bulk
+
+    def set_star(self, star=None):
+        """Star mode: star = (T_star [K], R_star [m], (x, y, z) as the input
+        file gives them), or None for star_mod = 0."""
+        if star is None:
+            self._check(lib().portal_set_star(self._h, 0, 0.0, 0.0, None))
+            return
+        T_s, R_s, X_s = star
+        x = _f64(np.asarray(X_s, dtype=np.float64))
+        self._check(lib().portal_set_star(self._h, 1, float(T_s), float(R_s), _p(x)))
 
     def set_populations(self, lev_p):
         self._check(lib().portal_set_populations(self._h, _p(_f64(lev_p))))

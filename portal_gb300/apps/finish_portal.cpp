@@ -87,7 +87,7 @@ int main(int argc, char **argv) {
     std::string err;
     FinishInput in;
     if (!read_finish_input(input, in, err)) return fail(err);
-    if (in.star_mod == 1) return fail("star mode (star_mod = 1) is not supported");
+    if (in.star_mod != 0 && in.star_mod != 1) return fail("star_mod must be 0 or 1");
     Molecule m;
     Cloud c;
     if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err)) return fail(err);
@@ -122,6 +122,8 @@ int main(int argc, char **argv) {
                          c.temp_all.data(), c.dust_p.data(), c.h2_dens.data(), c.ab_all.data(), c.lev_p.data(),
                          bvec.data(), c.maxne, c.del_ne.data(), c.del_num_ne.data(), c.tx),
         "portal_set_cloud");
+    if (in.star_mod == 1)  // R_star in metres; X_star as read (para_finish.f90:116, :187)
+        chk(portal_set_star(ctx, 1, in.T_star, in.R_star, in.XYZ_star), "portal_set_star");
     const int npx = 2 * in.im_pix + 1, nch = 2 * in.nvel + 1, nl = in.nlevels;
     // every line takes the frequency of the last (l1, l2) pair (para_finish.f90:173-175)
     const double nu0 = m.e_levs[in.l2[nl - 1] - 1] - m.e_levs[in.l1[nl - 1] - 1];

@@ -88,7 +88,7 @@ int main(int argc, char **argv) {
     std::string err;
     MainInput in;
     if (!read_main_input(input, in, err)) return fail(err);
-    if (in.star_mod == 1) return fail("star mode (star_mod = 1) is not supported");
+    if (in.star_mod != 0 && in.star_mod != 1) return fail("star_mod must be 0 or 1");
     Molecule m;
     Cloud c;
     if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err)) return fail(err);
@@ -135,6 +135,8 @@ int main(int argc, char **argv) {
                          c.temp_all.data(), c.dust_p.data(), c.h2_dens.data(), c.ab_all.data(), c.lev_p.data(),
                          bvec.data(), c.maxne, c.del_ne.data(), c.del_num_ne.data(), c.tx),
         "portal_set_cloud");
+    if (in.star_mod == 1)  // R_star in metres; X_star as read (main_para.f90:75, :122)
+        chk(portal_set_star(ctx, 1, in.T_star, in.R_star, in.XYZ_star), "portal_set_star");
     long long nseg = 0;
     const double dx = (double)1e-6f;  // main_para.f90:135
     if (const char *li = getenv("PORTAL_LAMBDA")) {

@@ -74,6 +74,17 @@ struct portal_ctx {
     portal::DevBuf<double> b64, tkin, tdust, dustp, h2, ab;
     bool has_dust = false;
 
+    // ---- star mode (star_mod = 1, main_para.f90:75, :122, :216-246) ----
+    int star_mode = 0;
+    double T_star = 0.0, R_star_m = 0.0;  // R_star as the input file gives it, metres
+    double X_star[3] = {0.0, 0.0, 0.0};   // used unscaled, as the reference does
+    portal::DevBuf<double> ab_star;       // ab, 0 for the nodes inside the star (skipped)
+    portal::DevBuf<float> bbstar;         // (r_num) black_body(T_star) per line
+    // the abundances the node loop runs on: nodes with ab <= 0 (and, in star
+    // mode, inside the star) are skipped by the radiation field and the SE
+    const double *active_ab() const { return star_mode ? ab_star.p : ab.p; }
+    double R_star() const { return R_star_m / tx; }  // main_para.f90:122
+
     // ---- derived / results ----
     portal::DevBuf<float4> ltab;      // (r_num,N) line table
     portal::DevBuf<unsigned char> linebuf;  // per-line constants of the molecule (rf.cu)

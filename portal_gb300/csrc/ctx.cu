@@ -155,6 +155,8 @@ static int upload(portal_ctx *c, double *dst, const double *src, size_t n) {
     return PORTAL_OK;
 }
 
+static int star_refresh(portal_ctx *c);
+
 extern "C" int portal_set_cloud(portal_ctx *c, int N, int bulk, int nlev, const double *xyz,
                                 const double *vel_all, const double *b_all, const double *temp_all,
                                 const double *dust_p, const double *h2_dens, const double *ab_all,
@@ -239,7 +241,46 @@ extern "C" int portal_set_cloud(portal_ctx *c, int N, int bulk, int nlev, const 
     c->has_dust = dust;
     if (!c->have_mol) c->nlev = nlev;
     c->have_cloud = true;
+    return star_refresh(c);
+}
+
+namespace {
+// star mode: the node loop skips nodes with |X| <= R_star (main_para.f90:232,
+// which compares |X| with R_star, the star taken as centred)
+__global__ void k_star_mask(int N, double R, const double *__restrict__ pos, const double *__restrict__ ab,
+                            double *__restrict__ out) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const double x = pos[3 * (size_t)n], y = pos[3 * (size_t)n + 1], z = pos[3 * (size_t)n + 2];
+    out[n] = (__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z))) > R) ? ab[n]
+                                                                                                      : 0.0;
+}
+}  // namespace
+
+// The abundances with the star's interior masked out (star mode, with a cloud).
+static int star_refresh(portal_ctx *c) {
+    if (!c->star_mode || !c->have_cloud) return PORTAL_OK;
+    if (c->ab_star.reserve(c->N)) return set_err(c, PORTAL_ERR_NOMEM, "star mask");
+    k_star_mask<<<(c->N + 255) / 256, 256, 0, c->stream>>>(c->N, c->R_star(), c->pos64.p, c->ab.p, c->ab_star.p);
+    PCHECK(c, cudaGetLastError());
+    PCHECK(c, cudaStreamSynchronize(c->stream));
     return PORTAL_OK;
+}
+
+extern "C" int portal_set_star(portal_ctx *c, int star_mod, double T_star, double R_star,
+                               const double *X_star) {
+    if (!c) return PORTAL_ERR_ARG;
+    if (star_mod != 0 && star_mod != 1) return set_err(c, PORTAL_ERR_ARG, "portal_set_star: star_mod 0 or 1");
+    if (star_mod == 1 && (!X_star || !(R_star > 0.0) || !(T_star >= 0.0)))
+        return set_err(c, PORTAL_ERR_ARG, "portal_set_star: R_star > 0, T_star >= 0 and X_star(3) needed");
+    cudaSetDevice(c->device);
+    c->star_mode = star_mod;
+    c->T_star = star_mod ? T_star : 0.0;
+    c->R_star_m = star_mod ? R_star : 0.0;
+    for (int k = 0; k < 3; k++) c->X_star[k] = star_mod ? X_star[k] : 0.0;
+    c->j_valid = false;
+    c->ali_valid = false;
+    return star_refresh(c);
 }
 
 extern "C" int portal_set_populations(portal_ctx *c, const double *lev_p) {

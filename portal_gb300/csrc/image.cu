@@ -46,7 +46,7 @@ using namespace portal;
 namespace {
 
 struct ImLine {
-    double nu0, A, kd, w1, w2, fas, bb_cmb;
+    double nu0, A, kd, w1, w2, fas, bb_cmb, bb_star;
     int lo, up, j1, j2;  // 0-based levels
 };
 constexpr int IM_MAX_LINES = 16;
@@ -148,6 +148,8 @@ __global__ void k_im_nodes(ImNodeArgs a) {
 struct ImArgs {
     int N, npx, im_pix, nlines, nvel, nch, n_depth;
     int mode, nrays;         // 0: pixel grid, nrays = npx^2; 1: one ray per bulk node
+    int star;                // star mode: rays starting on the star's disc start at its front
+    double Rs, sx, sy, sz;   // R_star / tx and the rotated star position
     double im_size, dx, tdx, alpha, dvel, v0;
     const double *xyz;       // rotated (3,N)
     const int *off, *idx;    // neighbour CSR
@@ -184,10 +186,10 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
         if (p0 >= npix) break;
         // ---- (1) march, one lane per pixel ----
         const int p = p0 + lane;
-        int nc = 0, st = 0;
+        int nc = 0, st = 0, fs = 0;  // fs: the ray starts on the star
         if (p < npix) {
             double x, y;
-            if (a.mode == 1) {  // the node's rotated sky position (para_finish.f90:292)
+            if (a.mode == 1) {  // the node's rotated sky position (para_finish.f90:296)
                 x = a.xyz[3 * (size_t)p];
                 y = a.xyz[3 * (size_t)p + 1];
             } else {
@@ -196,7 +198,15 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 y = ib * a.im_size / a.im_pix;
             }
             // the oracle's FP64 arithmetic, without FMA contraction, throughout the march
-            const double z0 = -1.0 * __dsqrt_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(x, x)), __dmul_rn(y, y)));
+            const double zs0 = -1.0 * __dsqrt_rn(__dsub_rn(__dsub_rn(1.0, __dmul_rn(x, x)), __dmul_rn(y, y)));
+            double z0 = zs0;
+            if (a.star) {  // raytrace.f90:103-115: on the star's disc, start at its front
+                const double xc = __dsub_rn(x, a.sx), yc = __dsub_rn(y, a.sy);
+                if (__dsqrt_rn(__dadd_rn(__dmul_rn(xc, xc), __dmul_rn(yc, yc))) < a.Rs) {
+                    z0 = __dadd_rn(a.sz, a.Rs);
+                    fs = 1;
+                }
+            }
             int2 *dl = wbase + (size_t)lane * a.n_depth;
             // nearest node to the start point (raytrace.f90:126-134 scans all
             // nodes; strict <, so the lowest index wins).  The same argmin by
@@ -227,7 +237,7 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
             if (!(best < 10.0)) { c = -1; st = 3; }  // start point outside the unit sphere (NaN; rsave = 10)
             double z = z0;
             int k = 0;
-            const double zexit = -z0;
+            const double zexit = -zs0;
             while (st == 0) {
                 // predicted first step at which a neighbour is nearer than c
                 const double cx = a.xyz[3 * (size_t)c], cy = a.xyz[3 * (size_t)c + 1],
@@ -286,16 +296,18 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
         for (int rr = 0; rr < npx_b; rr++) {
             const int ncr = __shfl_sync(FULL, nc, rr);
             const int str = __shfl_sync(FULL, st, rr);
+            const int fsr = __shfl_sync(FULL, fs, rr);
             const int pix = p0 + rr;
             const int2 *dl = wbase + (size_t)rr * a.n_depth;
             for (int j = 0; j < a.nlines; j++) {
                 const ImLine L = c_im[j];
                 float I[NS], Q[NS], U[NS], tau[NS], tauc[NS];
-                const float Iin = (float)L.bb_cmb;
+                const double Iin_d = fsr ? L.bb_star : L.bb_cmb;  // I_in (raytrace.f90:97-115)
+                const float Iin = (float)Iin_d;
 #pragma unroll
                 for (int s = 0; s < NS; s++) { I[s] = Iin; Q[s] = 0.f; U[s] = 0.f; tau[s] = 0.f; tauc[s] = 0.f; }
                 // dust terms: channel independent, FP64, every lane alike
-                double Id = L.bb_cmb, sig0 = 0.0, sig2 = 0.0, Qd = 0.0, Ud = 0.0, taud = 0.0;
+                double Id = Iin_d, sig0 = 0.0, sig2 = 0.0, Qd = 0.0, Ud = 0.0, taud = 0.0;
                 for (int i = 0; i + 1 < ncr && str == 0; i++) {
                     const int2 e0 = dl[i], e1 = dl[i + 1];
                     const int cell = e0.x;
@@ -442,6 +454,10 @@ static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const i
         L.fas = ((1 + L.j1 + L.j2) % 2 == 0) ? 1.0 : -1.0;
         L.bb_cmb = 1.4744995e-50 * std::pow(nu_last, 3.0) *
                    std::pow(std::exp(4.79924e-11 / 2.73 * nu_last) - 1.0, -1.0);
+        L.bb_star = (c->star_mode && c->T_star > 0.0)
+                        ? 1.4744995e-50 * std::pow(nu_last, 3.0) *
+                              std::pow(std::exp(4.79924e-11 / c->T_star * nu_last) - 1.0, -1.0)
+                        : 0.0;
     }
     PCHECK(c, cudaMemcpyToSymbolAsync(c_im, h, sizeof(ImLine) * nlines, 0, cudaMemcpyHostToDevice, c->stream));
     // rotation R_tot = R_z(ph_az) R_x(th_inc) (rotmat miscellaneous.f90:146-181)
@@ -496,6 +512,16 @@ static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const i
     ImArgs ia;
     ia.N = N; ia.npx = npx; ia.im_pix = im_pix; ia.nlines = nlines; ia.nvel = nvel; ia.nch = nch;
     ia.mode = mode; ia.nrays = nrays;
+    // star mode: R_star / tx (para_finish.f90:187) and the star's position rotated with the
+    // nodes (rotate_all_save miscellaneous.f90:899-904), used unscaled as the reference does
+    ia.star = c->star_mode;
+    ia.Rs = c->star_mode ? c->R_star() : 0.0;
+    {
+        double sp[3] = {0.0, 0.0, 0.0};
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) sp[j] = sp[j] + na.R[j + 3 * k] * c->X_star[k];
+        ia.sx = sp[0]; ia.sy = sp[1]; ia.sz = sp[2];
+    }
     ia.n_depth = n_depth_rt; ia.im_size = im_size; ia.dx = dx; ia.tdx = c->tx * dx; ia.alpha = alpha; ia.dvel = dvel; ia.v0 = v0;
     ia.xyz = xyz_r.p; ia.off = c->nb_off.p; ia.idx = c->nb_idx.p; ia.cellv = cellv.p; ia.cellb = cellb.p;
     ia.coef = coef.p; ia.dust_p = c->dustp.p; ia.tdust = c->tdust.p; ia.status = stat.p;

@@ -23,6 +23,11 @@ struct RFArgs {
     const float *__restrict__ chw;    // (nch) exp(-q0^2) * 2/(sqrt(pi) nvel)
     const float *__restrict__ bb;     // (L) black_body(2.73 K) per line: the incoming intensity
     double gx, gy, gz;
+    // star mode: each node's ray set from star_all (nth x nph bands around the
+    // star direction), star rays end on the star and start from B(T_star)
+    int star, nth, nph;
+    double xs, ys, zs, Rs;
+    const float *__restrict__ bbs;    // (L) black_body(T_star) per line
     double *J0, *J2;
     double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
     int *status;

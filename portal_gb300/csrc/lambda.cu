@@ -182,7 +182,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
         if (sp.reserve((size_t)N * 2 * nlev)) return set_err(c, PORTAL_ERR_NOMEM, "start pops");
         PCHECK(c, cudaMemcpyAsync(sp.p, start_pops, (size_t)N * 2 * nlev * sizeof(double),
                                   cudaMemcpyHostToDevice, c->stream));
-        k_rho_to_pops<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, sp.p, c->nmol.p, c->ab.p, jl.p, c->levp.p);
+        k_rho_to_pops<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, sp.p, c->nmol.p, c->active_ab(), jl.p, c->levp.p);
         PCHECK(c, cudaGetLastError());
         PCHECK(c, cudaStreamSynchronize(c->stream));
     }
@@ -214,7 +214,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
         if ((rc = run_solve_se(c, kmax, &nsing, false))) return rc;
         if (nsing) return set_err(c, PORTAL_ERR_SINGULAR, std::to_string(nsing) + " singular SE systems");
         PCHECK(c, cudaMemsetAsync(c->counters.p + 3, 0, sizeof(unsigned long long), c->stream));
-        k_update<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, c->pops.p, c->nmol.p, c->ab.p, jl.p, c->levp.p,
+        k_update<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, c->pops.p, c->nmol.p, c->active_ab(), jl.p, c->levp.p,
                                            rho_prev.p, c->counters.p + 3);
         PCHECK(c, cudaGetLastError());
         unsigned long long rb = 0;
@@ -249,7 +249,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
                 const double *x2 = ring.p + (size_t)((n_hist - 2) % 4) * nv;
                 const double *x1 = ring.p + (size_t)((n_hist - 3) % 4) * nv;
                 const double *x0 = ring.p + (size_t)((n_hist - 4) % 4) * nv;
-                k_ng_sums<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, c->ab.p, x0, x1, x2, x3, part.p);
+                k_ng_sums<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, c->active_ab(), x0, x1, x2, x3, part.p);
                 k_ng_final<<<1, 32, 0, c->stream>>>(nb, part.p, part.p + 5 * (size_t)nb);
                 PCHECK(c, cudaGetLastError());
                 double S[5];
@@ -260,7 +260,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
                     const double a = (S[3] * S[2] - S[1] * S[4]) / det;
                     const double b = (S[0] * S[4] - S[1] * S[3]) / det;
                     if (std::isfinite(a) && std::isfinite(b)) {
-                        k_ng_apply<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, a, b, c->ab.p, c->nmol.p, jl.p, x1,
+                        k_ng_apply<<<nb, tb, 0, c->stream>>>(N, c->bulk, nlev, a, b, c->active_ab(), c->nmol.p, jl.p, x1,
                                                             x2, x3, rho_prev.p, c->levp.p);
                         PCHECK(c, cudaGetLastError());
                         // the extrapolated state starts a new plain sequence

@@ -69,8 +69,17 @@ int upload_lines(portal_ctx *c) {
         h[k].up = up;
         bb[k] = (float)h[k].bb_cmb;
     }
-    if (c->linebuf.reserve(sizeof(LineConst) * c->r_num) || c->bbcmb.reserve(c->r_num))
+    if (c->linebuf.reserve(sizeof(LineConst) * c->r_num) || c->bbcmb.reserve(c->r_num) ||
+        c->bbstar.reserve(c->r_num))
         return set_err(c, PORTAL_ERR_NOMEM, "line constants");
+    // star rays start from black_body(T_star) (inverse_rt.f90:113-115)
+    std::vector<float> bs(c->r_num, 0.f);
+    if (c->star_mode && c->T_star > 0.0)
+        for (int k = 0; k < c->r_num; k++)
+            bs[k] = (float)(1.4744995e-50 * std::pow(c->nu[k], 3.0) *
+                            std::pow(std::exp(4.79924e-11 / c->T_star * c->nu[k]) - 1.0, -1.0));
+    PCHECK(c, cudaMemcpyAsync(c->bbstar.p, bs.data(), sizeof(float) * c->r_num, cudaMemcpyHostToDevice,
+                              c->stream));
     PCHECK(c, cudaMemcpyAsync(c->linebuf.p, h.data(), sizeof(LineConst) * c->r_num, cudaMemcpyHostToDevice,
                               c->stream));
     PCHECK(c, cudaMemcpyAsync(c->bbcmb.p, bb.data(), sizeof(float) * c->r_num, cudaMemcpyHostToDevice,
@@ -212,6 +221,11 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
     a.off = c->nb_off.p; a.idx = c->nb_idx.p; a.edge = c->edge.p; a.ltab = c->ltab.p;
     a.dirs = c->dirtab.p; a.chq = c->chtab.p; a.chw = c->chtab.p + nch; a.bb = c->bbcmb.p;
     a.gx = gvec[0]; a.gy = gvec[1]; a.gz = gvec[2];
+    a.ab = c->active_ab();
+    a.star = c->star_mode; a.nth = nth; a.nph = nph;
+    a.xs = c->X_star[0]; a.ys = c->X_star[1]; a.zs = c->X_star[2];
+    a.Rs = c->star_mode ? c->R_star() : 0.0;
+    a.bbs = c->bbstar.p;
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
     a.JE = split ? c->JE.p : nullptr;
     a.LS = split ? c->LS.p : nullptr;
@@ -287,9 +301,14 @@ int radiation_field_call(portal_ctx *c, int nth, int nph, int nvel, const double
     if (!st) { st_host.resize(c->N); st = st_host.data(); }
     PCHECK(c, cudaMemcpyAsync(st, c->status.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
-    for (int i = 0; i < c->N; i++)
+    for (int i = 0; i < c->N; i++) {
         if (st[i] & PORTAL_NODE_DEPTH)
             return set_err(c, PORTAL_ERR_DEPTH, "node_count > n_depth for node " + std::to_string(i + 1));
+        if (st[i] & PORTAL_NODE_STAR)
+            return set_err(c, PORTAL_ERR_ARG, "star mode: the star's rays exceed nth*nph for node " +
+                                                  std::to_string(i + 1) + " (a node this close to the star "
+                                                                          "stops the reference too)");
+    }
     return PORTAL_OK;
 }
 

@@ -92,9 +92,131 @@ struct CellRec {
 // (up to) 32 rays.
 struct RayBatch {
     double frame[13];    // b(3), x(3), w(3), node position(3), |p|^2
+    double sk[7];        // star mode: star direction k(3), th_star, dth_star, dth_rest, th_i
+    int sn[2];           // star mode: star rays, all rays of the node (-1: more than nth nph)
+    unsigned smask;      // star rays of the batch
     float4 dir[32];      // (d_x, d_y, d_z, v_node . d) per ray
+    float2 wts[32];      // (w, w c_in / sqrt 2) per ray
     int K[32];           // segments per ray (-1: n_depth overflow)
 };
+
+constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
+
+// star_all (miscellaneous.f90:1139-1217, circle_points :1219-1265) for ray
+// i of a node outside the star: (cos th, ph) of the ray in the field frame
+// and its quadrature weight, as (x, y, z).  sk as in RayBatch; f the node frame b (0-2),
+// x = b x g / |b x g| (3-5), x x b (6-8).  The first n_star rays cover the
+// star's cone (one ray: the reference's x(1:2) = cos(1), i.e. 1 rad off the
+// star direction; fewer than ten: a circle at th_star / 2; more: Vogel's
+// spiral), the others nth bands of ceiling(nph sin th) rays from th_star to
+// pi about the star direction.  Each direction, built about the star
+// direction with find_dir (gauge g), is re-expressed by find_angles in the
+// field frame (miscellaneous.f90:86-145).
+// Returns the direction's (cos th, sin th, cos ph, sin ph) in the field
+// frame as inverse_rt rebuilds it (find_dir of acos(mu), ph) and stores the
+// weights (w, w c_in / sqrt 2) in *wts.  Out of line: the default path
+// keeps the kernel's own code.
+__device__ __noinline__ double4 star_ray(const double *sk, int n_star, int i, int nth, int nph, double gx,
+                                         double gy, double gz, const double *f, float2 *wts) {
+    double x1 = 1.0, x2 = 0.0, w = 0.0;
+    if (i < n_star) {
+        const double ths = sk[3], dth = sk[4];
+        if (n_star == 1) {
+            x1 = cos(1.0);
+            x2 = cos(1.0);
+            w = 2.0 * PI_D * dth;
+        } else if (n_star < 10) {
+            const double wph = 2.0 * PI_D / n_star;
+            x1 = cos(ths / 2.0);
+            x2 = i * wph;
+            w = wph * dth;
+        } else {
+            x1 = cos(ths * sqrt(1.0 * (i + 1) / n_star));
+            x2 = (i + 1) * (PI_D * (3.0 - sqrt(5.0)));
+            w = dth * 2.0 * PI_D / n_star;
+        }
+        w = w / (4.0 * PI_D);
+    } else {
+        const double dr = sk[5], thi = sk[6];
+        int j = i - n_star, b = 1, np = 1;
+        double th = thi;
+        for (; b <= nth; b++) {
+            th = (b - 1) * dr + thi;
+            np = (int)ceil(nph * sin(th));
+            if (j < np) break;
+            j -= np;
+        }
+        if (b <= nth) {
+            double wth;
+            if (b == 1) wth = cos(sk[3]) - cos((b - 0.5) * dr + thi);
+            else if (b == nth) wth = cos((b - 1.5) * dr + thi) + 1.0;
+            else wth = cos((b - 1.5) * dr + thi) - cos((b - 0.5) * dr + thi);
+            const double wph = 2.0 * PI_D / np;
+            x1 = cos(th);
+            x2 = j * wph;
+            w = wth * wph / (4.0 * PI_D);
+        }
+    }
+    // find_dir about k: x_k = k x g / |k x g|, d = cos t k + sin t (cos x2 (x_k x k) + sin x2 x_k)
+    const double kx = sk[0], ky = sk[1], kz = sk[2];
+    double ux = ky * gz - kz * gy, uy = kz * gx - kx * gz, uz = kx * gy - ky * gx;
+    const double un = sqrt(ux * ux + uy * uy + uz * uz);
+    ux /= un; uy /= un; uz /= un;
+    const double vx = uy * kz - uz * ky, vy = uz * kx - ux * kz, vz = ux * ky - uy * kx;
+    const double t = acos(x1), ct = cos(t), st = sin(t), cp = cos(x2), sp = sin(x2);
+    const double dx = ct * kx + st * (cp * vx + sp * ux);
+    const double dy = ct * ky + st * (cp * vy + sp * uy);
+    const double dz = ct * kz + st * (cp * vz + sp * uz);
+    // find_angles in the field frame
+    const double bd = f[0] * dx + f[1] * dy + f[2] * dz;
+    const double thb = (bd > 1.0) ? 0.0 : (bd < -1.0) ? PI_D : acos(bd);
+    const double cx = f[1] * dz - f[2] * dy, cy = f[2] * dx - f[0] * dz, cz = f[0] * dy - f[1] * dx;
+    const double mub = cos(thb);
+    const double phb = atan2(f[3] * dx + f[4] * dy + f[5] * dz, f[3] * cx + f[4] * cy + f[5] * cz);
+    *wts = make_float2((float)w, (float)(w * ((3.0 * mub * mub - 1.0) / 2.0) / sqrt(2.0)));
+    const double th = acos(mub);
+    return make_double4(cos(th), sin(th), cos(phb), sin(phb));
+}
+
+// trace_node's star geometry (main_sub.f90:56-66) and star_all's ray counts
+// for the node at p: fills sk and sn of the warp's RayBatch.
+__device__ __noinline__ void star_node(double *sk, int *sn, double xs, double ys, double zs, double Rs, int nth,
+                                       int nph, double px, double py, double pz) {
+    const double kx = xs - px, ky = ys - py, kz = zs - pz;
+    const double d = sqrt(kx * kx + ky * ky + kz * kz);
+    const double q = Rs / d;
+    const double dOm = PI_D * (q * q);
+    sk[0] = kx / d; sk[1] = ky / d; sk[2] = kz / d;
+    const double dth = dOm / (2.0 * PI_D);
+    const double ths = acos(1 - dth);
+    const double dOm_max = 4.0 * PI_D / (nth * nph);
+    const int ns = (int)ceil(dOm / dOm_max);
+    const double dr = (PI_D - ths) / nth, thi = ths + dr / 2.0;
+    sk[3] = ths; sk[4] = dth; sk[5] = dr; sk[6] = thi;
+    int nv = ns;
+    for (int b = 1; b <= nth; b++) nv += (int)ceil(nph * sin((b - 1) * dr + thi));
+    sn[0] = ns;
+    // the reference stops when the rays exceed nth nph (miscellaneous.f90:1181-1184)
+    sn[1] = (ns > nth * nph || nv > nth * nph) ? -1 : nv;
+}
+
+// check_neigh_fast's star test (miscellaneous.f90:1056-1069) from the node
+// at p along d: the star's surface, when the ray meets it first, ends it.
+__device__ __noinline__ double star_exit(double sexit, double px, double py, double pz, double dx, double dy,
+                                         double dz, double xs, double ys, double zs, double Rs) {
+    const double ex = px - xs, ey = py - ys, ez = pz - zs;
+    const double qa = dx * dx + dy * dy + dz * dz;
+    const double qb = 2.0 * (ex * dx + ey * dy + ez * dz);
+    const double qc = (ex * ex + ey * ey + ez * ez) - Rs * Rs;
+    const double dis = qb * qb - 4.0 * qa * qc;
+    if (dis > 0.0) {
+        double r1 = (-qb + sqrt(dis)) / (2.0 * qa);
+        const double r2 = (-qb - sqrt(dis)) / (2.0 * qa);
+        if (r2 > 0.0) r1 = r2;
+        if (r1 > 0.0 && r1 < sexit) return r1;
+    }
+    return sexit;
+}
 
 // NS channel slots per lane, NLG lines per register group.
 // RT = 0: nch <= 32 NS, every channel in a slot.  RT = 1: nch = 32 NS + 1
@@ -163,24 +285,44 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                 f[0] = bx; f[1] = by; f[2] = bz; f[3] = xx; f[4] = xy; f[5] = xz;
                 f[6] = xy * bz - xz * by; f[7] = xz * bx - xx * bz; f[8] = xx * by - xy * bx;
                 f[9] = px; f[10] = py; f[11] = pz; f[12] = px * px + py * py + pz * pz;
+                if (a.star) star_node(B.sk, B.sn, a.xs, a.ys, a.zs, a.Rs, a.nth, a.nph, px, py, pz);
             }
             __syncwarp();
+            int ndir = a.ndir;
+            if (a.star) {
+                ndir = B.sn[1];
+                if (ndir < 0) {
+                    st |= PORTAL_NODE_STAR;
+                    ndir = 0;
+                }
+            }
             const float4 cvn = a.cellv[node];
             const float dqfac = 2.f * cvn.w / (float)a.nvel;
 
-            for (int k0 = 0; k0 < a.ndir && st == 0; k0 += 32) {
-                const int nr = min(32, a.ndir - k0);
+            for (int k0 = 0; k0 < ndir && st == 0; k0 += 32) {
+                const int nr = min(32, ndir - k0);
                 // ---- (1)+(2) set-up and walk, one lane per ray ----
                 int K = 0;
                 bool over = false;
+                const bool sray = a.star && lane < nr && k0 + lane < B.sn[0];
+                const unsigned smask = __ballot_sync(FULL, sray);
                 if (lane < nr) {
-                    const double *dr = a.dirs + 6 * (size_t)(k0 + lane);
                     const double *f = B.frame;
-                    const double mu = dr[0], sth = dr[1], cph = dr[2], sph = dr[3];
+                    double mu, sth, cph, sph;
+                    if (a.star) {
+                        const double4 r = star_ray(B.sk, B.sn[0], k0 + lane, a.nth, a.nph, a.gx, a.gy, a.gz, f,
+                                                   &B.wts[lane]);
+                        mu = r.x; sth = r.y; cph = r.z; sph = r.w;
+                    } else {
+                        const double *dr = a.dirs + 6 * (size_t)(k0 + lane);
+                        mu = dr[0]; sth = dr[1]; cph = dr[2]; sph = dr[3];
+                        B.wts[lane] = make_float2((float)dr[4], (float)dr[5]);
+                    }
                     const double dx = mu * f[0] + sth * (cph * f[6] + sph * f[3]);
                     const double dy = mu * f[1] + sth * (cph * f[7] + sph * f[4]);
                     const double dz = mu * f[2] + sth * (cph * f[8] + sph * f[5]);
-                    const double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
+                    double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
+                    if (sray) sexit = star_exit(sexit, f[9], f[10], f[11], dx, dy, dz, a.xs, a.ys, a.zs, a.Rs);
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
                     int2 *wl = wbase + (size_t)lane * n_depth;
@@ -229,6 +371,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                     }
                 }
                 B.K[lane] = over ? -1 : K;
+                if (lane == 0) B.smask = smask;
                 if (__any_sync(FULL, over)) { st |= PORTAL_NODE_DEPTH; break; }
                 __syncwarp();
 
@@ -237,14 +380,16 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                     const int Kr = B.K[rr];
                     const int2 *wl = wbase + (size_t)rr * n_depth;
                     const float4 d4 = B.dir[rr];
-                    const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
-                    const float wgt = (float)dr[4], wgt2 = (float)dr[5];
+                    const float2 wt = B.wts[rr];
+                    const float wgt = wt.x, wgt2 = wt.y;
+                    // the incoming intensity: B(T_star) for a star ray (inverse_rt.f90:113-118)
+                    const float *bbin = ((B.smask >> rr) & 1u) ? a.bbs : a.bb;
                     nseg += (unsigned long long)Kr;
                     const int2 w0 = wl[0];
                     // the remainder channel of this lane's line (RT): intensity, and
                     // its central-cell contributions to J0 (and J_eff, L*)
                     float Irem = 0.f, remJ = 0.f, remE = 0.f, remL = 0.f;
-                    if (RT && lane < a.L) Irem = a.bb[lane];
+                    if (RT && lane < a.L) Irem = bbin[lane];
                     for (int l0 = 0; l0 < a.L; l0 += NLG) {
                         // intensities of the lane's channels: slot pairs (s, s+1) in one
                         // float2 (packed FP32x2 arithmetic), an odd last slot in .x
@@ -252,7 +397,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
 #define IV(s, l) (((s) & 1) ? I2[(s) >> 1][l].y : I2[(s) >> 1][l].x)
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
-                            const float bb = (l0 + l < a.L) ? a.bb[l0 + l] : 0.f;
+                            const float bb = (l0 + l < a.L) ? bbin[l0 + l] : 0.f;
 #pragma unroll
                             for (int s2 = 0; s2 < NS; s2++) IV(s2, l) = bb;
                         }

@@ -575,7 +575,7 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     SEArgs a;
     a.N = c->N; a.bulk = c->bulk; a.c_dim = n; a.n_trans = c->n_trans; a.nlev = c->nlev; a.L = c->r_num;
     a.c_temp = c->c_temp; a.c_num = c->c_num; a.c_par = c->c_par; a.nent = c->se_ni;
-    a.J0 = c->J0.p; a.J2 = c->J2.p; a.h2 = c->h2.p; a.tkin = c->tkin.p; a.ab = c->ab.p;
+    a.J0 = c->J0.p; a.J2 = c->J2.p; a.h2 = c->h2.p; a.tkin = c->tkin.p; a.ab = c->active_ab();
     a.JE = c->ali_valid ? c->JE.p : nullptr;
     a.LS = c->ali_valid ? c->LS.p : nullptr;
     const int *I = c->se_ints.p;

@@ -70,11 +70,21 @@ def write_dust(path, table):
     np.savetxt(path, table, fmt="%.17g")
 
 
+def _star_line(star):
+    """The star record (star_mod T_star R_star X Y Z, run_portal.sh:120):
+    star = None (star_mod 0 with run_portal.sh's values) or (T_star [K],
+    R_star [m], (x, y, z))."""
+    if star is None:
+        return "0 2.5E3 2.99196E11 0.d0 0.d0 0.d0"
+    T_s, R_s, X_s = star
+    return "1 %s %s %s" % (_g(T_s), _g(R_s), " ".join(_g(v) for v in X_s))
+
+
 def write_main_input(path, rc, kmax=None, extra_info=0, max_ne_temp=10000, dust_ii_gas=0.01,
-                     field=(0, 1, 0, "1.d0")):
+                     field=(0, 1, 0, "1.d0"), star=None):
     """The input file of main_portal.x as run_portal.sh:118-128 writes it."""
     with open(path, "w") as f:
-        f.write("\n0 2.5E3 2.99196E11 0.d0 0.d0 0.d0\n")
+        f.write("\n%s\n" % _star_line(star))
         f.write("%d %d %d\n" % (rc.nth, rc.nph, rc.nvel))
         f.write("%s\n" % dust_ii_gas)
         f.write("%s %s %s %s\n" % field)
@@ -84,13 +94,13 @@ def write_main_input(path, rc, kmax=None, extra_info=0, max_ne_temp=10000, dust_
 
 def write_finish_input(path, l1, l2, th_inc, ph_az, nvel, dvel, v0, im_pix, im_size, kmax=6, fits=1,
                        distance=3.086e16, max_ne_temp=10000, n_depth_rt=10000, dust_ii_gas=0.01,
-                       field=(0, 1, 0, "1.d0"), pix_mod=1):
+                       field=(0, 1, 0, "1.d0"), pix_mod=1, star=None):
     """The input file of finish_portal.x as run_portal.sh:133-152 writes it."""
     with open(path, "w") as f:
         f.write("\n%d\n%s\n%s\n\n" % (len(l1), " ".join(map(str, l1)), " ".join(map(str, l2))))
         f.write("%d\n%s\n%s\n\n" % (len(th_inc), " ".join(_g(t) for t in th_inc), " ".join(_g(p) for p in ph_az)))
         f.write("%d %s %s\n\n" % (nvel, _g(dvel), _g(v0)))
-        f.write("0 2.5E3 2.99196E11 0.d0 0.d0 0.d0\n%s\n" % dust_ii_gas)
+        f.write("%s\n%s\n" % (_star_line(star), dust_ii_gas))
         f.write("%s %s %s %s\n" % field)
         f.write("%d 0\n%d %d %s\n%d %s\n%d %d\n\n" % (kmax, pix_mod, im_pix, _g(im_size), fits, _g(distance),
                                                    max_ne_temp, n_depth_rt))

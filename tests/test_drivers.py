@@ -198,6 +198,49 @@ def test_finish_portal_node_maps(case):
     assert not os.path.exists(os.path.join(d, "inc01-trans01-vel%02d-im.dat" % (2 * nvel + 2)))
 
 
+@pytest.mark.gpu
+def test_star_mode_end_to_end(case, tmp_path):
+    """star_mod = 1 in both input files (run_portal.sh's default): the
+    executables pass the star to the library (R_star in metres, X_star as
+    read); pol_pops.dat and the FITS cube equal the library calls with the
+    same star."""
+    import shutil
+    import portal_gb300 as pg
+    d = str(tmp_path)
+    for name in ("model.pop", "grid.vtk", "molecule.dat", "dust.tab", "bvec.dat"):
+        shutil.copy(os.path.join(case["d"], name), d)
+    cloud, mol = case["cloud"], case["mol"]
+    # 12 x 12 directions: enough rays for the nodes nearest the star (star_all)
+    rc = synth.RunConfig(nth=12, nph=12, nvel=16, kmax=6, gvec=case["rc"].gvec)
+    star = (2500.0, 0.05 * cloud.tx, (0.0, 0.0, 0.0))
+    c2 = dict(case, d=d, paths={k: os.path.join(d, os.path.basename(v)) for k, v in case["paths"].items()})
+    lime.write_main_input(os.path.join(d, "pol.dat"), rc, extra_info=0, star=star)
+    env = dict(PORTAL_BVEC_FILE=c2["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec))
+    r = _run(MAIN, c2, env)
+    assert r.returncode == 0, r.stderr
+    pops_file = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    im = dict(l1=[1], l2=[2], th_inc=[0.5], ph_az=[0.0], nvel=4, dvel=80.0, v0=0.0, im_pix=8, im_size=0.6)
+    lime.write_finish_input(os.path.join(d, "finish.dat"), im["l1"], im["l2"], im["th_inc"], im["ph_az"],
+                            im["nvel"], im["dvel"], im["v0"], im["im_pix"], im["im_size"], star=star)
+    r2 = _run(FINISH, c2, env, input_name="finish.dat")
+    assert r2.returncode == 0, r2.stderr
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        ctx.set_star(star)
+        ctx.radiation_field(rc, fetch=False)
+        pops, _ = ctx.solve_se(rc.kmax)
+        inside = np.linalg.norm(cloud.xyz[:cloud.bulk_node_num], axis=1) <= 0.05
+        assert inside.any() and (pops_file[:cloud.bulk_node_num][inside] == 0).all()
+        np.testing.assert_allclose(pops_file, pops, rtol=1e-15, atol=0)
+        cube, _ = ctx.image(im["l1"], im["l2"], im["th_inc"][0], im["ph_az"][0], im["nvel"], im["dvel"], im["v0"],
+                            im["im_pix"], im["im_size"], pol_pops=pops_file)
+    nu0 = mol.e_levs[1] - mol.e_levs[0]
+    h, dI = lime.read_fits(os.path.join(d, "inc01-trans01-im_i.fits"))
+    np.testing.assert_allclose(dI, (3.255e39 / nu0 ** 2 * cube[0, 0].astype(np.float64)).astype(np.float32),
+                               rtol=1e-6, atol=1e-30, equal_nan=True)
+
+
 _ROW_WRITER_CHECK = r"""
 #include <cstdio>
 #include <vector>

@@ -146,6 +146,77 @@ def test_skipped_and_surface_nodes(ctx):
     _check_J(J0[:200], J2[:200], oJ0[:200], oJ2[:200], mask=m)
 
 
+def test_star_mode_against_oracle(ctx):
+    """star_mod = 1 (a 2,500 K star of 0.05 r_max at the centre): nodes inside
+    the star are skipped (J and populations 0); every other node integrates
+    over its own star_all ray set, the star rays ending on the star and
+    starting from B(T_star).  J within the stated tolerances of the oracle's
+    star-mode node loop, then the populations of the same J to 1e-10.  12 x
+    12 directions: with 8 x 8 the nodes nearest the star would need more
+    rays than nth*nph, where the reference stops."""
+    import oracle
+    cloud, mol, rc = _small()
+    rc.nth = rc.nph = 12
+    star = (2500.0, 0.05 * cloud.tx, (0.0, 0.0, 0.0))
+    inside = np.linalg.norm(cloud.xyz, axis=1) <= 0.05
+    assert 10 < inside[:cloud.bulk_node_num].sum() < cloud.bulk_node_num // 2
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    ctx.set_star(star)
+    try:
+        J0, J2, st, nseg = ctx.radiation_field(rc)
+        pops, _ = ctx.solve_se(rc.kmax)
+    finally:
+        ctx.set_star(None)
+    P = oracle.OracleProblem(cloud, mol, star=star)
+    oJ0, oJ2, ost, onseg, nf = P.radiation_field(rc)
+    assert nf == 0 and not st.any() and not ost.any()
+    bulk = cloud.bulk_node_num
+    assert (J0[:bulk][inside[:bulk]] == 0).all() and (pops[:bulk][inside[:bulk]] == 0).all()
+    live = ~inside[:bulk] & (cloud.ab_all[:bulk] > 0)
+    _check_J(J0[:bulk], J2[:bulk], oJ0[:bulk], oJ2[:bulk], mask=live)
+    assert abs(nseg - onseg) <= 1e-4 * onseg
+    # the star shows in the field of the nodes next to it
+    J0n, _, _, _ = _rf(ctx, cloud, mol, rc)
+    near = live & (np.linalg.norm(cloud.xyz[:bulk], axis=1) < 0.1)
+    assert near.any() and np.abs(J0 - J0n)[:bulk][near].max() > 1e-3 * J0n[:bulk][near].max()
+    opp, _, _ = P.solve_se(rc.kmax, J0, J2)
+    assert (opp[:bulk][inside[:bulk]] == 0).all()
+    np.testing.assert_allclose(pops[:bulk][live], opp[:bulk][live], rtol=1e-10, atol=1e-14)
+
+
+def test_image_star_against_oracle(ctx):
+    """Star mode in the image: pixels on the star's disc start at its front
+    from B(T_star) (raytrace.f90:103-115); I, Q, U, tau against the oracle
+    with the pixel-mode tolerances, NaN where the oracle's are."""
+    import oracle
+    cloud, mol, rc, im = _image_case(n=2048, im_pix=8)
+    star = (2500.0, 0.1 * cloud.tx, (0.0, 0.0, 0.0))
+    P = oracle.OracleProblem(cloud, mol)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc)
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2)
+    Ps = oracle.OracleProblem(cloud, mol, star=star)
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    ctx.set_star(star)
+    try:
+        cube, st = ctx.image(im["l1"], im["l2"], im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
+                             im["im_pix"], im["im_size"], pol_pops=opp)
+    finally:
+        ctx.set_star(None)
+    ocube, ost, nf = Ps.image(im["l1"], im["l2"], opp, im["th_inc"], im["ph_az"], im["nvel"], im["dvel"],
+                              im["v0"], im["im_pix"], im["im_size"])
+    assert nf == 0 and not st.any()
+    npx, nch = 2 * im["im_pix"] + 1, 2 * im["nvel"] + 1
+    o = ocube.reshape(8, npx, npx, 1, nch).transpose(0, 3, 4, 2, 1)
+    _stokes_close(cube, o, [0])
+    # the disc's rays start at the star's front: less optical depth than the star-less rays
+    plain, _ = ctx.image(im["l1"], im["l2"], im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
+                         im["im_pix"], im["im_size"], pol_pops=opp)
+    c = im["im_pix"]
+    assert (cube[3, 0, :, c, c] < plain[3, 0, :, c, c]).all()
+
+
 def test_neighbour_lists_longer_than_a_warp(ctx):
     """Padding every neighbour list with non-adjacent nodes (beyond 32
     entries) leaves the Voronoi walk unchanged: the padded faces are never the

@@ -1,4 +1,5 @@
 """The oracle against the golden fixtures and analytic limits (CPU only)."""
+import ctypes as C
 import json
 import math
 import os
@@ -220,3 +221,54 @@ def test_node_maps_start_points_and_einstein_a():
     P = oracle.OracleProblem(cloud, mol)
     pix, _, _ = P.image([1, 1], [2, 3], pp, th, ph, 4, 80.0, 0.0, 2, 0.5)
     assert np.abs(pix[0, :, 1]).max() == 0.0 and np.abs(pix[0, :, 0]).max() > 0.0
+
+
+@pytest.mark.parametrize("nth,nph,dist", [(8, 8, 3.0), (16, 16, 1.5), (12, 12, 40.0), (16, 16, 1.05), (6, 6, 8.0)])
+def test_star_all_ray_sets(nth, nph, dist):
+    """star_all (miscellaneous.f90:1139-1217): the weights of a node's rays
+    sum to one, the star's cone carries dOm / 4 pi with dOm = pi (R / d)^2,
+    and the cone's rays point within th_star of the star (one ray: the
+    reference's cos(1) stand-in, 1 rad off); the count stays within nth*nph."""
+    rng = np.random.default_rng(nth + nph)
+    b = rng.normal(size=3); b /= np.linalg.norm(b)
+    k = rng.normal(size=3); k /= np.linalg.norm(k)
+    g = np.asarray(synth.gauge_vector(3), dtype=np.float64)
+    dOm = math.pi / dist ** 2
+    xth, n_star = oracle.star_all(nth, nph, k, g, b, dOm)
+    assert 1 <= n_star < len(xth) <= nth * nph
+    np.testing.assert_allclose(xth[:, 2].sum(), 1.0, rtol=1e-13)
+    np.testing.assert_allclose(xth[:n_star, 2].sum(), dOm / (4 * math.pi), rtol=1e-13)
+    th_star = math.acos(1 - dOm / (2 * math.pi))
+    d = np.zeros(3)
+    L = oracle.lib()
+    for mu, ph, _ in xth[:n_star]:
+        L.orc_find_dir(b.ctypes.data_as(oracle.P_D), g.ctypes.data_as(oracle.P_D), C.c_double(math.acos(mu)),
+                       C.c_double(ph), d.ctypes.data_as(oracle.P_D))
+        ang = math.acos(min(1.0, float(d @ k)))
+        if n_star == 1:
+            assert abs(ang - 1.0) < 1e-9
+        else:
+            assert ang <= th_star + 1e-9
+
+
+def test_star_mode_node_loop_skips_the_star_and_ends_rays_on_it():
+    """Star mode in the oracle's node loop (main_para.f90:216-246): nodes
+    inside the star get J = 0 and no populations; the star rays of a node
+    just outside end on the star, so its walk is shorter than without the
+    star, and B(T_star) raises its field."""
+    cloud, mol = _tiny_problem(512)
+    rc = synth.RunConfig(nth=8, nph=8, nvel=8, kmax=2, gvec=synth.gauge_vector(1))
+    R = 0.08
+    P0 = oracle.OracleProblem(cloud, mol)
+    Ps = oracle.OracleProblem(cloud, mol, star=(3000.0, R * cloud.tx, (0.0, 0.0, 0.0)))
+    r = np.linalg.norm(cloud.xyz, axis=1)
+    inside = np.where(r[:64] <= R)[0]
+    near = np.where((r[:64] > R) & (r[:64] < 2 * R))[0]
+    assert len(inside) and len(near)
+    J0, J2, st, nseg, nf = Ps.radiation_field(rc, 1, 64)
+    J0n, _, _, nseg_n, _ = P0.radiation_field(rc, 1, 64)
+    assert nf == 0 and not st[:64].any()
+    assert (J0[inside] == 0).all() and (J2[inside] == 0).all()
+    pp, _, _ = Ps.solve_se(rc.kmax, J0, J2, 1, 64)
+    assert (pp[inside] == 0).all() and (pp[near] != 0).any()
+    assert (J0[near, 0] > J0n[near, 0]).all()
