@@ -5,7 +5,8 @@
 //
 //   finish_portal.x <input_file> <output_map> <pop> <grid> <mol> <dust>
 //
-// Reads <output_map>/pol_pops.dat (para_finish.f90:222-240) and writes, per
+// Reads <output_map>/pol_pops.dat (para_finish.f90:222-240; or its binary
+// sidecar pol_pops.bin when that is present and not older) and writes, per
 // line i and inclination j, inc{j}-trans{i}-im_{i,q,u,tau}.fits and the
 // centre-channel dust maps inc{j}-trans{i}-dust_{i,q,u,tau}.fits
 // (para_finish.f90:460-616), I, Q and U scaled by I_to_T = 3.255e39/nu0^2.
@@ -103,7 +104,12 @@ int main(int argc, char **argv) {
     }
     const int N = c.node_num, nlev = m.nlev;
     std::vector<double> pops;
-    if (!read_rows(out + "/pol_pops.dat", pops, N, 2 * nlev, err)) return fail(err);
+    // the binary sidecar main_portal.x writes with PORTAL_POPS_BINARY=1, when it
+    // is current; else the text file
+    if (read_sidecar(out + "/pol_pops.bin", out + "/pol_pops.dat", pops, N, 2 * nlev))
+        printf("finish_portal: populations from pol_pops.bin\n");
+    else if (!read_rows(out + "/pol_pops.dat", pops, N, 2 * nlev, err))
+        return fail(err);
     const int dev = getenv("PORTAL_DEVICE") ? atoi(getenv("PORTAL_DEVICE")) : 0;
     portal_ctx *ctx = nullptr;
     if (portal_create(&ctx, dev)) return fail(std::string("portal_create: ") + portal_last_error(nullptr));

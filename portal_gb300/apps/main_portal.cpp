@@ -24,6 +24,9 @@
 //                            at most n passes, accelerated) before the pass
 //                            whose results are written (no reference
 //                            counterpart: the reference makes one pass)
+//   PORTAL_POPS_BINARY=1     also write pol_pops.bin, a binary copy of
+//                            pol_pops.dat that finish_portal.x reads instead
+//                            of parsing the text (same values to the bit)
 //   PORTAL_DUMP_INGESTED=dir write the ingested arrays (what the library
 //                            receives) as .npy files into dir and stop
 //                            before any device work
@@ -167,6 +170,9 @@ int main(int argc, char **argv) {
         "portal_solve_se");
     portal_destroy(ctx);
     if (!write_rows(out + "/pol_pops.dat", pops, N, 2 * nlev)) return fail("cannot write " + out + "/pol_pops.dat");
+    if (const char *pb = getenv("PORTAL_POPS_BINARY"))
+        if (atoi(pb) == 1 && !write_sidecar(out + "/pol_pops.bin", pops, N, 2 * nlev))
+            return fail("cannot write " + out + "/pol_pops.bin");
     if (in.extra_info == 1) {
         std::vector<double> mf((size_t)N * 6);
         for (int i = 0; i < N; i++)

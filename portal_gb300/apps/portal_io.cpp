@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <sys/stat.h>
 #include <fstream>
 #include <random>
 #include <sstream>
@@ -602,6 +603,35 @@ bool read_rows(const std::string &path, std::vector<double> &cm, int rows, int c
     for (int i = 0; i < rows; i++)  // para_finish.f90:226-227
         for (int k = 0; k < cols; k++) cm[(size_t)i + (size_t)rows * k] = v[(size_t)i * cols + k];
     return true;
+}
+
+bool write_sidecar(const std::string &path, const std::vector<double> &cm, int rows, int cols) {
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const int32_t shape[2] = {rows, cols};
+    bool ok = fwrite("PORTALPP", 1, 8, f) == 8 && fwrite(shape, 4, 2, f) == 2 &&
+              fwrite(cm.data(), 8, (size_t)rows * cols, f) == (size_t)rows * cols;
+    return (fclose(f) == 0) && ok;
+}
+
+bool read_sidecar(const std::string &path, const std::string &text_path, std::vector<double> &cm, int rows,
+                  int cols) {
+    struct stat sb, st;
+    if (stat(path.c_str(), &sb) != 0) return false;
+    if (stat(text_path.c_str(), &st) == 0 &&
+        (sb.st_mtim.tv_sec < st.st_mtim.tv_sec ||
+         (sb.st_mtim.tv_sec == st.st_mtim.tv_sec && sb.st_mtim.tv_nsec < st.st_mtim.tv_nsec)))
+        return false;  // the text file was written after the sidecar: it wins
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    char magic[8];
+    int32_t shape[2];
+    std::vector<double> v((size_t)rows * cols);
+    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "PORTALPP", 8) == 0 && fread(shape, 4, 2, f) == 2 &&
+                    shape[0] == rows && shape[1] == cols && fread(v.data(), 8, v.size(), f) == v.size();
+    fclose(f);
+    if (ok) cm.swap(v);
+    return ok;
 }
 
 // ---------------------------------------------------------------------------

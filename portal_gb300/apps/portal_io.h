@@ -110,6 +110,16 @@ void gauge_vector(unsigned long long seed, double g[3]);
 bool write_rows(const std::string &path, const std::vector<double> &colmajor, int rows, int cols);
 bool read_rows(const std::string &path, std::vector<double> &colmajor, int rows, int cols, std::string &err);
 
+// Binary sidecar of pol_pops.dat (no reference counterpart): the magic
+// "PORTALPP", rows and cols as little-endian int32, then the rows x cols
+// doubles column-major -- the array pol_pops(N, 2 nlev) itself, the same
+// values the text file holds to the last bit.
+bool write_sidecar(const std::string &path, const std::vector<double> &colmajor, int rows, int cols);
+// Reads the sidecar when it exists, has the expected shape and is not older
+// than the text file it accompanies; false (and cm untouched) otherwise.
+bool read_sidecar(const std::string &path, const std::string &text_path, std::vector<double> &colmajor, int rows,
+                  int cols);
+
 // FITS primary HDU, BITPIX -32, NAXIS 3, keywords of writeimage
 // fits_writing.f90:1-159; array (npix, npix, nvel) column-major
 bool write_fits(const std::string &path, const float *array, int npix, int nvel, float restfreq,

@@ -80,6 +80,9 @@ struct portal_ctx {
     double X_star[3] = {0.0, 0.0, 0.0};   // used unscaled, as the reference does
     portal::DevBuf<double> ab_star;       // ab, 0 for the nodes inside the star (skipped)
     portal::DevBuf<float> bbstar;         // (r_num) black_body(T_star) per line
+    portal::DevBuf<unsigned char> star_model;  // the RFArgs of a star-mode pass (batched kernel)
+    portal::DevBuf<int2> star_items;      // its work items (0, node)
+    int star_items_n = 0;
     // the abundances the node loop runs on: nodes with ab <= 0 (and, in star
     // mode, inside the star) are skipped by the radiation field and the SE
     const double *active_ab() const { return star_mode ? ab_star.p : ab.p; }

@@ -3,6 +3,8 @@
 // See rf.cu for the algorithm.
 #pragma once
 
+#include <type_traits>
+
 #include <cmath>
 
 #include "internal.cuh"
@@ -89,22 +91,28 @@ struct CellRec {
 };
 
 // Per-warp shared state of the node being processed and its current batch of
-// (up to) 32 rays.
+// (up to) 32 rays (RayBatch; RayBatchStar in the batched kernel).
 struct RayBatch {
     double frame[13];    // b(3), x(3), w(3), node position(3), |p|^2
-    double sk[7];        // star mode: star direction k(3), th_star, dth_star, dth_rest, th_i
-    int sn[2];           // star mode: star rays, all rays of the node (-1: more than nth nph)
-    unsigned smask;      // star rays of the batch
     float4 dir[32];      // (d_x, d_y, d_z, v_node . d) per ray
-    float2 wts[32];      // (w, w c_in / sqrt 2) per ray
     int K[32];           // segments per ray (-1: n_depth overflow)
+};
+// The batched kernel's: also the per-node ray sets of star mode.
+struct RayBatchStar {
+    double frame[13];
+    double sk[7];        // star direction k(3), th_star, dth_star, dth_rest, th_i
+    int sn[2];           // star rays, all rays of the node (-1: more than nth nph)
+    unsigned smask;      // star rays of the batch
+    float4 dir[32];
+    float2 wts[32];      // (w, w c_in / sqrt 2) per ray
+    int K[32];
 };
 
 constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
 
 // star_all (miscellaneous.f90:1139-1217, circle_points :1219-1265) for ray
 // i of a node outside the star: (cos th, ph) of the ray in the field frame
-// and its quadrature weight, as (x, y, z).  sk as in RayBatch; f the node frame b (0-2),
+// and its quadrature weight.  sk as in RayBatchStar; f the node frame b (0-2),
 // x = b x g / |b x g| (3-5), x x b (6-8).  The first n_star rays cover the
 // star's cone (one ray: the reference's x(1:2) = cos(1), i.e. 1 rad off the
 // star direction; fewer than ten: a circle at th_star / 2; more: Vogel's
@@ -179,7 +187,7 @@ __device__ __noinline__ double4 star_ray(const double *sk, int n_star, int i, in
 }
 
 // trace_node's star geometry (main_sub.f90:56-66) and star_all's ray counts
-// for the node at p: fills sk and sn of the warp's RayBatch.
+// for the node at p: fills sk and sn of the warp's RayBatchStar.
 __device__ __noinline__ void star_node(double *sk, int *sn, double xs, double ys, double zs, double Rs, int nth,
                                        int nph, double px, double py, double pz) {
     const double kx = xs - px, ky = ys - py, kz = zs - pz;
@@ -236,10 +244,11 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
     const int n_depth = BATCH ? bw.n_depth : a0.n_depth;
     int2 *const wbase = (BATCH ? bw.walk : a0.walk) + (size_t)gw * 32 * (size_t)n_depth;
     __shared__ CellRec<NLG, DUST> recs[8];
-    __shared__ RayBatch rbs[8];
+    using RB = typename std::conditional<BATCH, RayBatchStar, RayBatch>::type;
+    __shared__ RB rbs[8];
     __shared__ RFArgs margs[BATCH ? 8 : 1];
     CellRec<NLG, DUST> &R = recs[wib];
-    RayBatch &B = rbs[wib];
+    RB &B = rbs[wib];
 
     unsigned long long nseg = 0;
     int cur_model = -1;
@@ -285,44 +294,66 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                 f[0] = bx; f[1] = by; f[2] = bz; f[3] = xx; f[4] = xy; f[5] = xz;
                 f[6] = xy * bz - xz * by; f[7] = xz * bx - xx * bz; f[8] = xx * by - xy * bx;
                 f[9] = px; f[10] = py; f[11] = pz; f[12] = px * px + py * py + pz * pz;
-                if (a.star) star_node(B.sk, B.sn, a.xs, a.ys, a.zs, a.Rs, a.nth, a.nph, px, py, pz);
-            }
-            __syncwarp();
-            int ndir = a.ndir;
-            if (a.star) {
-                ndir = B.sn[1];
-                if (ndir < 0) {
-                    st |= PORTAL_NODE_STAR;
-                    ndir = 0;
+                if constexpr (BATCH) {
+                    if (a.star) {
+                        star_node(B.sk, B.sn, a.xs, a.ys, a.zs, a.Rs, a.nth, a.nph, px, py, pz);
+                    } else {
+                        B.sn[0] = 0;
+                        B.sn[1] = a.ndir;
+                    }
                 }
             }
+            __syncwarp();
+            // star mode runs in the batched kernel only: its node's ray count lives in
+            // shared memory (read where used, holding no register through the
+            // integration); the single-model kernel uses the common direction table
+            const volatile int *vsn = nullptr;
+            if constexpr (BATCH) {
+                vsn = B.sn;
+                if (vsn[1] < 0) st |= PORTAL_NODE_STAR;
+            }
+            auto n_rays = [&]() -> int {
+                if constexpr (BATCH) return vsn[1];
+                else return a.ndir;
+            };
             const float4 cvn = a.cellv[node];
             const float dqfac = 2.f * cvn.w / (float)a.nvel;
 
-            for (int k0 = 0; k0 < ndir && st == 0; k0 += 32) {
-                const int nr = min(32, ndir - k0);
+            for (int k0 = 0; st == 0 && k0 < n_rays(); k0 += 32) {
+                const int nr = min(32, n_rays() - k0);
                 // ---- (1)+(2) set-up and walk, one lane per ray ----
                 int K = 0;
                 bool over = false;
-                const bool sray = a.star && lane < nr && k0 + lane < B.sn[0];
-                const unsigned smask = __ballot_sync(FULL, sray);
+                bool sray = false;
+                unsigned smask = 0u;
+                if constexpr (BATCH) {
+                    sray = a.star && lane < nr && k0 + lane < vsn[0];
+                    smask = __ballot_sync(FULL, sray);
+                }
                 if (lane < nr) {
                     const double *f = B.frame;
                     double mu, sth, cph, sph;
-                    if (a.star) {
-                        const double4 r = star_ray(B.sk, B.sn[0], k0 + lane, a.nth, a.nph, a.gx, a.gy, a.gz, f,
-                                                   &B.wts[lane]);
-                        mu = r.x; sth = r.y; cph = r.z; sph = r.w;
-                    } else {
+                    bool tab = true;
+                    if constexpr (BATCH) {
+                        if (a.star) {
+                            const double4 r = star_ray(B.sk, vsn[0], k0 + lane, a.nth, a.nph, a.gx, a.gy, a.gz, f,
+                                                       &B.wts[lane]);
+                            mu = r.x; sth = r.y; cph = r.z; sph = r.w;
+                            tab = false;
+                        }
+                    }
+                    if (tab) {
                         const double *dr = a.dirs + 6 * (size_t)(k0 + lane);
                         mu = dr[0]; sth = dr[1]; cph = dr[2]; sph = dr[3];
-                        B.wts[lane] = make_float2((float)dr[4], (float)dr[5]);
+                        if constexpr (BATCH) B.wts[lane] = make_float2((float)dr[4], (float)dr[5]);
                     }
                     const double dx = mu * f[0] + sth * (cph * f[6] + sph * f[3]);
                     const double dy = mu * f[1] + sth * (cph * f[7] + sph * f[4]);
                     const double dz = mu * f[2] + sth * (cph * f[8] + sph * f[5]);
                     double sexit = sphere_exit(f[9], f[10], f[11], dx, dy, dz);
-                    if (sray) sexit = star_exit(sexit, f[9], f[10], f[11], dx, dy, dz, a.xs, a.ys, a.zs, a.Rs);
+                    if constexpr (BATCH) {
+                        if (sray) sexit = star_exit(sexit, f[9], f[10], f[11], dx, dy, dz, a.xs, a.ys, a.zs, a.Rs);
+                    }
                     const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
                     B.dir[lane] = make_float4(fdx, fdy, fdz, cvn.x * fdx + cvn.y * fdy + cvn.z * fdz);
                     int2 *wl = wbase + (size_t)lane * n_depth;
@@ -371,7 +402,9 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                     }
                 }
                 B.K[lane] = over ? -1 : K;
-                if (lane == 0) B.smask = smask;
+                if constexpr (BATCH) {
+                    if (lane == 0) B.smask = smask;
+                }
                 if (__any_sync(FULL, over)) { st |= PORTAL_NODE_DEPTH; break; }
                 __syncwarp();
 
@@ -380,16 +413,32 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                     const int Kr = B.K[rr];
                     const int2 *wl = wbase + (size_t)rr * n_depth;
                     const float4 d4 = B.dir[rr];
-                    const float2 wt = B.wts[rr];
-                    const float wgt = wt.x, wgt2 = wt.y;
-                    // the incoming intensity: B(T_star) for a star ray (inverse_rt.f90:113-118)
-                    const float *bbin = ((B.smask >> rr) & 1u) ? a.bbs : a.bb;
+                    float wgt, wgt2;
+                    if constexpr (BATCH) {
+                        const float2 wt = B.wts[rr];
+                        wgt = wt.x;
+                        wgt2 = wt.y;
+                    } else {
+                        const double *dr = a.dirs + 6 * (size_t)(k0 + rr);
+                        wgt = (float)dr[4];
+                        wgt2 = (float)dr[5];
+                    }
+                    // the incoming intensity: B(T_star) for a star ray (inverse_rt.f90:113-118),
+                    // the ray's flag read from shared memory where it is used
+                    auto bb_in = [&](int l) -> float {
+                        if constexpr (BATCH) {
+                            const volatile unsigned *vsm = &B.smask;
+                            return ((*vsm >> rr) & 1u) ? a.bbs[l] : a.bb[l];
+                        } else {
+                            return a.bb[l];
+                        }
+                    };
                     nseg += (unsigned long long)Kr;
                     const int2 w0 = wl[0];
                     // the remainder channel of this lane's line (RT): intensity, and
                     // its central-cell contributions to J0 (and J_eff, L*)
                     float Irem = 0.f, remJ = 0.f, remE = 0.f, remL = 0.f;
-                    if (RT && lane < a.L) Irem = bbin[lane];
+                    if (RT && lane < a.L) Irem = bb_in(lane);
                     for (int l0 = 0; l0 < a.L; l0 += NLG) {
                         // intensities of the lane's channels: slot pairs (s, s+1) in one
                         // float2 (packed FP32x2 arithmetic), an odd last slot in .x
@@ -397,7 +446,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
 #define IV(s, l) (((s) & 1) ? I2[(s) >> 1][l].y : I2[(s) >> 1][l].x)
 #pragma unroll
                         for (int l = 0; l < NLG; l++) {
-                            const float bb = (l0 + l < a.L) ? bbin[l0 + l] : 0.f;
+                            const float bb = (l0 + l < a.L) ? bb_in(l0 + l) : 0.f;
 #pragma unroll
                             for (int s2 = 0; s2 < NS; s2++) IV(s2, l) = bb;
                         }

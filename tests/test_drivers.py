@@ -241,6 +241,39 @@ def test_star_mode_end_to_end(case, tmp_path):
                                rtol=1e-6, atol=1e-30, equal_nan=True)
 
 
+@pytest.mark.gpu
+def test_pol_pops_binary_sidecar(case, tmp_path):
+    """PORTAL_POPS_BINARY=1: main_portal.x also writes pol_pops.bin, equal to
+    pol_pops.dat to the last bit; finish_portal.x reads it and writes the
+    same cube as from the text; a text file newer than the sidecar wins."""
+    import shutil
+    import time
+    d = str(tmp_path)
+    for name in ("model.pop", "grid.vtk", "molecule.dat", "dust.tab", "bvec.dat", "pol.dat"):
+        shutil.copy(os.path.join(case["d"], name), d)
+    c2 = dict(case, d=d, paths={k: os.path.join(d, os.path.basename(v)) for k, v in case["paths"].items()})
+    rc = case["rc"]
+    env = dict(PORTAL_BVEC_FILE=c2["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec))
+    r = _run(MAIN, c2, dict(env, PORTAL_POPS_BINARY="1"))
+    assert r.returncode == 0, r.stderr
+    text = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    raw = open(os.path.join(d, "pol_pops.bin"), "rb").read()
+    assert raw[:8] == b"PORTALPP"
+    rows, cols = np.frombuffer(raw[8:16], dtype="<i4")
+    binp = np.frombuffer(raw[16:], dtype="<f8").reshape(cols, rows).T
+    np.testing.assert_array_equal(binp, text)
+    lime.write_finish_input(os.path.join(d, "finish.dat"), [1], [2], [0.4], [0.1], 4, 80.0, 0.0, 6, 0.6)
+    r2 = _run(FINISH, c2, env, input_name="finish.dat")
+    assert r2.returncode == 0 and "pol_pops.bin" in r2.stdout, r2.stderr
+    _, from_bin = lime.read_fits(os.path.join(d, "inc01-trans01-im_i.fits"))
+    time.sleep(0.05)
+    os.utime(os.path.join(d, "pol_pops.dat"))  # the text is now newer: it wins
+    r3 = _run(FINISH, c2, env, input_name="finish.dat")
+    assert r3.returncode == 0 and "pol_pops.bin" not in r3.stdout, r3.stderr
+    _, from_text = lime.read_fits(os.path.join(d, "inc01-trans01-im_i.fits"))
+    np.testing.assert_array_equal(from_bin, from_text)
+
+
 _ROW_WRITER_CHECK = r"""
 #include <cstdio>
 #include <vector>
