@@ -207,8 +207,9 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
     bool verify = false;  // this pass is the plain pass that judges convergence
     while (it < max_iter) {
         long long nseg = 0;
+        int nfail = 0;
         const bool split = local_operator && !verify;
-        if ((rc = run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, &nseg, nullptr, split))) return rc;
+        if ((rc = run_radiation_field(c, nth, nph, nvel, gvec, dx, n_depth, &nseg, &nfail, split))) return rc;
         nseg_tot += nseg;
         int nsing = 0;
         if ((rc = run_solve_se(c, kmax, &nsing, false))) return rc;

@@ -316,8 +316,27 @@ int run_radiation_field(portal_ctx *c, int nth, int nph, int nvel, const double 
     timer_collect(c, T_LINETAB);
     timer_collect(c, T_RF);
     if (n_segments) *n_segments = (long long)cnt[1];
-    // failed nodes: count on the host from the status array only when asked
-    if (n_failed) *n_failed = 0;
+    // failed nodes, counted on the host from the status array when asked (the
+    // iterated node loop): a walk past n_depth or a star ray set past nth*nph
+    // is an error, as the reference stops there
+    if (n_failed) {
+        std::vector<int> st((size_t)c->N);
+        PCHECK(c, cudaMemcpyAsync(st.data(), c->status.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                  c->stream));
+        PCHECK(c, cudaStreamSynchronize(c->stream));
+        int nf = 0, first = -1, bits = 0;
+        for (int i = 0; i < c->N; i++)
+            if (st[i] & (PORTAL_NODE_DEPTH | PORTAL_NODE_STAR)) {
+                if (first < 0) first = i;
+                bits |= st[i];
+                nf++;
+            }
+        *n_failed = nf;
+        if (nf)
+            return set_err(c, (bits & PORTAL_NODE_DEPTH) ? PORTAL_ERR_DEPTH : PORTAL_ERR_ARG,
+                           std::string((bits & PORTAL_NODE_DEPTH) ? "node_count > n_depth" : "star rays > nth*nph") +
+                               " for " + std::to_string(nf) + " node(s), the first node " + std::to_string(first + 1));
+    }
     c->j_valid = true;
     c->ali_valid = split;
     return PORTAL_OK;

@@ -126,6 +126,31 @@ def test_n_depth_overflow_is_reported(ctx):
     with pytest.raises(pg.PortalError) as e:
         ctx.radiation_field(rc)
     assert e.value.code == -4
+    # the iterated node loop stops on it too (no pass runs on zeroed fields)
+    ctx.set_cloud(cloud)
+    with pytest.raises(pg.PortalError) as e:
+        ctx.lambda_iterate(rc, tol=1e-6, max_iter=3)
+    assert e.value.code == -4
+
+
+def test_star_rays_beyond_nth_nph_are_reported(ctx):
+    """A node so close to the star that star_all needs more than nth*nph
+    rays stops the reference (miscellaneous.f90:1181-1184): an error here,
+    with status bit PORTAL_NODE_STAR on that node."""
+    import portal_gb300 as pg
+    cloud, mol, rc = _small()
+    R = 0.05
+    r = np.linalg.norm(cloud.xyz[:cloud.bulk_node_num], axis=1)
+    assert ((r > R) & (r < 1.06 * R)).any()   # 8 x 8 directions cannot hold these nodes' rays
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    ctx.set_star((2500.0, R * cloud.tx, (0.0, 0.0, 0.0)))
+    try:
+        with pytest.raises(pg.PortalError) as e:
+            ctx.radiation_field(rc)
+        assert e.value.code == -2 and "star" in str(e.value)
+    finally:
+        ctx.set_star(None)
 
 
 def test_skipped_and_surface_nodes(ctx):
