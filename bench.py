@@ -67,19 +67,24 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_segment():
-    """DRAM bytes per ray segment of the radiation-field kernel, from the ncu
-    summary committed under profiles/ (None when absent)."""
+def profile_constant(key):
+    """A per-segment figure of the radiation-field kernel from the ncu summary
+    committed under profiles/ (a line "key: value"), None when absent."""
     p = os.path.join(ROOT, "profiles", "radiation_field_sphere262k.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("dram_bytes_per_segment:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def traffic_per_segment():
+    """DRAM bytes per ray segment of the radiation-field kernel (ncu)."""
+    return profile_constant("dram_bytes_per_segment")
 
 
 class ClockSampler:
@@ -387,6 +392,19 @@ def gpu_arm(args, rank, world, local_rank):
             "kernel": "k_radiation_field", "algorithmic_bytes_per_segment": b_seg,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "launch_ms": rf_launch_ms, "segments_per_launch": nseg_step}
+    # the kernel's actual bound is instruction issue (its data is L2-resident):
+    # warp instructions per segment (ncu, profiles/) x segments / launch time
+    # against one warp instruction per SMSP per cycle at the sampled SM clock
+    wips = profile_constant("warp_instructions_per_segment")
+    if wips and clk and clk.get("sm_mhz"):
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ipeak = sms * 4 * float(clk["sm_mhz"]) * 1e6
+        iach = wips * nseg_step / (rf_launch_ms * 1e-3)
+        roof["issue"] = {"achieved": iach, "peak": ipeak, "unit": "warp instructions/s", "frac": iach / ipeak,
+                         "warp_instructions_per_segment": wips,
+                         "peak_source": "%d SMs x 4 schedulers x 1 instruction/cycle at %.0f MHz" %
+                                        (sms, float(clk["sm_mhz"]))}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_total_ms / args.steps, "higher_is_better": True,

@@ -151,7 +151,7 @@ int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J
  * >= 3 adds Ng acceleration (no reference counterpart): after every
  * ng_period passes the state moves to the order-2 Ng extrapolation of the
  * last four iterates of rho^0_0 (weights 1/rho^2), clipped to positive
- * values and renormalised per node; convergence is still judged by the
+ * values and renormalised per node; convergence is still decided by the
  * change of one plain pass.  local_operator != 0 (no reference counterpart)
  * makes the passes accelerated Lambda iterations: the radiation-field
  * kernel also splits J^0_0 = J_eff + L* S at each node's own cell (L* the
@@ -330,7 +330,7 @@ int portal_batch_config(const portal_batch *batch, int *config, double *tune, in
  *
  * A small MLP maps per-node features of the cloud and of the first
  * radiation field to the converged level populations, which then start
- * portal_lambda_iterate (start_pops); the plain iteration stays the judge of
+ * portal_lambda_iterate (start_pops); the plain iteration still decides
  * convergence, so the fixed point it reaches is unchanged.  The network is
  * n_in -> width (SiLU) x depth -> n_out (linear), FP32 master parameters,
  * BF16 operands and FP32 accumulation on the tensor cores in every GEMM of

@@ -15,7 +15,7 @@
 // Optional Ng acceleration (ng_period > 0): after every ng_period plain
 // passes the state jumps to the order-2 Ng extrapolation of the last four
 // iterates (Ng 1974, J. Chem. Phys. 61, 2680; the form of Olson, Auer &
-// Buchler 1986, JQSRT 35, 431).  Convergence is still judged by the plain
+// Buchler 1986, JQSRT 35, 431).  Convergence is still decided by the plain
 // pass alone (the change one radiation field + SE pass makes), so the state
 // it stops at is a fixed point of the plain iteration to tol.
 //
@@ -204,7 +204,7 @@ extern "C" int portal_lambda_iterate(portal_ctx *c, int nth, int nph, int nvel, 
     long long nseg_tot = 0;
     int it = 0, rc = PORTAL_OK;
     double r = 1e300;
-    bool verify = false;  // this pass is the plain pass that judges convergence
+    bool verify = false;  // this pass is the plain pass that decides convergence
     while (it < max_iter) {
         long long nseg = 0;
         int nfail = 0;

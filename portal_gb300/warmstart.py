@@ -7,7 +7,7 @@ convergence; this module starts it closer to the answer.  A small MLP
 kernels) maps eight local features of a node -- the cloud's conditions and
 the first radiation field, ``Context.warmstart_features`` -- to that node's
 converged level populations and alignment.  The iteration then starts from
-the prediction; it alone judges convergence, so the fixed point it stops at
+the prediction; it alone decides convergence, so the fixed point it stops at
 is the one it reaches without the network.
 
 Targets per node (2 nlev values): log10 x_J, the fractional population of
