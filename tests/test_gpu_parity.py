@@ -117,6 +117,34 @@ def _small(n=2048, nlev=5, seed=5, **kw):
     return cloud, mol, rc
 
 
+def test_two_collision_partners(ctx):
+    """c_par = 2 (para and ortho H2 in LAMDA files such as the reference's
+    CO_coro_v2.dat): rates mixed 25 % / 75 % after the temperature
+    interpolation (miscellaneous.f90:331-360); the populations of the same J
+    equal the oracle's to 1e-10."""
+    import dataclasses
+    import oracle
+    cloud, mol, rc = _small(1024, t_law="loglinear")
+    T = mol.col_temps[None, :]
+    C2 = np.concatenate([0.5 * mol.C * (1.0 + T / 50.0), 2.0 * mol.C * (1.0 + T / 200.0)], axis=0)
+    mol2 = dataclasses.replace(mol, C=C2)
+    assert mol2.c_par == 2
+    P = oracle.OracleProblem(cloud, mol2)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc)
+    opp, _, _ = P.solve_se(rc.kmax, oJ0, oJ2)
+    ctx.set_molecule(mol2)
+    ctx.set_cloud(cloud)
+    pops, st = ctx.solve_se(rc.kmax, oJ0, oJ2)
+    bulk = cloud.bulk_node_num
+    scale = np.abs(opp[:bulk, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pops[:bulk, 0::2] - opp[:bulk, 0::2]) / scale).max() < 1e-10
+    assert (np.abs(pops[:bulk, 1::2] - opp[:bulk, 1::2]) / scale).max() < 1e-10
+    # the second partner matters: the one-partner molecule gives other populations
+    P1 = oracle.OracleProblem(cloud, mol)
+    opp1, _, _ = P1.solve_se(rc.kmax, oJ0, oJ2)
+    assert np.abs(opp1[:bulk, 0::2] - opp[:bulk, 0::2]).max() > 1e-3 * np.abs(opp[:bulk, 0::2]).max()
+
+
 def test_n_depth_overflow_is_reported(ctx):
     import portal_gb300 as pg
     cloud, mol, rc = _small()
