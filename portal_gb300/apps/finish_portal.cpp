@@ -9,8 +9,9 @@
 // sidecar pol_pops.bin when that is present and not older) and writes, per
 // line i and inclination j, inc{j}-trans{i}-im_{i,q,u,tau}.fits and the
 // centre-channel dust maps inc{j}-trans{i}-dust_{i,q,u,tau}.fits
-// (para_finish.f90:460-616), I, Q and U scaled by I_to_T = 3.255e39/nu0^2.
-// With fits = 0 the .dat maps of the same routine are written instead.
+// (para_finish.f90:460-652), I, Q and U scaled by I_to_T = 3.255e39/nu0^2.
+// With fits = 0 the .dat maps of the same routine are written instead: one
+// file per channel of FP64 rows, the dust maps included.
 // pix_mod = 0 (para_finish.f90:245-350): per inclination j the node positions
 // inc{j}-xy.dat, then per line i, inclination j and channel k the per-node
 // rows inc{j}-trans{i}-vel{k}-im.dat (I_to_T I, I_to_T Q, I_to_T U, tau); the
@@ -155,29 +156,34 @@ int main(int argc, char **argv) {
             for (int k = 0; k < 8; k++) {
                 const bool dustmap = k >= 4;
                 const bool scale = (k % 4) != 3;
-                const int nv = dustmap ? 1 : nch;
-                std::vector<float> a((size_t)npx * npx * nv);
-                for (int c3 = 0; c3 < nv; c3++) {
-                    const int ch = dustmap ? in.nvel : c3;  // dust: centre channel only
-                    for (size_t p = 0; p < (size_t)npx * npx; p++) {
-                        const double v = q[k][p + (size_t)npx * npx * (ch + (size_t)nch * i)];
-                        a[p + (size_t)npx * npx * c3] = (float)(scale ? I_to_T * v : v);
-                    }
-                }
-                char name[160];
+                // the value the reference forms, I_to_T times the Stokes value
+                // (para_finish.f90:477-480, :583-586)
+                auto val = [&](size_t p, int ch) {
+                    const double v = q[k][p + (size_t)npx * npx * (ch + (size_t)nch * i)];
+                    return scale ? I_to_T * v : v;
+                };
                 if (in.fits == 1) {
-                    snprintf(name, sizeof name, "%s/inc%02d-trans%02d-%s.fits", out.c_str(), j + 1, i + 1, names[k]);
+                    // REAL*4 cubes; the dust maps hold the centre channel only (:592-613)
+                    const int nv = dustmap ? 1 : nch;
+                    std::vector<float> a((size_t)npx * npx * nv);
+                    for (int c3 = 0; c3 < nv; c3++) {
+                        const int ch = dustmap ? in.nvel : c3;
+                        for (size_t p = 0; p < (size_t)npx * npx; p++) a[p + (size_t)npx * npx * c3] = (float)val(p, ch);
+                    }
+                    const std::string name = out + "/inc" + i2(j + 1) + "-trans" + i2(i + 1) + "-" + names[k] + ".fits";
                     if (!write_fits(name, a.data(), npx, nv, (float)nu0, (float)ang, (float)(in.im_pix + 1),
                                     (float)(-ang), (float)(in.im_pix + 1), (float)in.dvel, (float)(in.nvel + 1),
                                     0.f, 0.f, 0.f))
-                        return fail(std::string("cannot write ") + name);
+                        return fail("cannot write " + name);
                 } else {
-                    for (int c3 = 0; c3 < nv; c3++) {
-                        snprintf(name, sizeof name, "%s/inc%02d-trans%02d-vel%02d-%s.dat", out.c_str(), j + 1, i + 1,
-                                 c3 + 1, names[k]);
-                        std::vector<double> rows((size_t)npx * npx);
-                        for (size_t p = 0; p < rows.size(); p++) rows[p] = a[p + (size_t)npx * npx * c3];
-                        if (!write_rows(name, rows, npx, npx)) return fail(std::string("cannot write ") + name);
+                    // list-directed rows of FP64 values, one file per channel, the dust
+                    // maps too (:513-545, :619-650)
+                    std::vector<double> rows((size_t)npx * npx);
+                    for (int c3 = 0; c3 < nch; c3++) {
+                        const std::string name = out + "/inc" + i2(j + 1) + "-trans" + i2(i + 1) + "-vel" + i2(c3 + 1) +
+                                                 "-" + names[k] + ".dat";
+                        for (size_t p = 0; p < rows.size(); p++) rows[p] = val(p, c3);
+                        if (!write_rows(name, rows, npx, npx)) return fail("cannot write " + name);
                     }
                 }
             }

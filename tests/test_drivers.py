@@ -242,6 +242,40 @@ def test_star_mode_end_to_end(case, tmp_path):
 
 
 @pytest.mark.gpu
+def test_finish_portal_dat_maps(case, tmp_path):
+    """fits = 0: one list-directed .dat file per inclination, line and
+    channel for each of I, Q, U, tau and the dust I, Q, U, tau (dust maps in
+    every channel, unlike the FITS path's centre channel), FP64 rows
+    I_to_T x the cube, names with Fortran's i2.2 numbers."""
+    import shutil
+    import portal_gb300 as pg
+    d = str(tmp_path)
+    for name in ("model.pop", "grid.vtk", "molecule.dat", "dust.tab", "bvec.dat", "pol.dat"):
+        shutil.copy(os.path.join(case["d"], name), d)
+    c2 = dict(case, d=d, paths={k: os.path.join(d, os.path.basename(v)) for k, v in case["paths"].items()})
+    cloud, mol, rc = case["cloud"], case["mol"], case["rc"]
+    env = dict(PORTAL_BVEC_FILE=c2["paths"]["bvec"], PORTAL_GVEC=" ".join(repr(g) for g in rc.gvec))
+    assert _run(MAIN, c2, env).returncode == 0
+    pops_file = np.loadtxt(os.path.join(d, "pol_pops.dat"))
+    nvel, im_pix = 2, 5
+    lime.write_finish_input(os.path.join(d, "finish.dat"), [1], [2], [0.5], [0.0], nvel, 90.0, 0.0, im_pix, 0.6,
+                            fits=0)
+    r = _run(FINISH, c2, env, input_name="finish.dat")
+    assert r.returncode == 0, r.stderr
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        ctx.set_cloud(cloud)
+        cube, _ = ctx.image([1], [2], 0.5, 0.0, nvel, 90.0, 0.0, im_pix, 0.6, pol_pops=pops_file)
+    I_to_T = 3.255e39 / (mol.e_levs[1] - mol.e_levs[0]) ** 2
+    names = ["im_i", "im_q", "im_u", "im_tau", "dust_i", "dust_q", "dust_u", "dust_tau"]
+    for k in range(2 * nvel + 1):
+        for q, nm in enumerate(names):
+            got = np.loadtxt(os.path.join(d, "inc01-trans01-vel%02d-%s.dat" % (k + 1, nm)))
+            want = cube[q, 0, k].astype(np.float64).T * (1.0 if q % 4 == 3 else I_to_T)
+            np.testing.assert_allclose(got, want, rtol=1e-15, atol=0, equal_nan=True)
+
+
+@pytest.mark.gpu
 def test_pol_pops_binary_sidecar(case, tmp_path):
     """PORTAL_POPS_BINARY=1: main_portal.x also writes pol_pops.bin, equal to
     pol_pops.dat to the last bit; finish_portal.x reads it and writes the
