@@ -35,6 +35,37 @@ def test_python_mirror_binds_every_declared_symbol(built_lib):
     assert set(declared_symbols()) <= set(pg.EXPORTS)
 
 
+def _c_param_counts():
+    text = open(os.path.join(ROOT, "include", "portal_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(portal_\w+)\s*\(([^;{]*?)\)\s*;", text):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_fortran_interface_matches_header():
+    """include/portal_gb300.f90 (the ISO_C_BINDING module a Fortran caller
+    uses): every bind(C) name is a header entry point with the same number of
+    arguments, and every dummy argument has a declaration."""
+    f = re.sub(r"!.*", "", open(os.path.join(ROOT, "include", "portal_gb300.f90")).read())
+    f = f.replace("&\n", " ").replace("&", " ")
+    c = _c_param_counts()
+    found = 0
+    for m in re.finditer(r"function\s+(\w+)\s*\(([^)]*)\)\s*bind\(C,\s*name=\"(\w+)\"\)(.*?)end function", f,
+                         flags=re.S):
+        name, args, cname, body = m.group(1), m.group(2), m.group(3), m.group(4)
+        assert name == cname and cname in c, cname
+        dummies = [a.strip() for a in args.split(",") if a.strip()]
+        assert len(dummies) == c[cname], (cname, len(dummies), c[cname])
+        declared = set(re.findall(r"::\s*([^\n]+)", body))
+        names = {v.strip() for d in declared for v in re.sub(r"\([^)]*\)", "", d).split(",")}
+        assert set(dummies) <= names, (cname, set(dummies) - names)
+        found += 1
+    assert found >= 10
+
+
 def test_create_without_device_fails_loudly(built_lib):
     """No silent CPU path: without an sm_103a device portal_create refuses."""
     import portal_gb300 as pg
