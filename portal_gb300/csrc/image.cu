@@ -167,6 +167,48 @@ __device__ __forceinline__ float phi1(float x) {  // (1 - e^-x)/x, stable near 0
     return (1.f - expf(-x)) / x;
 }
 
+// Exponent of the lowest set bit of a double (v = m 2^e with m odd); a large
+// value for 0, which constrains nothing.
+__device__ __forceinline__ int lsb_exp(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+    if (b == 0ULL) return 1 << 20;
+    int ex = (int)(b >> 52);
+    unsigned long long m = b & 0xfffffffffffffULL;
+    if (ex) {
+        m |= 1ULL << 52;
+        ex -= 1075;
+    } else {
+        ex = -1074;
+    }
+    return ex + __ffsll((long long)m) - 1;
+}
+
+// n successive FP64 additions z = z + dx, bit for bit, in O(binades) steps.
+// While every partial sum z + j dx is representable -- all of them are
+// multiples of g = min(lsb(z), lsb(dx)), so each is exact as long as its
+// magnitude stays below L = g 2^53 -- the additions are exact and their
+// result is the single correctly rounded fma(m, dx, z) (m dx itself is exact:
+// dx is the REAL*4 step, a 24-bit mantissa, and m < 2^29).  Only a sum that
+// enters a binade whose spacing exceeds g can round; that one addition is
+// made as the reference makes it, after which z lies on the coarser grid.
+__device__ double add_steps(double z, long long n, double dx, int e_dx) {
+    while (n > 0) {
+        const int eg = min(lsb_exp(z), e_dx);
+        const double L = ldexp(1.0, eg + 53);
+        long long m = (long long)floor(__ddiv_rn(__dsub_rn(L, z), dx)) - 2;  // z + m dx < L, with margin
+        if (m > n) m = n;
+        if (m > 0) {
+            z = __fma_rn((double)m, dx, z);
+            n -= m;
+        }
+        if (n > 0) {
+            z = __dadd_rn(z, dx);
+            n--;
+        }
+    }
+    return z;
+}
+
 __device__ double black_body(double T, double nu) {
     if (T == 0.0) return 0.0;
     return 1.4744995e-50 * nu * nu * nu / (exp(4.79924e-11 / T * nu) - 1.0);
@@ -179,6 +221,7 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int2 *const wbase = a.walk + (size_t)gw * 32 * (size_t)a.n_depth;
     const int npix = a.nrays;
+    const int e_dx = lsb_exp(a.dx);
     for (;;) {
         int p0 = 0;
         if (lane == 0) p0 = (int)atomicAdd(&a.counters[0], 32ULL);
@@ -257,7 +300,10 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                     else if (dzn > 0.0) zt = fmin(zt, A / (2.0 * dzn));
                 }
                 long long kt = (long long)floor((zt - z0) / a.dx) - 3;
-                while ((long long)k < kt) { z = z + a.dx; k++; }   // the reference's own additions
+                if ((long long)k < kt) {  // the reference's own additions, in jumps
+                    z = add_steps(z, kt - k, a.dx, e_dx);
+                    k = (int)kt;
+                }
                 // exact replay of trace_out_raytrace's loop until c changes or the ray exits
                 bool done = false, changed = false;
                 while (!done && !changed) {
