@@ -288,6 +288,14 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 const double cc = cx * cx + cy * cy + cz * cz;
                 double zt = zexit;
                 const int o = a.off[c], deg = a.off[c + 1] - o;
+                // Candidates of the replay below: the neighbours (of the first 64)
+                // that come within 1e-12 of c's squared distance somewhere up to
+                // z_lim.  Every other neighbour stays farther than c by more than
+                // the FP64 rounding of both squared distances (~1e-15), so it
+                // cannot win check_neigh's strict comparison and skipping it leaves
+                // the scan's outcome unchanged.
+                const double WIN = 6.0 * a.dx;
+                unsigned long long cand = 0ULL;
                 for (int j = 0; j < deg; j++) {
                     const int nb = a.idx[o + j];
                     const double nx = a.xyz[3 * (size_t)nb], ny = a.xyz[3 * (size_t)nb + 1],
@@ -296,9 +304,17 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                     const double dzn = nz - cz;
                     const double A = (nx * nx + ny * ny + nz * nz) - cc - 2.0 * x * (nx - cx) -
                                      2.0 * y * (ny - cy);
-                    if (A - 2.0 * z * dzn < 1e-12) zt = z;   // already (nearly) nearer: replay now
-                    else if (dzn > 0.0) zt = fmin(zt, A / (2.0 * dzn));
+                    if (A - 2.0 * z * dzn < 1e-12) {   // already (nearly) nearer: replay now
+                        zt = z;
+                        if (j < 64) cand |= 1ULL << j;
+                    } else if (dzn > 0.0) {
+                        zt = fmin(zt, A / (2.0 * dzn));
+                        // A - 2 z' dzn <= 1e-12 for some z' <= zt + WIN (zt only falls
+                        // further in this loop, so the set is a superset)
+                        if (j < 64 && A - 1e-12 <= 2.0 * (zt + WIN) * dzn) cand |= 1ULL << j;
+                    }
                 }
+                const double z_lim = zt + WIN;
                 long long kt = (long long)floor((zt - z0) / a.dx) - 3;
                 if ((long long)k < kt) {  // the reference's own additions, in jumps
                     z = add_steps(z, kt - k, a.dx, e_dx);
@@ -315,15 +331,22 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                         dl[nc++] = make_int2(c, k);
                         done = true;
                     }
-                    // check_neigh miscellaneous.f90:1-46
+                    // check_neigh miscellaneous.f90:1-46, in list order: the candidates
+                    // while z <= z_lim (and every neighbour past the 64th), else all
                     double d0 = dsum3sq(x - cx, y - cy, z - cz);
                     int nn = c;
-                    for (int j = 0; j < deg; j++) {
+                    auto probe = [&](int j) {
                         const int nb = a.idx[o + j];
                         const double ex = x - a.xyz[3 * (size_t)nb], ey = y - a.xyz[3 * (size_t)nb + 1],
                                      ez = z - a.xyz[3 * (size_t)nb + 2];
                         const double dd = dsum3sq(ex, ey, ez);
                         if (dd < d0) { d0 = dd; nn = nb; }
+                    };
+                    if (z <= z_lim) {
+                        for (unsigned long long m = cand; m; m &= m - 1ULL) probe(__ffsll((long long)m) - 1);
+                        for (int j = 64; j < deg; j++) probe(j);
+                    } else {
+                        for (int j = 0; j < deg; j++) probe(j);
                     }
                     if (nn != c) {
                         if (nc >= a.n_depth) { st = 1; break; }
