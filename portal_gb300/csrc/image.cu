@@ -20,10 +20,13 @@
 //                     march along +z.  The step at which a neighbour becomes
 //                     nearer is predicted from the bisector-plane crossing,
 //                     the photon's z is advanced by the reference's own
-//                     sequence of FP64 additions, and check_neigh is replayed
-//                     exactly (FP64, strict <, list order) around each
-//                     predicted change and at the exit, so the recorded
-//                     (node, step) list is the reference's;
+//                     sequence of FP64 additions (computed in exact jumps,
+//                     add_steps), and check_neigh is replayed exactly (FP64,
+//                     strict <, list order) around each predicted change and
+//                     at the exit -- over the neighbours that can come within
+//                     1e-12 of the current node's squared distance before the
+//                     next predicted change, the others being unable to win
+//                     -- so the recorded (node, step) list is the reference's;
 //                 (2) per pixel, lanes over velocity channels, lines looped:
 //                     the polarized propagation in the numerically stable
 //                     form o11 = (phi(p)+phi(m))/2, o12 = -(phi(p)-phi(m))/2,
