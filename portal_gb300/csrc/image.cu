@@ -62,6 +62,7 @@ struct ImNodeArgs {
     const double *xyz, *vel, *bvec, *b, *tdust, *levp, *pops_in;
     const int *j_lev;
     double *xyz_r;            // (3,N) rotated positions
+    double *nrm2;             // (N) |X|^2 of the rotated positions (the march's predictions)
     float4 *cellv;            // (vz, 1/b, cos 2alpha, sin 2alpha)
     float4 *cellb;            // (mu2, cos 2phi, sin 2phi, dust rho)
     float4 *coef;             // (nlines, N): eta_I, eta_Q, eps_I, eps_Q per step / (b sqrt(pi)) / peak
@@ -84,6 +85,7 @@ __global__ void k_im_nodes(ImNodeArgs a) {
         x[j] = sx; v[j] = sv; bb[j] = sb;
     }
     for (int j = 0; j < 3; j++) a.xyz_r[3 * (size_t)n + j] = x[j];
+    a.nrm2[n] = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
     // rot_stokes: alpha = acos(chi_y), negative when chi_x > 0
     const double cn = sqrt(bb[0] * bb[0] + bb[1] * bb[1]);
     const double chx = bb[0] / cn, chy = bb[1] / cn;
@@ -155,6 +157,7 @@ struct ImArgs {
     double Rs, sx, sy, sz;   // R_star / tx and the rotated star position
     double im_size, dx, tdx, alpha, dvel, v0;
     const double *xyz;       // rotated (3,N)
+    const double *nrm2;      // |X|^2 per node
     const int *off, *idx;    // neighbour CSR
     const float4 *cellv, *cellb, *coef;
     const double *dust_p, *tdust;
@@ -288,8 +291,7 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 // predicted first step at which a neighbour is nearer than c
                 const double cx = a.xyz[3 * (size_t)c], cy = a.xyz[3 * (size_t)c + 1],
                              cz = a.xyz[3 * (size_t)c + 2];
-                const double cc = cx * cx + cy * cy + cz * cz;
-                double zt = zexit;
+                const double cc = a.nrm2[c];
                 const int o = a.off[c], deg = a.off[c + 1] - o;
                 // Candidates of the replay below: the neighbours (of the first 64)
                 // that come within 1e-12 of c's squared distance somewhere up to
@@ -299,24 +301,32 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
                 // the scan's outcome unchanged.
                 const double WIN = 6.0 * a.dx;
                 unsigned long long cand = 0ULL;
+                // the predicted crossing zt = tn / td, the minimum of A / (2 dzn) kept
+                // as a fraction (compared by cross-multiplication, one division at the end)
+                double tn = zexit, td = 1.0;
                 for (int j = 0; j < deg; j++) {
                     const int nb = a.idx[o + j];
                     const double nx = a.xyz[3 * (size_t)nb], ny = a.xyz[3 * (size_t)nb + 1],
                                  nz = a.xyz[3 * (size_t)nb + 2];
                     // |P-X_n|^2 - |P-X_c|^2 = A - 2 z dzn along the ray
                     const double dzn = nz - cz;
-                    const double A = (nx * nx + ny * ny + nz * nz) - cc - 2.0 * x * (nx - cx) -
-                                     2.0 * y * (ny - cy);
+                    const double A = a.nrm2[nb] - cc - 2.0 * x * (nx - cx) - 2.0 * y * (ny - cy);
                     if (A - 2.0 * z * dzn < 1e-12) {   // already (nearly) nearer: replay now
-                        zt = z;
+                        tn = z;
+                        td = 1.0;
                         if (j < 64) cand |= 1ULL << j;
                     } else if (dzn > 0.0) {
-                        zt = fmin(zt, A / (2.0 * dzn));
+                        const double d2 = 2.0 * dzn;
+                        if (A * td < tn * d2) {
+                            tn = A;
+                            td = d2;
+                        }
                         // A - 2 z' dzn <= 1e-12 for some z' <= zt + WIN (zt only falls
                         // further in this loop, so the set is a superset)
-                        if (j < 64 && A - 1e-12 <= 2.0 * (zt + WIN) * dzn) cand |= 1ULL << j;
+                        if (j < 64 && (A - 1e-12) * td <= d2 * (tn + WIN * td)) cand |= 1ULL << j;
                     }
                 }
+                const double zt = tn / td;
                 const double z_lim = zt + WIN;
                 long long kt = (long long)floor((zt - z0) / a.dx) - 3;
                 if ((long long)k < kt) {  // the reference's own additions, in jumps
@@ -552,13 +562,13 @@ static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const i
             na.R[i + 3 * j] = s;
         }
     // device buffers
-    DevBuf<double> xyz_r, pops_d, vel_d;
+    DevBuf<double> xyz_r, pops_d, vel_d, nrm2;
     DevBuf<int> jl;
     DevBuf<float4> cellv, cellb, coef;
     DevBuf<float> outd;
     DevBuf<int> stat;
     const size_t cube = (size_t)nrays * nch * nlines;
-    if (xyz_r.reserve(3 * (size_t)N) || cellv.reserve(N) || cellb.reserve(N) ||
+    if (xyz_r.reserve(3 * (size_t)N) || nrm2.reserve(N) || cellv.reserve(N) || cellb.reserve(N) ||
         coef.reserve((size_t)nlines * N) || jl.reserve(nlev) || stat.reserve((size_t)(nrays > 0 ? nrays : 1)))
         return set_err(c, PORTAL_ERR_NOMEM, "image buffers");
     const double *pops_src = c->pops.p;
@@ -572,7 +582,7 @@ static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const i
     na.N = N; na.bulk = c->bulk; na.nlev = nlev; na.nlines = nlines; na.tdx = c->tx * dx;
     na.xyz = c->pos64.p; na.vel = c->vel64.p; na.bvec = c->bvec64.p; na.b = c->b64.p;
     na.tdust = c->tdust.p; na.levp = c->levp.p; na.pops_in = pops_src; na.j_lev = jl.p;
-    na.xyz_r = xyz_r.p; na.cellv = cellv.p; na.cellb = cellb.p; na.coef = coef.p;
+    na.xyz_r = xyz_r.p; na.nrm2 = nrm2.p; na.cellv = cellv.p; na.cellb = cellb.p; na.coef = coef.p;
     timer_start(c, T_EMCOEF);
     k_im_nodes<<<(N + 127) / 128, 128, 0, c->stream>>>(na);
     timer_stop(c, T_EMCOEF);
@@ -595,7 +605,7 @@ static int image_call(portal_ctx *c, const double *pol_pops, int nlines, const i
         ia.sx = sp[0]; ia.sy = sp[1]; ia.sz = sp[2];
     }
     ia.n_depth = n_depth_rt; ia.im_size = im_size; ia.dx = dx; ia.tdx = c->tx * dx; ia.alpha = alpha; ia.dvel = dvel; ia.v0 = v0;
-    ia.xyz = xyz_r.p; ia.off = c->nb_off.p; ia.idx = c->nb_idx.p; ia.cellv = cellv.p; ia.cellb = cellb.p;
+    ia.xyz = xyz_r.p; ia.nrm2 = nrm2.p; ia.off = c->nb_off.p; ia.idx = c->nb_idx.p; ia.cellv = cellv.p; ia.cellb = cellb.p;
     ia.coef = coef.p; ia.dust_p = c->dustp.p; ia.tdust = c->tdust.p; ia.status = stat.p;
     {
         int q2 = 0;
