@@ -76,6 +76,24 @@ def test_input_file_line_shift_is_reproduced(case):
     np.testing.assert_allclose(b, ref, rtol=0, atol=1e-14)
 
 
+def test_executables_fail_loudly_without_a_gpu(case):
+    """No CPU path in the drop-ins either: without an sm_103a device both
+    executables stop with the library's error after parsing, and write no
+    output."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    env = dict(PORTAL_BVEC_FILE=case["paths"]["bvec"])
+    out = os.path.join(case["d"], "pol_pops.dat")
+    before = os.path.getmtime(out) if os.path.exists(out) else None
+    r = _run(MAIN, case, env)
+    assert r.returncode != 0 and "portal_create" in r.stderr, (r.returncode, r.stderr)
+    assert (os.path.getmtime(out) if os.path.exists(out) else None) == before
+
+
 def test_fits_writer_roundtrip(tmp_path, built_lib):
     """writeimage's header keywords and big-endian float data
     (fits_writing.f90:57-149), read back by the repo's own parser."""
