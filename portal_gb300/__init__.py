@@ -24,7 +24,7 @@ P_D = C.POINTER(C.c_double)
 P_I = C.POINTER(C.c_int)
 
 PORTAL_OK = 0
-NODE_DEPTH, NODE_SINGULAR, NODE_REFINE = 1, 2, 4
+NODE_DEPTH, NODE_SINGULAR, NODE_REFINE, NODE_STAR = 1, 2, 4, 8
 KERNEL_SLOTS = ("line_table", "radiation_field", "solve_se", "emcoefs", "image_walk", "image_rt")
 
 EXPORTS = (
