@@ -3,6 +3,7 @@
 #include "portal_io.h"
 
 #include <algorithm>
+#include <cctype>
 #include <charconv>
 #include <cmath>
 #include <cstdint>
@@ -197,14 +198,47 @@ bool ListReader::read(std::vector<std::string> &out, size_t n) {
     return true;
 }
 
+// Fortran's list-directed READ stops the program on an item that is not a
+// number; the readers here fail the same way: to_double / to_int remember
+// the first token they cannot read whole, and every reader checks it.
+namespace {
+thread_local std::string g_bad;
+}
+
 double to_double(const std::string &tok) {
     std::string t = tok;
     for (auto &ch : t)
         if (ch == 'd' || ch == 'D') ch = 'e';
-    return strtod(t.c_str(), nullptr);
+    char *ep = nullptr;
+    double v = strtod(t.c_str(), &ep);
+    if (ep == t.c_str() || *ep != 0) {
+        // numeric input also takes an exponent given by its sign alone (1.5+3 = 1.5e3)
+        const size_t s = t.find_last_of("+-");
+        if (s != std::string::npos && s > 0 && (isdigit((unsigned char)t[s - 1]) || t[s - 1] == '.')) {
+            const std::string u = t.substr(0, s) + "e" + t.substr(s);
+            char *eu = nullptr;
+            const double w = strtod(u.c_str(), &eu);
+            if (eu != u.c_str() && *eu == 0) return w;
+        }
+        if (g_bad.empty()) g_bad = tok;
+    }
+    return v;
 }
 
-int to_int(const std::string &tok) { return (int)strtol(tok.c_str(), nullptr, 10); }
+int to_int(const std::string &tok) {
+    char *ep = nullptr;
+    const long v = strtol(tok.c_str(), &ep, 10);
+    if ((ep == tok.c_str() || *ep != 0) && g_bad.empty()) g_bad = tok;
+    return (int)v;
+}
+
+// false (with the message) when a token of `path` was not a number
+static bool numbers_ok(const std::string &path, std::string &err) {
+    if (g_bad.empty()) return true;
+    err = path + ": not a number: '" + g_bad + "'";
+    g_bad.clear();
+    return false;
+}
 
 bool ListReader::read_doubles(std::vector<double> &out, size_t n) {
     std::vector<std::string> t;
@@ -227,6 +261,7 @@ bool ListReader::read_ints(std::vector<int> &out, size_t n) {
 // ---------------------------------------------------------------------------
 
 bool read_main_input(const std::string &path, MainInput &in, std::string &err) {
+    g_bad.clear();
     ListReader r(path);
     if (!r.ok()) { err = "cannot open " + path; return false; }
     std::vector<std::string> t;
@@ -243,10 +278,11 @@ bool read_main_input(const std::string &path, MainInput &in, std::string &err) {
     in.kmax = to_int(t[0]); in.extra_info = to_int(t[1]);
     if (!r.read(t, 2)) { err = path + ": max_ne_temp n_depth"; return false; }
     in.max_ne_temp = to_int(t[0]); in.n_depth = to_int(t[1]);
-    return true;
+    return numbers_ok(path, err);
 }
 
 bool read_finish_input(const std::string &path, FinishInput &in, std::string &err) {
+    g_bad.clear();
     ListReader r(path);
     if (!r.ok()) { err = "cannot open " + path; return false; }
     std::vector<std::string> t;
@@ -276,7 +312,7 @@ bool read_finish_input(const std::string &path, FinishInput &in, std::string &er
     in.fits = to_int(t[0]); in.distance = to_double(t[1]);
     if (!r.read(t, 2)) { err = path + ": max_ne_temp n_depth_rt"; return false; }
     in.max_ne_temp = to_int(t[0]); in.n_depth_rt = to_int(t[1]);
-    return true;
+    return numbers_ok(path, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -289,6 +325,7 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     (void)dust_ii_gas;  // the per-node gas-to-dust column of the .pop is what eat_lime uses
     std::vector<std::string> t;
     std::vector<double> vd;
+    g_bad.clear();
     // ---- grid.vtk: points (eat_lime_dim eat_lime.f90:21-34, :124-136) ----
     ListReader g(grid);
     if (!g.ok()) { err = "cannot open " + grid; return false; }
@@ -359,6 +396,7 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     for (int i = 0; i < N; i++)
         for (int s2 = 0; s2 < c.del_num_ne[i]; s2++) c.del_ne[(size_t)i + (size_t)N * s2] = raw[(size_t)roff[i] + s2];
 
+    if (!numbers_ok(grid, err)) return false;
     // ---- LAMDA (eat_lime_dim :38-62, eat_lime_no_delaunay :151-196) ----
     ListReader f(mol);
     if (!f.ok()) { err = "cannot open " + mol; return false; }
@@ -425,6 +463,7 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
                 m.C[(size_t)k + (size_t)m.c_temp * (i + (size_t)m.c_num)] = to_double(t[3 + k]);
         }
     }
+    if (!numbers_ok(mol, err)) return false;
     // ---- .pop rows (eat_lime.f90:207-224) ----
     ListReader p(pop);
     if (!p.ok()) { err = "cannot open " + pop; return false; }
@@ -475,6 +514,7 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     }
     for (auto &v : c.xyz) v /= rmax;
     c.tx = rmax;
+    if (!numbers_ok(pop, err)) return false;
     // ---- dust table (eat_lime.f90:285-298, dust_to_opacities miscellaneous.f90:643-700) ----
     ListReader d(dust);
     if (!d.ok()) { err = "cannot open " + dust; return false; }
@@ -505,6 +545,7 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     c.dust_p.assign(N, 0.0);  // :302-311
     for (int i = 0; i < N; i++)
         if (g2d[i] != 0.0) c.dust_p[i] = c.h2_dens[i] * f4(2.32e-27) / g2d[i];
+    if (!numbers_ok(dust, err)) return false;
     // ---- main_para.f90:119-120, :178-185 ----
     for (auto &v : m.nu) v = f4(1e9) * v;
     for (auto &v : m.e_levs) v = f4(29.9792458e9) * v;
@@ -594,12 +635,14 @@ bool write_rows(const std::string &path, const std::vector<double> &cm, int rows
 }
 
 bool read_rows(const std::string &path, std::vector<double> &cm, int rows, int cols, std::string &err) {
+    g_bad.clear();
     ListReader r(path);
     if (!r.ok()) { err = "cannot open " + path; return false; }
     cm.assign((size_t)rows * cols, 0.0);
     std::vector<double> v((size_t)rows * cols);
     const size_t got = r.read_block_doubles(v.data(), (size_t)rows, (size_t)cols, io_threads());
     if (got < (size_t)rows) { err = path + ": row " + std::to_string(got + 1); return false; }
+    if (!numbers_ok(path, err)) return false;
     for (int i = 0; i < rows; i++)  // para_finish.f90:226-227
         for (int k = 0; k < cols; k++) cm[(size_t)i + (size_t)rows * k] = v[(size_t)i * cols + k];
     return true;

@@ -76,6 +76,69 @@ def test_input_file_line_shift_is_reproduced(case):
     np.testing.assert_allclose(b, ref, rtol=0, atol=1e-14)
 
 
+def _copy_case(case, tmp_path):
+    import shutil
+    d = str(tmp_path)
+    for name in ("model.pop", "grid.vtk", "molecule.dat", "dust.tab", "bvec.dat", "pol.dat"):
+        shutil.copy(os.path.join(case["d"], name), d)
+    return dict(case, d=d, paths={k: os.path.join(d, os.path.basename(v)) for k, v in case["paths"].items()})
+
+
+def _edit_line(path, lineno, fn):
+    with open(path) as f:
+        lines = f.readlines()
+    lines[lineno] = fn(lines[lineno])
+    with open(path, "w") as f:
+        f.writelines(lines)
+
+
+def test_garbled_numbers_stop_the_reader(case, tmp_path):
+    """An item that is not a number stops the reading, as Fortran's
+    list-directed READ stops the reference: in grid.vtk, in the .pop rows and
+    in the input file, each with the file and the token named; nothing is
+    ingested."""
+    c2 = _copy_case(case, tmp_path)
+    p = c2["paths"]
+    dd = os.path.join(c2["d"], "dump")
+    os.makedirs(dd, exist_ok=True)
+    cases = [
+        (p["grid"], 6, lambda l: "1.2.3 " + l.split(None, 1)[1], "1.2.3"),        # a POINTS row
+        (p["pop"], 5, lambda l: l.replace(l.split()[6], "12x4", 1), "12x4"),        # a .pop row's density
+        (os.path.join(c2["d"], "pol.dat"), 2, lambda l: "8 8x 16\n", "8x"),         # nth nph nvel
+    ]
+    for path, lineno, fn, tok in cases:
+        backup = open(path).read()
+        _edit_line(path, lineno, fn)
+        r = _run(MAIN, c2, dict(PORTAL_DUMP_INGESTED=dd))
+        assert r.returncode != 0, (path, r.stdout)
+        assert "not a number: '%s'" % tok in r.stderr and os.path.basename(path) in r.stderr, r.stderr
+        assert not os.listdir(dd)
+        with open(path, "w") as f:
+            f.write(backup)
+
+
+def test_sign_exponents_are_read(case, tmp_path):
+    """Numeric input takes an exponent given by its sign alone (1.25-1 is
+    0.125), as the reference's list-directed READ does; the general reader
+    path handles it (the parallel line parser falls back to it)."""
+    c2 = _copy_case(case, tmp_path)
+    grid = c2["paths"]["grid"]
+    with open(grid) as f:
+        lines = f.readlines()
+    i = next(k for k, l in enumerate(lines) if l.startswith("POINTS")) + 1
+    x0 = [float(v) for v in lines[i].split()]
+    lines[i] = "%s %s %s\n" % ("%.17g" % x0[0], "1.25-1", "-2.5+2")
+    with open(grid, "w") as f:
+        f.writelines(lines)
+    dd = os.path.join(c2["d"], "dump")
+    os.makedirs(dd, exist_ok=True)
+    r = _run(MAIN, c2, dict(PORTAL_DUMP_INGESTED=dd, PORTAL_BVEC_FILE=c2["paths"]["bvec"]))
+    assert r.returncode == 0, r.stderr
+    xyz = _npy(dd, "xyz").reshape(-1, 3)
+    tx = _npy(dd, "scalars")[0]
+    np.testing.assert_allclose(xyz[0, 1:] * tx, [0.125, -250.0], rtol=1e-15)
+
+
 def test_executables_fail_loudly_without_a_gpu(case):
     """No CPU path in the drop-ins either: without an sm_103a device both
     executables stop with the library's error after parsing, and write no
