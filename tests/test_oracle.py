@@ -272,3 +272,27 @@ def test_star_mode_node_loop_skips_the_star_and_ends_rays_on_it():
     pp, _, _ = Ps.solve_se(rc.kmax, J0, J2, 1, 64)
     assert (pp[inside] == 0).all() and (pp[near] != 0).any()
     assert (J0[near, 0] > J0n[near, 0]).all()
+
+
+def test_star_mode_image_starts_on_the_disc():
+    """raytrace.f90:103-115: pixels within R_star of the star's sky position
+    start at its front (less optical depth behind them, B(T_star) as the
+    input); every other pixel is the star-less image exactly."""
+    cloud, mol = _tiny_problem(512)
+    pp = np.zeros((cloud.node_num, 2 * mol.nlev))
+    g = np.sqrt(2.0 * mol.j_lev + 1.0)
+    pp[:, 0::2] = cloud.lev_p / cloud.lev_p.sum(axis=1, keepdims=True) / g
+    pp[:, 1::2] = 1e-3 * pp[:, 0::2]
+    R = 0.15
+    P0 = oracle.OracleProblem(cloud, mol)
+    Ps = oracle.OracleProblem(cloud, mol, star=(3000.0, R * cloud.tx, (0.0, 0.0, 0.0)))
+    im_pix, size = 4, 0.6
+    a, _, nf0 = P0.image([1], [2], pp, 0.4, 0.2, 3, 80.0, 0.0, im_pix, size)
+    b, _, nf1 = Ps.image([1], [2], pp, 0.4, 0.2, 3, 80.0, 0.0, im_pix, size)
+    assert nf0 == 0 and nf1 == 0
+    npx = 2 * im_pix + 1
+    ij = np.array([(i - im_pix, j - im_pix) for i in range(npx) for j in range(npx)]) * size / im_pix
+    on = np.hypot(ij[:, 0], ij[:, 1]) < R
+    assert on.sum() == 1 and (~on).sum() == npx * npx - 1
+    np.testing.assert_array_equal(a[:, ~on], b[:, ~on])
+    assert (b[3, on] < a[3, on]).all()          # tau: the ray starts at the star's front
