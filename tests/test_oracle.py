@@ -296,3 +296,81 @@ def test_star_mode_image_starts_on_the_disc():
     assert on.sum() == 1 and (~on).sum() == npx * npx - 1
     np.testing.assert_array_equal(a[:, ~on], b[:, ~on])
     assert (b[3, on] < a[3, on]).all()          # tau: the ray starts at the star's front
+
+
+def _rodrigues(n, th):
+    """rotmat (miscellaneous.f90:146-181): rotation by th about the unit n."""
+    c, s = math.cos(th), math.sin(th)
+    x, y, z = n
+    return np.array([[c + (1 - c) * x * x, x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                     [y * x * (1 - c) + z * s, c + (1 - c) * y * y, y * z * (1 - c) - x * s],
+                     [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + (1 - c) * z * z]])
+
+
+def test_node_field_against_an_independent_numpy_restatement():
+    """J^0_0 and J^2_0 of a few nodes from the oracle's inverse_rt against a
+    separate numpy restatement written from inverse_rt.f90:1-137 and ray_in
+    :217-344 (find_dir by explicit rotation matrices, the channel loop
+    vectorised), on the oracle's own walks: the two agree to 1e-12."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(384, t_law="loglinear", b_random=0.3)
+    rc = synth.RunConfig(nth=6, nph=6, nvel=6, kmax=2, gvec=synth.gauge_vector(2))
+    P = oracle.OracleProblem(cloud, mol)
+    J0, J2, st, _, nf = P.radiation_field(rc, 1, 12)
+    assert nf == 0
+    L = oracle.lib()
+    xth = oracle.legendre_all(rc.nth, rc.nph)
+    g = np.asarray(rc.gvec, dtype=np.float64)
+    dx = rc.dx
+    tdx = cloud.tx * dx
+    dl = np.zeros(2 * (rc.n_depth + 2), dtype=np.int32)
+    nc = C.c_int(0)
+    spi = math.sqrt(math.pi)
+    nvel = rc.nvel
+    for node in range(1, 13):
+        if not cloud.ab_all[node - 1] > 0:
+            continue
+        b = cloud.bvec[node - 1]
+        xv = np.cross(b, g)
+        xv /= np.linalg.norm(xv)
+        j0 = np.zeros(mol.r_num)
+        j2 = np.zeros(mol.r_num)
+        for mu, ph, w in xth:
+            d = _rodrigues(b, ph) @ (_rodrigues(xv, math.acos(mu)) @ b)
+            stt = L.orc_trace_out(C.byref(P.c), node, d.ctypes.data_as(oracle.P_D), C.c_double(dx), rc.n_depth,
+                                  dl.ctypes.data_as(oracle.P_I), C.byref(nc))
+            assert stt == 0
+            n = nc.value
+            cells = dl[0:2 * n:2] - 1
+            steps = dl[1:2 * n:2].astype(np.float64)
+            v_ray = cloud.vel[cells] @ d
+            v_node = cloud.vel[node - 1] @ d
+            c_in = (3.0 * mu * mu - 1.0) / 2.0
+            for k in range(mol.r_num):
+                lo, up = mol.r_trans[k] - 1
+                g1, g2 = 2 * mol.j_lev[lo] + 1, 2 * mol.j_lev[up] + 1
+                nu0 = mol.nu[k]
+                c1, c2, cnu = 2.2102191e-42 * nu0, 5.272859e-35 * nu0, 299792458.0 / nu0
+                kv = c1 * mol.Bij[k] * (cloud.lev_p[cells, lo] - g1 * cloud.lev_p[cells, up] / g2)
+                ev = c2 * mol.A[k] * cloud.lev_p[cells, up]
+                bn = cloud.b_all[node - 1]
+                nv = np.arange(-nvel, nvel + 1)
+                v0 = 2.0 * bn * nv / nvel
+                phi0 = np.exp(-(v0 / bn) ** 2) / (spi * bn)
+                v0 = v0 + v_node
+                I = np.full(nv.shape, oracle.black_body(2.73, nu0))
+                for i in range(n - 1, 0, -1):          # cells node_count .. 2
+                    bi = cloud.b_all[cells[i]]
+                    phi = cnu * np.exp(-((v0 - v_ray[i]) / bi) ** 2) / (spi * bi)
+                    tau = kv[i] * phi * tdx * (steps[i] - steps[i - 1])   # dust off
+                    upd = tau > 1e-30
+                    S = ev[i] / kv[i] if kv[i] != 0 else 0.0
+                    I = np.where(upd, I * np.exp(-tau) + S * (1.0 - np.exp(-tau)), I)
+                phin = phi0 * cnu
+                taun = kv[0] * phin * tdx * steps[0]
+                Iout = I * np.exp(-taun) + (ev[0] / kv[0]) * (1.0 - np.exp(-taun))
+                Ibar = np.sum(phi0 * Iout * (2.0 * bn / nvel))
+                j0[k] += Ibar * w
+                j2[k] += Ibar * w * c_in / math.sqrt(2.0)
+        np.testing.assert_allclose(j0, J0[node - 1], rtol=1e-12)
+        np.testing.assert_allclose(j2, J2[node - 1], rtol=1e-9, atol=1e-12 * np.abs(j0).max())
