@@ -374,3 +374,101 @@ def test_node_field_against_an_independent_numpy_restatement():
                 j2[k] += Ibar * w * c_in / math.sqrt(2.0)
         np.testing.assert_allclose(j0, J0[node - 1], rtol=1e-12)
         np.testing.assert_allclose(j2, J2[node - 1], rtol=1e-9, atol=1e-12 * np.abs(j0).max())
+
+
+def test_image_pixels_against_an_independent_numpy_restatement():
+    """I, Q, U, tau of image pixels from the oracle's finish_portal loop
+    against a second, numpy restatement written from para_finish.f90:222-240
+    (population read-back), rotate_all_save, comp_emcoefs (em_coefs.f90:1-113),
+    ray_in_raytrace (raytrace.f90:179-323) with rot_stokes / rot_stokes_back
+    and polarize_prop, on the oracle's marches: equal to 1e-11 of the peak."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(512, t_law="loglinear", b_random=0.4)
+    N, nlev = cloud.node_num, mol.nlev
+    rng = np.random.default_rng(3)
+    g = np.sqrt(2.0 * mol.j_lev + 1.0)
+    pp_in = np.zeros((N, 2 * nlev))
+    pp_in[:, 0::2] = cloud.lev_p / cloud.lev_p.sum(axis=1, keepdims=True) / g
+    pp_in[:, 1::2] = pp_in[:, 0::2] * rng.uniform(-0.02, 0.02, size=(N, nlev))
+    P = oracle.OracleProblem(cloud, mol)
+    th_inc, ph_az, nvel, dvel, v0, im_pix, size = 0.7, 0.4, 4, 90.0, 10.0, 3, 0.6
+    out, st, nf = P.image([1], [2], pp_in, th_inc, ph_az, nvel, dvel, v0, im_pix, size)
+    assert nf == 0
+    # rotate_all_save miscellaneous.f90:844-907: x' = R_z(ph) R_x(th) x
+    R = _rodrigues((0.0, 0.0, 1.0), ph_az) @ _rodrigues((1.0, 0.0, 0.0), th_inc)
+    X, V, B = cloud.xyz @ R.T, cloud.vel @ R.T, cloud.bvec @ R.T
+    # read-back para_finish.f90:226-239
+    pp = pp_in.copy()
+    pp[:, 0] = cloud.lev_p[:, 0] / g[0]
+    for i in range(1, nlev):
+        rat = pp_in[:, 2 * i + 1] / pp_in[:, 2 * i]
+        pp[:, 2 * i + 1] = rat * cloud.lev_p[:, i] / g[i]
+        pp[:, 2 * i] = cloud.lev_p[:, i] / g[i]
+    # comp_emcoefs of line (1, 2) for the bulk nodes with pp(:,1) != 0
+    j1, j2 = int(mol.j_lev[0]), int(mol.j_lev[1])
+    nu0 = mol.e_levs[1] - mol.e_levs[0]
+    Aji = mol.A[0]
+    fas = (-1.0) ** (1 + j1 + j2)
+    w1 = fas * math.sqrt(3.0 * (2 * j1 + 1)) * oracle.wigner6j(2, 2, 4, 2 * j1, 2 * j1, 2 * j2)
+    w2 = fas * math.sqrt(3.0 * (2 * j2 + 1)) * oracle.wigner6j(2, 2, 4, 2 * j2, 2 * j2, 2 * j1)
+    g1, g2 = 2.0 * j1 + 1, 2.0 * j2 + 1
+    coef = np.zeros((N, 4))
+    for n in range(cloud.bulk_node_num):
+        if pp[n, 0] == 0.0:
+            continue
+        th = math.acos(B[n, 2])
+        tki = (3.0 * math.cos(th) ** 2 - 1.0) / (2.0 * math.sqrt(2.0))
+        tkq = -3.0 * math.sin(th) ** 2 / (2.0 * math.sqrt(2.0))
+        r10, r20, r12, r22 = pp[n, 0], pp[n, 2], pp[n, 1], pp[n, 3]
+        naI, naQ = 1.0 + w1 * (r12 / r10) * tki, w1 * (r12 / r10) * tkq
+        nsI, nsQ = 1.0 + w2 * (r22 / r20) * tki, w2 * (r22 / r20) * tkq
+        Bji = Aji / (nu0 ** 3 / 6.781962e49)
+        hv = 5.273e-35 * nu0
+        coef[n] = [hv * (g2 / g1) * Bji * (math.sqrt(g1) * r10 * naI - math.sqrt(g2) * r20 * nsI * g1 / g2),
+                   hv * (g2 / g1) * Bji * (math.sqrt(g1) * r10 * naQ - math.sqrt(g2) * r20 * nsQ * g1 / g2),
+                   hv * Aji * nsI * math.sqrt(g2) * r20, hv * Aji * nsQ * math.sqrt(g2) * r20]
+    L = oracle.lib()
+    L.orc_trace_out_raytrace.restype = C.c_int
+    dx = synth.F4(1e-4)
+    Xf = np.ascontiguousarray(X, dtype=np.float64)
+    dl = np.zeros(2 * 10002, dtype=np.int32)
+    nc = C.c_int(0)
+    cnu = synth.F4(2.99792e8) / nu0
+    I_cmb = oracle.black_body(2.73, nu0)
+    npx = 2 * im_pix + 1
+    peak = np.abs(out[0]).max()
+    for p in (0, 5, 17, 24, 40):
+        a, b2 = p // npx - im_pix, p % npx - im_pix
+        x, y = a * size / im_pix, b2 * size / im_pix
+        assert L.orc_trace_out_raytrace(C.c_double(x), C.c_double(y), N, Xf.ctypes.data_as(oracle.P_D),
+                                        P.c.del_ne, P.c.del_num_ne, P.c.maxne, C.c_double(dx), 10000,
+                                        dl.ctypes.data_as(oracle.P_I), C.byref(nc)) == 0
+        n = nc.value
+        cells, steps = dl[0:2 * n:2] - 1, dl[1:2 * n:2]
+        vobs = np.arange(-nvel, nvel + 1) * dvel + v0
+        I = np.full(vobs.shape, I_cmb)
+        Qi, Ui, tau = np.zeros_like(I), np.zeros_like(I), np.zeros_like(I)
+        for i in range(n - 1):
+            c = cells[i]
+            vc = np.exp(-((vobs - V[c, 2]) ** 2) / cloud.b_all[c] ** 2) / (cloud.b_all[c] * math.sqrt(math.pi))
+            ch = np.array([B[c, 0], B[c, 1]]) / math.hypot(B[c, 0], B[c, 1])
+            al = math.acos(ch[1]) * (-1.0 if ch[0] > 0.0 else 1.0)
+            c2a, s2a = math.cos(2 * al), math.sin(2 * al)
+            Q, U = Qi * c2a + Ui * s2a, Ui * c2a - Qi * s2a          # rot_stokes
+            eI, eQ, sI, sQ = (cnu * vc * coef[c, q] for q in range(4))
+            ds = cloud.tx * dx * (steps[i + 1] - steps[i])
+            go = ds * eI > 1e-30
+            shQ, chQ, et = np.sinh(eQ * ds), np.cosh(eQ * ds), np.exp(-eI * ds)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                fac = 1.0 / (eI ** 2 - eQ ** 2)
+                o11 = fac * eI * (1.0 - (chQ + (eQ / eI) * shQ) * et)
+                o12 = -fac * eQ * (1.0 - (chQ + (eI / eQ) * shQ) * et)
+            In = o11 * sI + o12 * sQ + et * (chQ * I - shQ * Q)
+            Qn = o12 * sI + o11 * sQ + et * (-shQ * I + chQ * Q)
+            I, Q, U = np.where(go, In, I), np.where(go, Qn, Q), np.where(go, U * et, U)
+            tau = np.where(go, tau + eI * ds, tau)
+            Qi, Ui = Q * c2a - U * s2a, U * c2a + Q * s2a              # rot_stokes_back
+        got = out[:4, p, 0]
+        for q, want in enumerate((I - I_cmb, Qi, Ui)):
+            np.testing.assert_allclose(got[q], want, rtol=0, atol=1e-11 * peak)
+        np.testing.assert_allclose(got[3], tau, rtol=1e-12, atol=1e-300)
