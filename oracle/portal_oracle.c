@@ -1154,13 +1154,15 @@ int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const doub
                     size_t p1 = p0 + N;
                     int ca = count_array[i];
                     pol_pops[p0] = rhovec[ca];
-                    pol_pops[p1] = (m->j_lev[i] != 0) ? rhovec[ca + 1] : 0.0;
+                    /* with kmax = 0 the reference reads the next level's rho^0_0 here,
+                     * and past the end of rhovec for the last level (0 here) */
+                    pol_pops[p1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rhovec[ca + 1] : 0.0;
                     if (rates) {
                         for (int q = 0; q < 3; q++) {
                             size_t r0 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i));
                             size_t r1 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i + 1));
                             rates[r0] = rt[3 * ca + q];
-                            rates[r1] = (m->j_lev[i] != 0) ? rt[3 * (ca + 1) + q] : 0.0;
+                            rates[r1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rt[3 * (ca + 1) + q] : 0.0;
                         }
                     }
                     /* main_sub.f90:131-136 (the reference zeroes the same

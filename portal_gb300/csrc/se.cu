@@ -512,11 +512,15 @@ void build_program(const portal_ctx *c, int kmax, Program &P) {
         std::vector<int> fill(P.row_off.begin(), P.row_off.end() - 1);
         for (int e = 0; e < (int)P.ent_pos.size(); e++) P.row_ent[fill[P.ent_pos[e] % n]++] = e;
     }
-    // packing main_sub.f90:112-129
+    // packing main_sub.f90:112-129: the alignment of a J != 0 level is the
+    // component after its rho^0_0.  With kmax = 0 there is none, and the
+    // reference then reads the next level's rho^0_0 (and, for the last
+    // level, past the end of rhovec); the first is kept, the read past the
+    // end gives 0 here.
     P.pack.assign(2 * nlev, -1);
     for (int i = 0; i < nlev; i++) {
         P.pack[2 * i] = P.count_array[i];
-        if (J[i] != 0) P.pack[2 * i + 1] = P.count_array[i] + 1;
+        if (J[i] != 0 && P.count_array[i] + 1 < P.c_dim) P.pack[2 * i + 1] = P.count_array[i] + 1;
     }
 }
 

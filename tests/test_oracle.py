@@ -472,3 +472,54 @@ def test_image_pixels_against_an_independent_numpy_restatement():
         for q, want in enumerate((I - I_cmb, Qi, Ui)):
             np.testing.assert_allclose(got[q], want, rtol=0, atol=1e-11 * peak)
         np.testing.assert_allclose(got[3], tau, rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("kmax", [0, 6])
+def test_se_without_anisotropy_is_the_scalar_rate_equations(kmax):
+    """With J^2_0 = 0 the polarized SE (setup_stateq pop_eqs.f90:361-653 on
+    make_AC's rates) must give the textbook statistical equilibrium: level
+    populations n_J = sqrt(2J+1) rho^0_0 from A_ul + B_ul J, B_lu J
+    (B_lu = g_u/g_l B_ul, B_ul = 6.781962e49 A / nu^3) and collisions C_ul,
+    C_lu = C_ul g_u/g_l exp(-h nu / k T), the rate table interpolated
+    linearly in T; rho^2_0 = 0.  An independent numpy build of that scalar
+    system, solved by numpy, equals the oracle to 1e-13.  (With kmax = 0 the
+    alignment columns of the packing, rhovec(count_array(i) + 2) in
+    main_sub.f90:116-135, hold the next level's rho^0_0, as in the
+    reference, so they are checked for kmax >= 2 only.)"""
+    mol = synth.linear_rotor(6)
+    cloud = synth.power_law_sphere(64, 3, mol, t_law="loglinear")
+    P = oracle.OracleProblem(cloud, mol)
+    N, R = cloud.node_num, mol.r_num
+    rng = np.random.default_rng(kmax)
+    bb = np.array([oracle.black_body(30.0, v) for v in mol.nu])
+    J0 = np.tile(bb, (N, 1)) * rng.uniform(0.01, 2.0, size=(N, R))
+    pp, st, nf = P.solve_se(kmax, J0, np.zeros((N, R)))
+    assert nf == 0
+    g = 2 * mol.j_lev + 1
+    ct = mol.col_temps
+    for node in range(0, cloud.bulk_node_num, 7):
+        T, nH2 = cloud.t_kin[node], cloud.h2_dens[node]
+        Rm = np.zeros((mol.nlev, mol.nlev))          # Rm[i, j]: rate from level i to level j
+        for k in range(R):
+            lo, up = mol.r_trans[k] - 1
+            nu = mol.e_levs[up] - mol.e_levs[lo]
+            B21 = 6.781962e49 * mol.A[k] / nu ** 3
+            Rm[up, lo] += mol.A[k] + B21 * J0[node, k]
+            Rm[lo, up] += g[up] / g[lo] * B21 * J0[node, k]
+        for k in range(mol.c_num):
+            lo, up = mol.c_trans[k] - 1
+            nu = mol.e_levs[up] - mol.e_levs[lo]
+            C21 = float(np.interp(T, ct, mol.C[0, k])) * nH2 * 1e-6
+            Rm[up, lo] += C21
+            Rm[lo, up] += C21 * g[up] / g[lo] * math.exp(-4.79924e-11 * nu / T)
+        M = Rm.T - np.diag(Rm.sum(axis=1))
+        M[0, :] = 1.0
+        rhs = np.zeros(mol.nlev)
+        rhs[0] = 1.0
+        n = np.linalg.solve(M, rhs)
+        np.testing.assert_allclose(pp[node, 0::2] * np.sqrt(g), n, rtol=1e-13, atol=1e-16)
+        if kmax >= 2:
+            assert np.abs(pp[node, 1::2]).max() < 1e-14 * np.abs(pp[node, 0::2]).max()
+        else:
+            np.testing.assert_array_equal(pp[node, 3:-2:2], pp[node, 4::2])   # J >= 1 but the last
+            assert pp[node, 1] == 0.0 and pp[node, -1] == 0.0
