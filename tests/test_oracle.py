@@ -523,3 +523,65 @@ def test_se_without_anisotropy_is_the_scalar_rate_equations(kmax):
         else:
             np.testing.assert_array_equal(pp[node, 3:-2:2], pp[node, 4::2])   # J >= 1 but the last
             assert pp[node, 1] == 0.0 and pp[node, -1] == 0.0
+
+
+def test_image_dust_maps_against_an_independent_numpy_restatement():
+    """The dust branch of ray_in_raytrace (raytrace.f90:268-290, :308-317:
+    dust intensity, the sigma_0 / sigma_2 sums and the Q, U of aligned
+    grains with alpha = 0.15, para_finish.f90:78) against a numpy
+    restatement on the oracle's marches, for a cloud with dust (gas-to-dust
+    100): the dust I, Q, U, tau to 1e-12 of their peaks."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(384, t_law="loglinear", b_random=0.5)
+    cloud.dust_p = cloud.h2_dens * synth.F4(2.32e-27) / 100.0
+    cloud.t_dust = cloud.t_kin * 0.8
+    N, nlev = cloud.node_num, mol.nlev
+    g = np.sqrt(2.0 * mol.j_lev + 1.0)
+    pp = np.zeros((N, 2 * nlev))
+    pp[:, 0::2] = cloud.lev_p / np.maximum(cloud.lev_p.sum(axis=1, keepdims=True), 1e-300) / g
+    pp[:, 1::2] = 1e-3 * pp[:, 0::2]
+    P = oracle.OracleProblem(cloud, mol)
+    th_inc, ph_az, nvel, im_pix, size, alpha = 0.9, 0.3, 2, 3, 0.6, 0.15
+    out, st, nf = P.image([1], [2], pp, th_inc, ph_az, nvel, 80.0, 0.0, im_pix, size, alpha=alpha)
+    assert nf == 0 and np.abs(out[4]).max() > 0.0 and np.abs(out[5]).max() > 0.0
+    R = _rodrigues((0.0, 0.0, 1.0), ph_az) @ _rodrigues((1.0, 0.0, 0.0), th_inc)
+    X, B = cloud.xyz @ R.T, cloud.bvec @ R.T
+    nu0 = mol.e_levs[1] - mol.e_levs[0]
+    kd = mol.kd_v[0]
+    L = oracle.lib()
+    dx = synth.F4(1e-4)
+    Xf = np.ascontiguousarray(X, dtype=np.float64)
+    dl = np.zeros(2 * 10002, dtype=np.int32)
+    nc = C.c_int(0)
+    I_cmb = oracle.black_body(2.73, nu0)
+    npx = 2 * im_pix + 1
+    peaks = [np.abs(out[q]).max() for q in range(4, 8)]
+    for p in (0, 10, 24, 31, 48):
+        a, b2 = p // npx - im_pix, p % npx - im_pix
+        assert L.orc_trace_out_raytrace(C.c_double(a * size / im_pix), C.c_double(b2 * size / im_pix), N,
+                                        Xf.ctypes.data_as(oracle.P_D), P.c.del_ne, P.c.del_num_ne, P.c.maxne,
+                                        C.c_double(dx), 10000, dl.ctypes.data_as(oracle.P_I), C.byref(nc)) == 0
+        n = nc.value
+        cells, steps = dl[0:2 * n:2] - 1, dl[1:2 * n:2]
+        Id, s0, s2, Qd, Ud, td = I_cmb, 0.0, 0.0, 0.0, 0.0, 0.0
+        for i in range(n - 1):
+            c = cells[i]
+            tau_d = kd * cloud.dust_p[c] * cloud.tx * dx * (steps[i + 1] - steps[i])
+            if tau_d > 1e-30:
+                Ibb = oracle.black_body(cloud.t_dust[c], nu0)
+                e = math.exp(-tau_d)
+                mu2 = 1.0 - B[c, 2] * B[c, 2]
+                sI, sQ = 0.5 * alpha * (mu2 - 2.0 / 3.0), alpha * mu2
+                Id = Id * e + Ibb * (1 - e)
+                s0 = s0 * e + Ibb * (1 - e)
+                s2 = s2 * e + sI * Ibb * (1 - e)
+                phi = math.acos(B[c, 1] / math.sqrt(B[c, 0] ** 2 + B[c, 1] ** 2))
+                if B[c, 0] < 0.0:
+                    phi = -phi
+                Qd = Qd * e + sQ * Ibb * (1 - e) * math.cos(2 * phi)
+                Ud = Ud * e + sQ * Ibb * (1 - e) * math.sin(2 * phi)
+                td += tau_d
+        Id -= I_cmb
+        want = (Id, Id * Qd / (s0 - s2), Id * Ud / (s0 - s2), td) if Id != 0.0 else (0.0, 0.0, 0.0, 0.0)
+        for q in range(4):
+            np.testing.assert_allclose(out[4 + q, p, 0], want[q], rtol=0, atol=1e-12 * peaks[q])
