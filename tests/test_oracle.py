@@ -594,3 +594,73 @@ def test_image_dust_maps_against_an_independent_numpy_restatement():
         want = (Id, Id * Qd / (s0 - s2), Id * Ud / (s0 - s2), td) if Id != 0.0 else (0.0, 0.0, 0.0, 0.0)
         for q in range(4):
             np.testing.assert_allclose(out[4 + q, p, 0], want[q], rtol=0, atol=1e-12 * peaks[q])
+
+
+def test_walks_against_an_independent_restatement():
+    """trace_out / check_neigh_fast / pos_quadratic (inverse_rt.f90:139-214,
+    miscellaneous.f90:1017-1098) restated in plain Python floats (the same
+    IEEE operations in the same order: norm2 squared, left-to-right dot
+    products, the REAL*4 1E-10 threshold, nint): the (cell, cumulative step)
+    lists equal the oracle's bit for bit on 200 random rays."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(1024)
+    P = oracle.OracleProblem(cloud, mol)
+    L = oracle.lib()
+    X = [tuple(float(v) for v in row) for row in cloud.xyz]
+    dne, dnn = cloud.del_ne(), cloud.del_num_ne()          # (maxne, N) and (N)
+    thr = synth.F4(1e-10)
+    dx = synth.F4(1e-6)
+    rng = np.random.default_rng(7)
+    dl = np.zeros(2 * 20002, dtype=np.int32)
+    nc = C.c_int(0)
+
+    def norm2(a, b, c):
+        return math.sqrt(a * a + b * b + c * c)
+
+    for _ in range(200):
+        node = int(rng.integers(1, cloud.bulk_node_num + 1))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        d = (float(d[0]), float(d[1]), float(d[2]))
+        darr = np.array(d)
+        assert L.orc_trace_out(C.byref(P.c), node, darr.ctypes.data_as(oracle.P_D), C.c_double(dx), 20000,
+                               dl.ctypes.data_as(oracle.P_I), C.byref(nc)) == 0
+        n = nc.value
+        want = [(int(dl[2 * i]), int(dl[2 * i + 1])) for i in range(n)]
+        # the restatement
+        p = list(X[node - 1])
+        cur, delta, out = node, 0.0, []
+        while True:
+            nd = norm2(*d)
+            npn = norm2(*p)
+            a_, b_, c_ = nd * nd, 2.0 * (p[0] * d[0] + p[1] * d[1] + p[2] * d[2]), npn * npn - 1.0
+            dis = b_ * b_ - 4.0 * a_ * c_
+            if dis > 0:
+                r1 = (-b_ + math.sqrt(dis)) / (2.0 * a_)
+                r2 = (-b_ - math.sqrt(dis)) / (2.0 * a_)
+                delta = r2 if r2 > 0 else r1
+            nxt = 0
+            xc = X[cur - 1]
+            e0 = (xc[0] - p[0], xc[1] - p[1], xc[2] - p[2])
+            n4 = norm2(*e0)
+            q4 = n4 * n4
+            q5 = e0[0] * d[0] + e0[1] * d[1] + e0[2] * d[2]
+            for s in range(int(dnn[cur - 1])):
+                nb = int(dne[s, cur - 1])
+                xn = X[nb - 1]
+                e1 = (xn[0] - p[0], xn[1] - p[1], xn[2] - p[2])
+                n1 = norm2(*e1)
+                q1 = n1 * n1
+                q2 = e1[0] * d[0] + e1[1] * d[1] + e1[2] * d[2]
+                new_x = 0.5 * (q1 - q4) / (q2 - q5)
+                if new_x > delta or new_x <= thr:
+                    continue
+                delta, nxt = new_x, nb
+            p = [p[k] + delta * d[k] for k in range(3)]
+            out.append([cur, int(math.floor(delta / dx + 0.5))])
+            cur = nxt
+            if nxt == 0:
+                break
+        for i in range(1, len(out)):
+            out[i][1] += out[i - 1][1]
+        assert [tuple(o) for o in out] == want
