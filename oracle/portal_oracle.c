@@ -1269,7 +1269,7 @@ static int check_neigh(const double *X_phot, int node, const double *xyz, const 
     return new_node;
 }
 
-/* trace_out_raytrace raytrace.f90:58-177 (star_mod = 0, dir = +z).
+/* trace_out_raytrace raytrace.f90:58-177 (dir = +z).
  * depth_list is (2, n_depth_rt) = (cell id, step index). */
 static int trace_out_raytrace(double x_co, double y_co, int node_num, const double *xyz,
                               const int *del_ne, const int *del_num_ne, double dx, int n_depth_rt,

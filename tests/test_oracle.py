@@ -664,3 +664,56 @@ def test_walks_against_an_independent_restatement():
         for i in range(1, len(out)):
             out[i][1] += out[i - 1][1]
         assert [tuple(o) for o in out] == want
+
+
+def test_image_marches_against_an_independent_restatement():
+    """trace_out_raytrace (raytrace.f90:58-177) with check_neigh
+    (miscellaneous.f90:1-46) restated in plain Python floats: the start
+    node by the O(N) scan (strict <), then one 1e-4 step at a time, the exit
+    at |P| > 1 and the nearest of the node and its neighbours (strict <, list
+    order) after every step; the (node, step) lists equal the oracle's bit
+    for bit."""
+    import ctypes as C
+    cloud, mol = _tiny_problem(512)
+    P = oracle.OracleProblem(cloud, mol)
+    L = oracle.lib()
+    L.orc_trace_out_raytrace.restype = C.c_int
+    X = [tuple(float(v) for v in row) for row in cloud.xyz]
+    dne, dnn = cloud.del_ne(), cloud.del_num_ne()
+    dx = synth.F4(1e-4)
+    dl = np.zeros(2 * 10002, dtype=np.int32)
+    nc = C.c_int(0)
+    Xf = np.ascontiguousarray(cloud.xyz, dtype=np.float64)
+    for x, y in ((0.0, 0.0), (0.31, -0.2), (-0.55, 0.4), (0.05, 0.66)):
+        assert L.orc_trace_out_raytrace(C.c_double(x), C.c_double(y), cloud.node_num, Xf.ctypes.data_as(oracle.P_D),
+                                        P.c.del_ne, P.c.del_num_ne, P.c.maxne, C.c_double(dx), 10000,
+                                        dl.ctypes.data_as(oracle.P_I), C.byref(nc)) == 0
+        want = [(int(dl[2 * i]), int(dl[2 * i + 1])) for i in range(nc.value)]
+        z = -1.0 * math.sqrt(1.0 - x * x - y * y)
+        rsave, node = 10.0, 0
+        for i, c in enumerate(X):
+            r = math.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2)
+            if r < rsave:
+                rsave, node = r, i + 1
+        out, k = [], 0
+        while True:
+            z = z + dx
+            k += 1
+            done = math.sqrt(x * x + y * y + z * z) > 1.0
+            if done:
+                out.append((node, k))
+            c = X[node - 1]
+            d0 = (x - c[0]) * (x - c[0]) + (y - c[1]) * (y - c[1]) + (z - c[2]) * (z - c[2])
+            new = node
+            for s in range(int(dnn[node - 1])):
+                nb = int(dne[s, node - 1])
+                n_ = X[nb - 1]
+                dd = (x - n_[0]) * (x - n_[0]) + (y - n_[1]) * (y - n_[1]) + (z - n_[2]) * (z - n_[2])
+                if dd < d0:
+                    d0, new = dd, nb
+            if new != node:
+                out.append((new, k))
+                node = new
+            if done:
+                break
+        assert out == want, (x, y)
