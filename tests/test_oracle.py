@@ -717,3 +717,28 @@ def test_image_marches_against_an_independent_restatement():
             if done:
                 break
         assert out == want, (x, y)
+
+
+@pytest.mark.parametrize("anis", [0.1, -0.3, 0.5])
+def test_se_two_level_alignment_limit(anis):
+    """The polarized SE in the two-level limit of Landi Degl'Innocenti &
+    Landolfi (2004): a J = 0 -> 1 transition, collisions negligible and the
+    radiation weak (B J / A = 1e-6, so stimulated emission is negligible)
+    gives the upper level the alignment sigma^2_0 = rho^2_0 / rho^0_0 =
+    w^(2)_{10} J^2_0 / J^0_0 with w^(2)_{10} = 1 (the unpolarized J = 0 lower
+    level), to the O(B J / A) of stimulated emission."""
+    import dataclasses
+    mol = synth.linear_rotor(2)
+    mol = dataclasses.replace(mol, C=mol.C * 1e-25)
+    cloud = synth.power_law_sphere(64, 3, mol)
+    P = oracle.OracleProblem(cloud, mol)
+    N, R = cloud.node_num, mol.r_num
+    nu, A = mol.nu[0], mol.A[0]
+    B21 = 6.781962e49 * A / nu ** 3
+    J0 = np.full((N, R), 1e-6 * A / B21)
+    pp, st, nf = P.solve_se(2, J0, anis * J0)
+    assert nf == 0
+    w = 3.0 * oracle.wigner6j(2, 2, 4, 2, 2, 0)          # (-1)^2 sqrt(3) sqrt(3) {1 1 2; 1 1 0}
+    assert w == pytest.approx(1.0, rel=1e-14)
+    sig = pp[:cloud.bulk_node_num, 3] / pp[:cloud.bulk_node_num, 2]
+    np.testing.assert_allclose(sig, w * anis, rtol=1e-5)
