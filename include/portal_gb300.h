@@ -52,7 +52,7 @@ enum {
     PORTAL_NODE_REFINE = 4,    /* FP32 LU + FP64 refinement did not converge; the
                                   node was solved by the FP64 LU instead           */
     PORTAL_NODE_STAR = 8       /* star mode: star_all's rays exceed nth*nph
-                                  (miscellaneous.f90:1181-1184 would have stopped) */
+                                  (miscellaneous.f90:1203-1206 would have stopped) */
 };
 
 const char *portal_strerror(int code);
@@ -203,7 +203,7 @@ int portal_image(portal_ctx *ctx, const double *pol_pops, int nlines, const int 
  *   - the node loop skips nodes with |X| <= R_star (main_para.f90:232): zero
  *     J and populations;
  *   - every other node integrates over its own ray set from star_all
- *     (miscellaneous.f90:1139-1217; main_sub.f90:56-79): ceil(dOm / (4 pi /
+ *     (miscellaneous.f90:1139-1226; main_sub.f90:56-79): ceil(dOm / (4 pi /
  *     (nth nph))) rays into the star's cone of solid angle
  *     dOm = pi (R_star / |X_star - X|)^2, then nth bands of
  *     ceil(nph sin th) rays over the rest of the sphere; the star rays end

@@ -237,7 +237,7 @@ static double norm2_3(const double *v)
     return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
 }
 
-/* find_angles miscellaneous.f90:86-145: (th, ph) of dir in the frame of
+/* find_angles miscellaneous.f90:86-134: (th, ph) of dir in the frame of
  * find_dir (z = bvec, x = bvec x gvec normalised) */
 static void find_angles(const double *b, const double *g, const double *dir, double *th, double *ph)
 {
@@ -252,7 +252,7 @@ static void find_angles(const double *b, const double *g, const double *dir, dou
     *ph = atan2(xv[0] * dir[0] + xv[1] * dir[1] + xv[2] * dir[2], xv[0] * cbd[0] + xv[1] * cbd[1] + xv[2] * cbd[2]);
 }
 
-/* circle_points miscellaneous.f90:1219-1265: n points on the star's cap of
+/* circle_points miscellaneous.f90:1228-1265: n points on the star's cap of
  * half-angle th_s, x(3,n) = (cos th, ph, weight).  One point keeps the
  * reference's x(1:2,1) = cos(1): polar angle 1 rad, azimuth cos(1). */
 static void circle_points(int n, double th_s, double dth_s, double *x)

@@ -87,11 +87,11 @@ double orc_wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
 void   orc_find_dir(const double *bvec, const double *gvec, double th, double ph,
                     double *dir);
 
-/* star_all miscellaneous.f90:1139-1217 with circle_points :1219-1265: the
+/* star_all miscellaneous.f90:1139-1226 with circle_points :1228-1265: the
  * ray set of a node outside the star -- n_star rays into the star's cone
  * around kvec (the node-to-star direction) with solid angle dOm, then nth
  * bands over the rest of the sphere -- as (cos th, ph, weight) relative to
- * bvec (find_angles miscellaneous.f90:86-145).  xth holds nth*nph columns;
+ * bvec (find_angles miscellaneous.f90:86-134).  xth holds nth*nph columns;
  * returns the ray count, or -1 where the reference would run past them. */
 int orc_star_all(int nth, int nph, const double *kvec, const double *gvec, const double *bvec,
                  double dOm_star, int *n_star, double *xth);

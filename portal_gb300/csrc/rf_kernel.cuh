@@ -110,7 +110,7 @@ struct RayBatchStar {
 
 constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
 
-// star_all (miscellaneous.f90:1139-1217, circle_points :1219-1265) for ray
+// star_all (miscellaneous.f90:1139-1226, circle_points :1228-1265) for ray
 // i of a node outside the star: (cos th, ph) of the ray in the field frame
 // and its quadrature weight.  sk as in RayBatchStar; f the node frame b (0-2),
 // x = b x g / |b x g| (3-5), x x b (6-8).  The first n_star rays cover the
@@ -119,7 +119,7 @@ constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
 // spiral), the others nth bands of ceiling(nph sin th) rays from th_star to
 // pi about the star direction.  Each direction, built about the star
 // direction with find_dir (gauge g), is re-expressed by find_angles in the
-// field frame (miscellaneous.f90:86-145).
+// field frame (miscellaneous.f90:86-134).
 // Returns the direction's (cos th, sin th, cos ph, sin ph) in the field
 // frame as inverse_rt rebuilds it (find_dir of acos(mu), ph) and stores the
 // weights (w, w c_in / sqrt 2) in *wts.  Out of line: the default path
@@ -204,7 +204,7 @@ __device__ __noinline__ void star_node(double *sk, int *sn, double xs, double ys
     int nv = ns;
     for (int b = 1; b <= nth; b++) nv += (int)ceil(nph * sin((b - 1) * dr + thi));
     sn[0] = ns;
-    // the reference stops when the rays exceed nth nph (miscellaneous.f90:1181-1184)
+    // the reference stops when the rays exceed nth nph (miscellaneous.f90:1203-1206)
     sn[1] = (ns > nth * nph || nv > nth * nph) ? -1 : nv;
 }
 

@@ -163,7 +163,7 @@ def test_n_depth_overflow_is_reported(ctx):
 
 def test_star_rays_beyond_nth_nph_are_reported(ctx):
     """A node so close to the star that star_all needs more than nth*nph
-    rays stops the reference (miscellaneous.f90:1181-1184): an error here,
+    rays stops the reference (miscellaneous.f90:1203-1206): an error here,
     with status bit PORTAL_NODE_STAR on that node."""
     import portal_gb300 as pg
     cloud, mol, rc = _small()

@@ -225,7 +225,7 @@ def test_node_maps_start_points_and_einstein_a():
 
 @pytest.mark.parametrize("nth,nph,dist", [(8, 8, 3.0), (16, 16, 1.5), (12, 12, 40.0), (16, 16, 1.05), (6, 6, 8.0)])
 def test_star_all_ray_sets(nth, nph, dist):
-    """star_all (miscellaneous.f90:1139-1217): the weights of a node's rays
+    """star_all (miscellaneous.f90:1139-1226): the weights of a node's rays
     sum to one, the star's cone carries dOm / 4 pi with dOm = pi (R / d)^2,
     and the cone's rays point within th_star of the star (one ray: the
     reference's cos(1) stand-in, 1 rad off); the count stays within nth*nph."""
