@@ -94,5 +94,10 @@ module portal_gpu
       integer(c_int) :: iterations
       integer(c_long_long) :: n_segments
     end function
+    integer(c_int) function portal_node_segments(ctx, segments) bind(C, name="portal_node_segments")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+      integer(c_int) :: segments(*)
+    end function
   end interface
 end module

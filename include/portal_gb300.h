@@ -242,14 +242,16 @@ int portal_image_nodes(portal_ctx *ctx, const double *pol_pops, int nlines, cons
  * cudaMalloc: a host whose device memory is owned by its own pool (e.g. CUDA
  * Fortran device arrays, a framework that hands out pre-sized buffers), or
  * code that may not allocate between simulation steps.  It computes what
- * portal_radiation_field computes, needs no context, and allocates nothing:
+ * portal_radiation_field computes for a run without a star (star_mod = 0:
+ * it has no star parameters), needs no context, and allocates nothing:
  *   - every input is a DEVICE pointer to the reference-layout array that
  *     portal_set_cloud takes from the host (xyz(3,N), vel_all(3,N), b_all(N),
  *     temp_all(2,N), dust_p(N), ab_all(N), lev_p(nlev,N), bvec_all(3,N),
  *     del_ne(N,maxne), del_num_ne(N)); the molecule's line data
  *     (j_lev, r_trans(2,r_num), t_Aji, nu, t_Bij, kd_v) and gvec are HOST
  *     pointers;
- *   - J0(r_num,N), J2(r_num,N) and status(N) (or NULL) are DEVICE outputs;
+ *   - J0(r_num,N), J2(r_num,N) and status(N) (or NULL) are DEVICE outputs,
+ *     written for every node (0 for the non-bulk nodes and the skipped ones);
  *   - its only scratch is a fixed 64 MiB array inside the library image,
  *     held on every GPU that loads the library until the process exits.
  * The call is asynchronous on cuda_stream (a cudaStream_t, NULL = legacy
@@ -257,7 +259,9 @@ int portal_image_nodes(portal_ctx *ctx, const double *pol_pops, int nlines, cons
  * shares the one scratch array (and the line constants), so calls that
  * overlap on the GPU race; serialise them.  The first call on each device
  * looks up the scratch array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.
+ * that first call before any stream capture.  The address is kept for the
+ * life of the process, so no cudaDeviceReset may happen while the library
+ * is loaded.
  * Limits (PORTAL_ERR_ARG beyond them; portal_radiation_field_static_limits
  * reports them): n_depth <= 857 cells per ray, r_num <= 64 lines,
  * 2*nvel+1 <= 288 channels, nth*nph <= 8192 directions.  Walk overflow is
@@ -291,6 +295,12 @@ int portal_last_kernel_times(const portal_ctx *ctx, double *times_ms, int *launc
  * NULL): J0, J2 (r_num,N), pol_pops(N, 2*nlev), status(N).  For models run by
  * a batch, whose results stay on the device. */
 int portal_get_results(portal_ctx *ctx, double *J0, double *J2, double *pol_pops, int *status);
+
+/* Ray segments of every node in the last radiation-field pass:
+ * segments(N), the sum over the node's rays of trace_out's node_count
+ * (inverse_rt.f90:139-214), 0 for skipped and non-bulk nodes.  No
+ * reference counterpart (the reference keeps node_count per ray only). */
+int portal_node_segments(portal_ctx *ctx, int *segments);
 
 /* ---- many models in one launch (no counterpart in the reference) --------
  *

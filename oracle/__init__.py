@@ -143,6 +143,39 @@ class OracleProblem:
                                         _p(J2), _p(JE), _p(LS), _p(st, P_I), C.byref(nseg))
         return J0, J2, JE, LS, st
 
+    def radiation_field_nodes(self, rc, nodes, nthreads=0, split=False):
+        """The node loop over a list of 0-based bulk node ids: J0, J2 (and
+        J_eff, L* with split) of shape (N, r_num) filled at the listed rows,
+        the status and the segment count of each listed node."""
+        N, R = self.cloud.node_num, self.mol.r_num
+        ids = np.ascontiguousarray(np.asarray(nodes, dtype=np.int64) + 1, dtype=np.int32)
+        J0 = np.zeros((N, R)); J2 = np.zeros((N, R))
+        JE = np.zeros((N, R)) if split else None
+        LS = np.zeros((N, R)) if split else None
+        st = np.zeros(len(ids), dtype=np.int32)
+        seg = np.zeros(len(ids), dtype=np.int64)
+        g = np.ascontiguousarray(rc.gvec, dtype=np.float64)
+        lib().orc_radiation_field_nodes(C.byref(self.c), C.byref(self.m), rc.nth, rc.nph, rc.nvel, _p(g),
+                                        C.c_double(rc.dx), rc.n_depth, _p(ids, P_I), len(ids), nthreads,
+                                        _p(J0), _p(J2), _p(JE) if split else None, _p(LS) if split else None,
+                                        _p(st, P_I), _p(seg, P_L))
+        if split:
+            return J0, J2, JE, LS, st, seg
+        return J0, J2, st, seg
+
+    def solve_se_nodes(self, kmax, J0, J2, nodes, nthreads=0):
+        """pol_pops (N, 2*nlev) at the listed 0-based bulk nodes' rows (0
+        elsewhere) and the status per listed node."""
+        N, nlev = self.cloud.node_num, self.mol.nlev
+        ids = np.ascontiguousarray(np.asarray(nodes, dtype=np.int64) + 1, dtype=np.int32)
+        pp = np.zeros((2 * nlev, N))
+        st = np.zeros(len(ids), dtype=np.int32)
+        J0c = np.ascontiguousarray(J0, dtype=np.float64)
+        J2c = np.ascontiguousarray(J2, dtype=np.float64)
+        lib().orc_solve_se_nodes(C.byref(self.c), C.byref(self.m), kmax, _p(J0c), _p(J2c), _p(ids, P_I),
+                                 len(ids), nthreads, _p(pp), None, _p(st, P_I))
+        return pp.T.copy(), st
+
     def solve_se(self, kmax, J0, J2, node_lo=1, node_hi=None, nthreads=0, rates=False):
         """pol_pops as an (N, 2*nlev) array (reference pol_pops(node,:))."""
         N, nlev = self.cloud.node_num, self.mol.nlev

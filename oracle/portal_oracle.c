@@ -568,8 +568,47 @@ static int inside_star(const orc_cloud *c, int node)
     return c->star_mod == 1 && !(norm2_3(c->xyz + 3 * (node - 1)) > c->R_star);
 }
 
-/* The node loop main_para.f90:210-257, radiation field half of trace_node
- * (main_sub.f90:56-85; star mode: the node's own ray set from star_all). */
+/* One node of the node loop main_para.f90:210-257, radiation field half of
+ * trace_node (main_sub.f90:56-85; star mode: the node's own ray set from
+ * star_all).  Returns the node's status; adds its segments to *ns. */
+static int rf_node(const orc_cloud *c, const orc_molecule *m, int nth, int nph, int nvel,
+                   const double *gvec, double dx, int n_depth, const double *xth, int n_sphere,
+                   int node, double *J0, double *J2, double *JE, double *LS, int64_t *ns)
+{
+    const int t_num = m->r_num;
+    double *j0 = J0 + (size_t)t_num * (node - 1);
+    double *j2 = J2 + (size_t)t_num * (node - 1);
+    double *je = JE ? JE + (size_t)t_num * (node - 1) : NULL;
+    double *ls = JE ? LS + (size_t)t_num * (node - 1) : NULL;
+    int st = ORC_OK;
+    if (c->ab_all[node - 1] > 0.0 && c->star_mod == 1 && !inside_star(c, node)) {
+        const double *X = c->xyz + 3 * (node - 1);
+        double kv[3] = {c->X_star[0] - X[0], c->X_star[1] - X[1], c->X_star[2] - X[2]};
+        double d = norm2_3(kv);
+        double q = c->R_star / d;
+        double dOm = acos(-1.0) * (q * q);
+        for (int k = 0; k < 3; k++) kv[k] = kv[k] / d;
+        double *xs = (double *)malloc(sizeof(double) * 3 * (size_t)nth * nph);
+        int n_star = 0;
+        int n_var = orc_star_all(nth, nph, kv, gvec, c->bvec + 3 * (node - 1), dOm, &n_star, xs);
+        if (n_var < 0) {
+            st = ORC_ERR_ARG;
+            for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
+        } else {
+            st = inverse_rt(c, m, node, xs, n_var, n_star, gvec, nvel, dx, n_depth, j0, j2, je, ls, ns);
+        }
+        free(xs);
+    } else if (c->ab_all[node - 1] > 0.0 && c->star_mod != 1) {
+        st = inverse_rt(c, m, node, xth, n_sphere, 0, gvec, nvel, dx, n_depth, j0, j2, je, ls, ns);
+    } else {
+        for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
+        if (je)
+            for (int k = 0; k < t_num; k++) { je[k] = 0.0; ls[k] = 0.0; }
+    }
+    return st;
+}
+
+/* The node loop main_para.f90:210-257 over nodes node_lo..node_hi. */
 int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth, int nph,
                               int nvel, const double *gvec, double dx, int n_depth, int node_lo,
                               int node_hi, int nthreads, double *J0, double *J2, double *JE,
@@ -579,7 +618,6 @@ int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth
     int n_sphere = orc_legendre_all(nth, nph, xth);
     int nfail = 0;
     int64_t nseg = 0;
-    const int t_num = m->r_num;
     if (node_lo < 1) node_lo = 1;
     if (node_hi > c->bulk_node_num) node_hi = c->bulk_node_num;
 #ifdef _OPENMP
@@ -587,42 +625,44 @@ int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth
 #endif
 #pragma omp parallel for schedule(static) reduction(+ : nfail, nseg)
     for (int node = node_lo; node <= node_hi; node++) {
-        double *j0 = J0 + (size_t)t_num * (node - 1);
-        double *j2 = J2 + (size_t)t_num * (node - 1);
-        double *je = JE ? JE + (size_t)t_num * (node - 1) : NULL;
-        double *ls = JE ? LS + (size_t)t_num * (node - 1) : NULL;
-        int st = ORC_OK;
         int64_t ns = 0;
-        if (c->ab_all[node - 1] > 0.0 && c->star_mod == 1 && !inside_star(c, node)) {
-            const double *X = c->xyz + 3 * (node - 1);
-            double kv[3] = {c->X_star[0] - X[0], c->X_star[1] - X[1], c->X_star[2] - X[2]};
-            double d = norm2_3(kv);
-            double q = c->R_star / d;
-            double dOm = acos(-1.0) * (q * q);
-            for (int k = 0; k < 3; k++) kv[k] = kv[k] / d;
-            double *xs = (double *)malloc(sizeof(double) * 3 * (size_t)nth * nph);
-            int n_star = 0;
-            int n_var = orc_star_all(nth, nph, kv, gvec, c->bvec + 3 * (node - 1), dOm, &n_star, xs);
-            if (n_var < 0) {
-                st = ORC_ERR_ARG;
-                for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
-            } else {
-                st = inverse_rt(c, m, node, xs, n_var, n_star, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
-            }
-            free(xs);
-        } else if (c->ab_all[node - 1] > 0.0 && c->star_mod != 1) {
-            st = inverse_rt(c, m, node, xth, n_sphere, 0, gvec, nvel, dx, n_depth, j0, j2, je, ls, &ns);
-        } else {
-            for (int k = 0; k < t_num; k++) { j0[k] = 0.0; j2[k] = 0.0; }
-            if (je)
-                for (int k = 0; k < t_num; k++) { je[k] = 0.0; ls[k] = 0.0; }
-        }
+        int st = rf_node(c, m, nth, nph, nvel, gvec, dx, n_depth, xth, n_sphere, node, J0, J2, JE, LS, &ns);
         if (status) status[node - 1] = st;
         if (st != ORC_OK) nfail++;
         nseg += ns;
     }
     free(xth);
     if (n_segments) *n_segments = nseg;
+    return nfail;
+}
+
+/* The same node loop over an arbitrary list of bulk nodes (1-based ids; a
+ * sample of a cloud too large to restate whole).  Nodes vary widely in cost,
+ * so the threads take them one at a time.  seg_per_node (n_nodes) or NULL
+ * receives each listed node's segment count. */
+int orc_radiation_field_nodes(const orc_cloud *c, const orc_molecule *m, int nth, int nph, int nvel,
+                              const double *gvec, double dx, int n_depth, const int *nodes,
+                              int n_nodes, int nthreads, double *J0, double *J2, double *JE,
+                              double *LS, int *status, int64_t *seg_per_node)
+{
+    double *xth = (double *)malloc(sizeof(double) * 3 * (size_t)nth * nph);
+    int n_sphere = orc_legendre_all(nth, nph, xth);
+    int nfail = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : nfail)
+    for (int i = 0; i < n_nodes; i++) {
+        const int node = nodes[i];
+        int64_t ns = 0;
+        int st = ORC_ERR_ARG;
+        if (node >= 1 && node <= c->bulk_node_num)
+            st = rf_node(c, m, nth, nph, nvel, gvec, dx, n_depth, xth, n_sphere, node, J0, J2, JE, LS, &ns);
+        if (status) status[i] = st;
+        if (seg_per_node) seg_per_node[i] = ns;
+        if (st != ORC_OK) nfail++;
+    }
+    free(xth);
     return nfail;
 }
 
@@ -1116,11 +1156,63 @@ int orc_node_matrix(const orc_cloud *c, const orc_molecule *m, int kmax, int nod
 
 /* SE half of trace_node main_sub.f90:93-137 over nodes node_lo..node_hi of
  * the bulk, in the node loop of main_para.f90:210-257. */
-int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
-                 const double *J2, int node_lo, int node_hi, int nthreads, double *pol_pops,
-                 double *rates, int *status)
+/* trace_node's SE half (main_sub.f90:93-137) for one node: pol_pops
+ * (node_num, 2*nlev) column-major, rates (node_num,3,2*nlev) or NULL; AC,
+ * rhovec and rt are the thread's work arrays.  Returns the node's status. */
+static int se_node(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
+                   const double *J2, int c_dim, const int *count_array, int n_trans,
+                   const int *all_trans, int node, double *AC, double *rhovec, double *rt,
+                   double *pol_pops, double *rates)
 {
     int nlev = m->nlev, N = c->node_num;
+    int st = ORC_OK;
+    if (c->ab_all[node - 1] > 0.0 && !inside_star(c, node)) {
+        orc_make_AC(m, c->h2_dens[node - 1], c->t_kin[node - 1], n_trans, all_trans,
+                    J0 + (size_t)m->r_num * (node - 1), J2 + (size_t)m->r_num * (node - 1), AC);
+        st = orc_get_rhovec(c_dim, count_array, nlev, m->j_lev, n_trans, all_trans, AC, kmax,
+                            c->t_kin[node - 1], rhovec, rates ? rt : NULL);
+        if (st != ORC_OK) {
+            for (int i = 0; i < c_dim; i++) rhovec[i] = NAN;
+            for (int i = 0; i < 3 * c_dim; i++) rt[i] = 0.0;
+        }
+        for (int i = 0; i < nlev; i++) {
+            size_t p0 = (size_t)(node - 1) + (size_t)N * (2 * i);
+            size_t p1 = p0 + N;
+            int ca = count_array[i];
+            pol_pops[p0] = rhovec[ca];
+            /* with kmax = 0 the reference reads the next level's rho^0_0 here,
+             * and past the end of rhovec for the last level (0 here) */
+            pol_pops[p1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rhovec[ca + 1] : 0.0;
+            if (rates) {
+                for (int q = 0; q < 3; q++) {
+                    size_t r0 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i));
+                    size_t r1 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i + 1));
+                    rates[r0] = rt[3 * ca + q];
+                    rates[r1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rt[3 * (ca + 1) + q] : 0.0;
+                }
+            }
+            /* main_sub.f90:131-136 (the reference zeroes the same
+             * rates entry twice; the restatement keeps that) */
+            if (isnan(pol_pops[p0])) {
+                pol_pops[p0] = 0.0;
+                pol_pops[p1] = 0.0;
+                if (rates)
+                    for (int q = 0; q < 3; q++)
+                        rates[(size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i + 1))] = 0.0;
+            }
+        }
+    }
+    return st;
+}
+
+/* The SE half of the node loop over nodes node_lo..node_hi (node_list NULL)
+ * or over the n_list 1-based bulk nodes of node_list (status then per list
+ * entry). */
+static int solve_se_impl(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
+                         const double *J2, int node_lo, int node_hi, const int *node_list,
+                         int n_list, int nthreads, double *pol_pops, double *rates, int *status)
+{
+    int nlev = m->nlev;
     int *count_array = (int *)malloc(sizeof(int) * nlev);
     int c_dim = orc_setup_count_array(m->j_lev, nlev, kmax, count_array);
     int *all_trans = (int *)malloc(sizeof(int) * 2 * (m->r_num + m->c_num + 1));
@@ -1128,6 +1220,7 @@ int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const doub
     int nfail = 0;
     if (node_lo < 1) node_lo = 1;
     if (node_hi > c->bulk_node_num) node_hi = c->bulk_node_num;
+    const int n_items = node_list ? n_list : (node_hi >= node_lo ? node_hi - node_lo + 1 : 0);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -1137,52 +1230,34 @@ int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const doub
         double *rhovec = (double *)malloc(sizeof(double) * c_dim);
         double *rt = (double *)malloc(sizeof(double) * 3 * c_dim);
 #pragma omp for schedule(static)
-        for (int node = node_lo; node <= node_hi; node++) {
-            int st = ORC_OK;
-            if (c->ab_all[node - 1] > 0.0 && !inside_star(c, node)) {
-                orc_make_AC(m, c->h2_dens[node - 1], c->t_kin[node - 1], n_trans, all_trans,
-                            J0 + (size_t)m->r_num * (node - 1), J2 + (size_t)m->r_num * (node - 1),
-                            AC);
-                st = orc_get_rhovec(c_dim, count_array, nlev, m->j_lev, n_trans, all_trans, AC,
-                                    kmax, c->t_kin[node - 1], rhovec, rates ? rt : NULL);
-                if (st != ORC_OK) {
-                    for (int i = 0; i < c_dim; i++) rhovec[i] = NAN;
-                    for (int i = 0; i < 3 * c_dim; i++) rt[i] = 0.0;
-                }
-                for (int i = 0; i < nlev; i++) {
-                    size_t p0 = (size_t)(node - 1) + (size_t)N * (2 * i);
-                    size_t p1 = p0 + N;
-                    int ca = count_array[i];
-                    pol_pops[p0] = rhovec[ca];
-                    /* with kmax = 0 the reference reads the next level's rho^0_0 here,
-                     * and past the end of rhovec for the last level (0 here) */
-                    pol_pops[p1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rhovec[ca + 1] : 0.0;
-                    if (rates) {
-                        for (int q = 0; q < 3; q++) {
-                            size_t r0 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i));
-                            size_t r1 = (size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i + 1));
-                            rates[r0] = rt[3 * ca + q];
-                            rates[r1] = (m->j_lev[i] != 0 && ca + 1 < c_dim) ? rt[3 * (ca + 1) + q] : 0.0;
-                        }
-                    }
-                    /* main_sub.f90:131-136 (the reference zeroes the same
-                     * rates entry twice; the restatement keeps that) */
-                    if (isnan(pol_pops[p0])) {
-                        pol_pops[p0] = 0.0;
-                        pol_pops[p1] = 0.0;
-                        if (rates)
-                            for (int q = 0; q < 3; q++)
-                                rates[(size_t)(node - 1) + (size_t)N * (q + 3 * (size_t)(2 * i + 1))] = 0.0;
-                    }
-                }
-            }
-            if (status) status[node - 1] = st;
+        for (int it = 0; it < n_items; it++) {
+            const int node = node_list ? node_list[it] : node_lo + it;
+            int st = ORC_ERR_ARG;
+            if (node >= 1 && node <= c->bulk_node_num)
+                st = se_node(c, m, kmax, J0, J2, c_dim, count_array, n_trans, all_trans, node, AC, rhovec,
+                             rt, pol_pops, rates);
+            if (status) status[node_list ? it : node - 1] = st;
             if (st != ORC_OK) nfail++;
         }
         free(AC); free(rhovec); free(rt);
     }
     free(count_array); free(all_trans);
     return nfail;
+}
+
+int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
+                 const double *J2, int node_lo, int node_hi, int nthreads, double *pol_pops,
+                 double *rates, int *status)
+{
+    return solve_se_impl(c, m, kmax, J0, J2, node_lo, node_hi, NULL, 0, nthreads, pol_pops, rates, status);
+}
+
+int orc_solve_se_nodes(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
+                       const double *J2, const int *nodes, int n_nodes, int nthreads,
+                       double *pol_pops, double *rates, int *status)
+{
+    return solve_se_impl(c, m, kmax, J0, J2, 1, c->bulk_node_num, nodes, n_nodes, nthreads, pol_pops, rates,
+                         status);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -120,6 +120,15 @@ int orc_radiation_field_split(const orc_cloud *c, const orc_molecule *m, int nth
                               int node_hi, int nthreads, double *J0, double *J2, double *JE,
                               double *LS, int *status, int64_t *n_segments);
 
+/* The node loop over a list of n_nodes 1-based bulk node ids (a sample of a
+ * cloud too large to restate whole): J0/J2 (and JE/LS when JE is not NULL)
+ * written at the listed nodes' columns, status and seg_per_node (each may
+ * be NULL) per list entry.  Returns the number of failed nodes. */
+int orc_radiation_field_nodes(const orc_cloud *c, const orc_molecule *m, int nth, int nph, int nvel,
+                              const double *gvec, double dx, int n_depth, const int *nodes,
+                              int n_nodes, int nthreads, double *J0, double *J2, double *JE,
+                              double *LS, int *status, int64_t *seg_per_node);
+
 /* ---- statistical equilibrium ---- */
 int orc_setup_count_array(const int *j_lev, int nlev, int kmax, int *count_array);
 int orc_all_transitions(const orc_molecule *m, int *all_trans /* (2,r_num+c_num) */);
@@ -138,6 +147,10 @@ int orc_get_rhovec(int c_dim, const int *count_array, int nlev, const int *j_lev
 int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax,
                  const double *J0, const double *J2, int node_lo, int node_hi,
                  int nthreads, double *pol_pops, double *rates, int *status);
+/* orc_solve_se over a list of 1-based bulk node ids (status per entry). */
+int orc_solve_se_nodes(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
+                       const double *J2, const int *nodes, int n_nodes, int nthreads,
+                       double *pol_pops, double *rates, int *status);
 /* Coupling constants of pop_eqs.f90:1-359 for the tests: which = 0 t_A,
  * 1 t_S, 2 t_E (c0 only), 3 r_A, 4 r_S. */
 void orc_coupling_constants(int which, int j, int k, int j2, int k2, double *c0, double *c2);

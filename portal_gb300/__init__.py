@@ -39,7 +39,7 @@ EXPORTS = (
     "portal_mlp_get_params", "portal_mlp_set_params", "portal_mlp_gradients", "portal_mlp_train",
     "portal_mlp_predict", "portal_warmstart_features", "portal_get_results",
     "portal_batch_create", "portal_batch_destroy", "portal_batch_last_error", "portal_batch_add",
-    "portal_batch_prepare", "portal_batch_run", "portal_batch_config",
+    "portal_batch_prepare", "portal_batch_run", "portal_batch_config", "portal_node_segments",
 )
 
 _lib = None
@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
     L.portal_mlp_predict.argtypes = [C.c_void_p, P_F, C.c_int, P_F]
     L.portal_warmstart_features.argtypes = [C.c_void_p, P_F]
     L.portal_get_results.argtypes = [C.c_void_p, P_D, P_D, P_D, P_I]
+    L.portal_node_segments.argtypes = [C.c_void_p, P_I]
     L.portal_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
     L.portal_batch_destroy.argtypes = [C.c_void_p]
     L.portal_batch_last_error.restype = C.c_char_p
@@ -348,6 +349,12 @@ class Context:
         pp = np.zeros((2 * self.nlev, self.N)) if pops else None
         self._check(lib().portal_get_results(self._h, _p(J0), _p(J2), _p(pp), None))
         return J0, J2, (None if pp is None else pp.T.copy())
+
+    def node_segments(self) -> np.ndarray:
+        """Ray segments of every node in the last radiation-field pass (N,)."""
+        seg = np.zeros(self.N, dtype=np.int32)
+        self._check(lib().portal_node_segments(self._h, _p(seg, P_I)))
+        return seg
 
     def warmstart_features(self) -> np.ndarray:
         """Features (N, 8) of the warm start from the device-resident

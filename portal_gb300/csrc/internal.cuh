@@ -31,6 +31,7 @@ struct RFArgs {
     double *J0, *J2;
     double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
     int *status;
+    int *segs;                        // (N) ray segments of each node (sum of node_count) or null
     int2 *walk;
     unsigned long long *counters;
 };

@@ -247,7 +247,8 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
         ct[nch + i] = (float)(std::exp(-q0 * q0) * 2.0 / (spi * nvel));
     }
     if (c->dirtab.reserve(dt.size()) || c->chtab.reserve(ct.size()) ||
-        c->ltab.reserve((size_t)L * N) || c->J0.reserve((size_t)L * N) || c->J2.reserve((size_t)L * N))
+        c->ltab.reserve((size_t)L * N) || c->J0.reserve((size_t)L * N) || c->J2.reserve((size_t)L * N) ||
+        c->nodeseg.reserve((size_t)N))
         return set_err(c, PORTAL_ERR_NOMEM, "radiation-field buffers");
     if (split && (c->JE.reserve((size_t)L * N) || c->LS.reserve((size_t)L * N)))
         return set_err(c, PORTAL_ERR_NOMEM, "split-field buffers");
@@ -270,6 +271,7 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
     a.Rs = c->star_mode ? c->R_star() : 0.0;
     a.bbs = c->bbstar.p;
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
+    a.segs = c->nodeseg.p;
     a.JE = split ? c->JE.p : nullptr;
     a.LS = split ? c->LS.p : nullptr;
     a.walk = nullptr;
@@ -286,6 +288,7 @@ int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s) {
     PCHECK(c, cudaMemsetAsync(c->J0.p, 0, (size_t)L * N * sizeof(double), s));
     PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), s));
     PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), s));
+    if (a.segs) PCHECK(c, cudaMemsetAsync(a.segs, 0, (size_t)N * sizeof(int), s));
     if (a.JE) {
         PCHECK(c, cudaMemsetAsync(c->JE.p, 0, (size_t)L * N * sizeof(double), s));
         PCHECK(c, cudaMemsetAsync(c->LS.p, 0, (size_t)L * N * sizeof(double), s));
@@ -388,4 +391,13 @@ extern "C" int portal_radiation_field_split(portal_ctx *c, int nth, int nph, int
                                             double *L_star, int *status, long long *n_segments) {
     return radiation_field_call(c, nth, nph, nvel, gvec, dx, n_depth, J0, J2, J_eff, L_star, true, status,
                                 n_segments);
+}
+
+extern "C" int portal_node_segments(portal_ctx *c, int *segments) {
+    if (!c || !segments) return PORTAL_ERR_ARG;
+    if (!c->j_valid || !c->nodeseg.p) return set_err(c, PORTAL_ERR_STATE, "no radiation field computed");
+    PCHECK(c, cudaMemcpyAsync(segments, c->nodeseg.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    return PORTAL_OK;
 }

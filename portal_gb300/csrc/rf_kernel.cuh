@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
         KahanF accEa, accEb, accLa, accLb;  // J_eff and L* of the same lines (split field only)
         const bool split = (a.JE != nullptr);
         int st = 0;
+        int node_seg = 0;   // the node's ray segments (sum of node_count over its rays)
         if (a.ab[node] > 0.0) {
             if (lane == 0) {
                 // node frame (find_dir miscellaneous.f90:48-82): x = b x g / |b x g|,
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             return a.bb[l];
                         }
                     };
-                    nseg += (unsigned long long)Kr;
+                    node_seg += Kr;
                     const int2 w0 = wl[0];
                     // the remainder channel of this lane's line (RT): intensity, and
                     // its central-cell contributions to J0 (and J_eff, L*)
@@ -711,7 +712,11 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                 a.LS[(size_t)node * a.L + lane + 32] = (st == 0) ? accLb.value() : 0.0;
             }
         }
-        if (lane == 0) a.status[node] = st;
+        if (lane == 0) {
+            a.status[node] = st;
+            if (a.segs) a.segs[node] = node_seg;
+        }
+        nseg += (unsigned long long)node_seg;
         __syncwarp();
     }
     // segment count (every lane holds the same count)

@@ -294,6 +294,15 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
 std::mutex g_rs_mutex;
 unsigned char *g_rs_ptr[64] = {};
 
+// The host side of each call's line constants, direction and channel
+// tables.  Kept in static storage (not on the call's stack) so that the
+// memory a copy reads from stays valid after the call returns; filled and
+// copied under g_rs_tables_mutex.
+std::mutex g_rs_tables_mutex;
+RsLine g_rs_hlines[RS_MAX_LINES];
+double g_rs_hdirs[6 * RS_MAX_DIRS];
+float g_rs_hch[2 * RS_MAX_CH];
+
 }  // namespace
 
 extern "C" int portal_radiation_field_static(
@@ -325,42 +334,63 @@ extern "C" int portal_radiation_field_static(
         scratch = g_rs_ptr[dev];
     }
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    // line constants
-    RsLine h[RS_MAX_LINES];
     for (int k = 0; k < r_num; k++) {
         const int lo = r_trans[2 * k] - 1, up = r_trans[2 * k + 1] - 1;
         if (lo < 0 || lo >= nlev || up < 0 || up >= nlev) return PORTAL_ERR_ARG;
-        h[k].nu = nu[k]; h[k].A = t_Aji[k]; h[k].B = t_Bij[k]; h[k].kd = kd_v[k];
-        h[k].glo = 2.0 * j_lev[lo] + 1.0; h[k].gup = 2.0 * j_lev[up] + 1.0;
-        h[k].bb_cmb = 1.4744995e-50 * std::pow(nu[k], 3.0) * std::pow(std::exp(4.79924e-11 / 2.73 * nu[k]) - 1.0, -1.0);
-        h[k].lo = lo; h[k].up = up;
     }
-    if (cudaMemcpyToSymbolAsync(c_rs_lines, h, sizeof(RsLine) * r_num, 0, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return PORTAL_ERR_CUDA;
-    // direction and channel tables into the static array
     std::vector<double> xth;
     const int ndir = legendre_all(nth, nph, xth);
     if (ndir > RS_MAX_DIRS) return PORTAL_ERR_ARG;
-    std::vector<double> dt(6 * (size_t)ndir);
-    for (int k = 0; k < ndir; k++) {
-        const double mu = xth[3 * k], ph = xth[3 * k + 1], w = xth[3 * k + 2];
-        const double th = std::acos(mu);
-        dt[6 * k] = std::cos(th); dt[6 * k + 1] = std::sin(th);
-        dt[6 * k + 2] = std::cos(ph); dt[6 * k + 3] = std::sin(ph);
-        dt[6 * k + 4] = w; dt[6 * k + 5] = w * (3.0 * mu * mu - 1.0) / 2.0 / std::sqrt(2.0);
-    }
     const int nch = 2 * nvel + 1;
-    std::vector<float> ct(2 * RS_MAX_CH, 0.f);
-    const double spi = std::sqrt(std::acos(-1.0));
-    for (int i = 0; i < nch; i++) {
-        const double q0 = 2.0 * (i - nvel) / nvel;
-        ct[i] = (float)q0;
-        ct[RS_MAX_CH + i] = (float)(std::exp(-q0 * q0) * 2.0 / (spi * nvel));
+    {
+        std::lock_guard<std::mutex> lk(g_rs_tables_mutex);
+        // line constants
+        RsLine *h = g_rs_hlines;
+        for (int k = 0; k < r_num; k++) {
+            const int lo = r_trans[2 * k] - 1, up = r_trans[2 * k + 1] - 1;
+            h[k].nu = nu[k]; h[k].A = t_Aji[k]; h[k].B = t_Bij[k]; h[k].kd = kd_v[k];
+            h[k].glo = 2.0 * j_lev[lo] + 1.0; h[k].gup = 2.0 * j_lev[up] + 1.0;
+            h[k].bb_cmb = 1.4744995e-50 * std::pow(nu[k], 3.0) * std::pow(std::exp(4.79924e-11 / 2.73 * nu[k]) - 1.0, -1.0);
+            h[k].lo = lo; h[k].up = up;
+        }
+        // direction and channel tables, copied into the static device array
+        double *dt = g_rs_hdirs;
+        for (int k = 0; k < ndir; k++) {
+            const double mu = xth[3 * k], ph = xth[3 * k + 1], w = xth[3 * k + 2];
+            const double th = std::acos(mu);
+            dt[6 * k] = std::cos(th); dt[6 * k + 1] = std::sin(th);
+            dt[6 * k + 2] = std::cos(ph); dt[6 * k + 3] = std::sin(ph);
+            dt[6 * k + 4] = w; dt[6 * k + 5] = w * (3.0 * mu * mu - 1.0) / 2.0 / std::sqrt(2.0);
+        }
+        float *ct = g_rs_hch;
+        for (int i = 0; i < 2 * RS_MAX_CH; i++) ct[i] = 0.f;
+        const double spi = std::sqrt(std::acos(-1.0));
+        for (int i = 0; i < nch; i++) {
+            const double q0 = 2.0 * (i - nvel) / nvel;
+            ct[i] = (float)q0;
+            ct[RS_MAX_CH + i] = (float)(std::exp(-q0 * q0) * 2.0 / (spi * nvel));
+        }
+        if (cudaMemcpyToSymbolAsync(c_rs_lines, h, sizeof(RsLine) * r_num, 0, cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(scratch + RS_OFF_DIRS, dt, 6 * sizeof(double) * (size_t)ndir, cudaMemcpyHostToDevice,
+                            st) != cudaSuccess ||
+            cudaMemcpyAsync(scratch + RS_OFF_CH, ct, 2 * RS_MAX_CH * sizeof(float), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess)
+            return PORTAL_ERR_CUDA;
     }
-    if (cudaMemcpyAsync(scratch + RS_OFF_DIRS, dt.data(), dt.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(scratch + RS_OFF_CH, ct.data(), ct.size() * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemsetAsync(scratch, 0, 256, st) != cudaSuccess)   // the node counter starts at zero
+    if (cudaMemsetAsync(scratch, 0, 256, st) != cudaSuccess)   // the node counter starts at zero
         return PORTAL_ERR_CUDA;
+    // the rows of the non-bulk nodes, which the kernel does not visit, are
+    // zero as in portal_radiation_field
+    if (bulk_node_num < node_num) {
+        const size_t rest = (size_t)(node_num - bulk_node_num);
+        if (cudaMemsetAsync(J0 + (size_t)r_num * bulk_node_num, 0, rest * r_num * sizeof(double), st) !=
+                cudaSuccess ||
+            cudaMemsetAsync(J2 + (size_t)r_num * bulk_node_num, 0, rest * r_num * sizeof(double), st) !=
+                cudaSuccess ||
+            (status && cudaMemsetAsync(status + bulk_node_num, 0, rest * sizeof(int), st) != cudaSuccess))
+            return PORTAL_ERR_CUDA;
+    }
     RsArgs a;
     a.N = node_num; a.bulk = bulk_node_num; a.nlev = nlev; a.L = r_num; a.nvel = nvel; a.nch = nch;
     a.ndir = ndir; a.n_depth = n_depth; a.maxne = maxne; a.dx32 = (float)dx; a.tdx = tx * dx;
