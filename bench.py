@@ -16,10 +16,11 @@ main_para.f90:210-257 of the reference.  Workload: the power-law sphere with
            reads pol_pops back;
   cpu_baseline  the FP64 oracle port (OpenMP over nodes like the reference)
            on this host's cores, on a bounded sample of the same nodes;
-  convergence   time to a converged Lambda iteration (1e-6 relative change
-           per pass) on a held-out 16,384-point turbulent cube: plain, Ng,
-           accelerated (local operator + Ng), warm-started by the MLP the
-           run trains on eight other cubes, and warm-started + accelerated.
+  convergence   time to converged populations (within 1e-6 of a reference
+           fixed point, rho^0_0 and rho^2_0) on a held-out 16,384-point
+           turbulent cube: plain, Ng, accelerated (local operator + Ng),
+           warm-started by the MLP the run trains on eight other cubes, and
+           warm-started + accelerated.
 
 --impl reference times that CPU port alone on the same workload.
 Multi-GPU: every rank runs its own replica of the workload (weak scaling);
@@ -191,14 +192,32 @@ def reference_arm(args, rank, world):
     return 0
 
 
-def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
-    """Time to a converged Lambda iteration (largest relative change of
-    rho^0_0 per pass below 1e-6) on a held-out turbulent cube, plain against
-    the accelerated (local operator + Ng every 4 passes) and the warm-started
-    iterations.  The network is trained here, by the library's kernels, on
-    the converged solutions of n_train seeded cubes of the same recipe."""
+def _qi_errors(cube, ref_cube):
+    """Largest |Q/I| and |U/I| difference of an image against a reference
+    image of the same cloud (pixels and channels where the reference I is
+    above 1e-3 of its peak; the denominators of the image parity tests)."""
+    I, Q, U = ref_cube[0], ref_cube[1], ref_cube[2]
+    ok = np.isfinite(I) & np.isfinite(Q) & np.isfinite(U)
+    Ipk = np.abs(I[ok]).max()
+    den = np.maximum(np.abs(I), 1e-3 * Ipk)
+    dq = np.where(ok, np.abs(cube[1] - Q) / den, 0.0)
+    du = np.where(ok, np.abs(cube[2] - U) / den, 0.0)
+    return float(max(dq.max(), du.max()))
+
+
+def convergence_leg(device, n_points=16384, n_train=8, epochs=60, target=1e-6):
+    """Time to converged populations on a held-out turbulent cube: plain,
+    Ng, accelerated (local operator + Ng every 4 passes), warm-started by the
+    MLP the run trains on n_train other cubes, and warm-started +
+    accelerated.  'Converged' is measured, not inferred from the change per
+    pass: a reference fixed point is converged far past the target first,
+    and each method's time is that of a run of exactly the passes it needs
+    to bring rho^0_0 (relative) and rho^2_0 / rho^0_0 within `target` of it
+    (portal_gb300.convergence).  Each method's Stokes image (65 x 65 pixels x
+    33 channels, line 1-0 at 45 degrees) is compared with the reference's."""
     import torch
     import portal_gb300 as pg
+    from portal_gb300 import convergence as conv
     from portal_gb300 import synth
     from portal_gb300.warmstart import WarmStart
 
@@ -207,7 +226,17 @@ def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
     out = {"workload": "turbulent cube (lognormal density sigma_ln 1.5, mean 1e4 cm^-3; k^-11/3 velocity, "
                        "1 km/s rms; field along x + equal turbulent part), %d points, 20-level rotor, 16x16 "
                        "directions, 65 channels, kmax 2; held-out seed 300" % n_points,
-           "tol": 1e-6}
+           "target": target, "criterion": "max relative error of rho^0_0 and max |d rho^2_0|/rho^0_0 "
+                                          "against the reference fixed point, levels above 1e-12 of each "
+                                          "node's largest"}
+    im = dict(l1=[1], l2=[2], th_inc=0.78539816339, ph_az=0.0, nvel=16, dvel=100.0, v0=0.0, im_pix=32,
+              im_size=0.7)
+
+    def image(ctx, pp):
+        cube, _ = ctx.image(im["l1"], im["l2"], im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
+                            im["im_pix"], im["im_size"], pol_pops=pp, quantities=3)
+        return cube[:3, 0].astype(np.float64)
+
     with WarmStart(mol.j_lev, seed=1, device=device) as ws, pg.Context(device) as ctx:
         ctx.set_molecule(mol)
         t0 = time.perf_counter()
@@ -225,30 +254,42 @@ def convergence_leg(device, n_points=16384, n_train=8, epochs=60):
                            "data_seconds": t1 - t0, "fit_seconds": t2 - t1,
                            "loss_first_last": [float(losses[0]), float(losses[-1])]}
         cl = synth.turbulent_cube(n_points, 300, mol, grid=32)
-        ref = None
+        live = np.zeros(cl.node_num, dtype=bool)
+        live[:cl.bulk_node_num] = cl.ab_all[:cl.bulk_node_num] > 0
+
+        def set_cloud():
+            ctx.set_cloud(cl)
+
+        set_cloud()
+        t0 = time.perf_counter()
+        ref, rec = conv.reference_solution(ctx, rc)
+        rec["seconds"] = time.perf_counter() - t0
+        out["reference"] = rec
+        ref_img = image(ctx, ref)
         for name, warm, ng, lo in (("plain", False, 0, False), ("ng", False, 4, False),
                                    ("accelerated", False, 4, True), ("warm", True, 0, False),
                                    ("warm_accelerated", True, 4, True)):
-            ctx.set_cloud(cl)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            if warm:
-                pp, _, n, res, _ = ws.solve(ctx, rc, tol=1e-6, max_iter=3000, ng_period=ng, local_operator=lo)
-            else:
-                pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=3000, ng_period=ng,
-                                                      local_operator=lo)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            r0 = pp[:, 0::2]
-            if ref is None:
-                ref = r0
-            out[name] = {"passes": int(n) + (1 if warm else 0), "seconds": dt,
-                         "final_residual": float(res[-1]),
-                         "max_rel_diff_vs_plain": float(np.abs(r0 - ref).max() / np.abs(ref).max())}
+            r = conv.time_to_error(ctx, set_cloud, rc, ref, live, target=target, ng_period=ng, local_operator=lo,
+                                   warm=ws if warm else None, sync=torch.cuda.synchronize)
+            r["qi_abs_err"] = _qi_errors(image(ctx, r.pop("pol_pops")), ref_img)
+            out[name] = r
+        # where the change-per-pass rule (tol 1e-6) stops, and how far that is
+        # from the fixed point
+        for name, ng, lo in (("plain", 0, False), ("accelerated", 4, True)):
+            set_cloud()
+            pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=target, max_iter=3000, ng_period=ng, local_operator=lo)
+            e0, e2 = conv.rho_errors(pp, ref, live)
+            out[name]["residual_rule"] = {"passes": int(n), "last_change": float(res[-1]), "err_rho00": e0,
+                                          "err_rho20": e2}
     out["speedup_vs_plain"] = {k: out["plain"]["seconds"] / out[k]["seconds"]
                                for k in ("ng", "accelerated", "warm", "warm_accelerated")}
-    out["note"] = ("passes of warm runs include the radiation-field pass that feeds the network; "
-                   "wall time on the host around each call, network inference included")
+    out["warm_gain"] = {"passes_plain_over_warm": out["plain"]["passes"] / out["warm"]["passes"],
+                        "seconds_accelerated_over_warm_accelerated":
+                            out["accelerated"]["seconds"] / out["warm_accelerated"]["seconds"],
+                        "training_seconds": out["training"]["data_seconds"] + out["training"]["fit_seconds"]}
+    out["note"] = ("seconds: host wall time of one call of exactly the passes the method needs to reach the "
+                   "target (feature pass and network inference included for warm runs); passes of warm runs "
+                   "include the feature pass; qi_abs_err against the reference fixed point's image")
     return out
 
 

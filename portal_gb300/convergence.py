@@ -1,0 +1,115 @@
+"""Time to a converged Lambda iteration, measured against its fixed point.
+
+``Context.lambda_iterate`` stops when one pass changes rho^0_0 by less than
+``tol`` (the relative residual).  For a slowly contracting iteration that
+says little about the distance to the fixed point: with a contraction rate
+q per pass the remaining error is about residual * q / (1 - q), 25x the
+residual at q = 0.96.  This module measures the distance itself:
+
+* ``reference_solution`` converges the iteration far past the target (the
+  accelerated iteration, then plain passes until the change stops
+  shrinking) and reports the plain change per pass it ends at, the noise
+  floor of the FP32 radiation field;
+* ``rho_errors`` is the largest relative error of rho^0_0 and the largest
+  error of rho^2_0 relative to rho^0_0 over the live nodes and their
+  significant levels (those above ``floor`` of the node's largest rho^0_0,
+  the same rule as the residual);
+* ``time_to_error`` runs one method in short chunks of passes (each call
+  continues from the context's populations), stops at the first chunk whose
+  populations are within ``target`` of the reference, then repeats the
+  method in one call of exactly that many passes and times it: the time to
+  converged populations, with no measurement inside the timed run.
+
+The methods are those of ``lambda_iterate`` (plain, Ng, local operator) and
+the learned warm start (``WarmStart``), each an independent route to the
+same fixed point.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+TINY_TOL = 1e-300   # a tolerance no pass meets: run exactly max_iter passes
+
+
+def rho_errors(pp, ref, live, floor: float = 1e-12):
+    """(max relative error of rho^0_0, max |d rho^2_0| / rho^0_0) of pol_pops
+    pp against ref (both (N, 2 nlev)) over the live rows and the levels above
+    floor of each node's largest reference rho^0_0."""
+    q0 = np.asarray(ref)[live][:, 0::2]
+    q2 = np.asarray(ref)[live][:, 1::2]
+    r0 = np.asarray(pp)[live][:, 0::2]
+    r2 = np.asarray(pp)[live][:, 1::2]
+    big = np.abs(q0).max(axis=1, keepdims=True)
+    sig = np.abs(q0) >= floor * big
+    den = np.where(sig, np.abs(q0), 1.0)
+    e0 = np.where(sig, np.abs(r0 - q0) / den, 0.0)
+    e2 = np.where(sig, np.abs(r2 - q2) / den, 0.0)
+    bad0 = ~np.isfinite(e0)
+    bad2 = ~np.isfinite(e2)
+    return (float(np.inf) if bad0.any() else float(e0.max()),
+            float(np.inf) if bad2.any() else float(e2.max()))
+
+
+def reference_solution(ctx, rc, *, tol: float = 1e-10, max_iter: int = 600, extra_plain: int = 40):
+    """A fixed point of the plain pass to well below 1e-6: the accelerated
+    iteration (local operator + Ng every 4 passes) to tol, then plain passes
+    while their change keeps falling (at most extra_plain).  Returns
+    (pol_pops, record) where record holds the passes and the last plain
+    change per pass."""
+    pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=tol, max_iter=max_iter, ng_period=4, local_operator=True)
+    changes = []
+    for _ in range(extra_plain):
+        pp2, _, _, r, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=1)
+        changes.append(float(r[0]))
+        pp = pp2
+        if len(changes) >= 3 and changes[-1] >= 0.9 * min(changes[:-1]):
+            break
+    return pp, {"accelerated_passes": int(n), "accelerated_last_change": float(res[-1]),
+                "plain_passes": len(changes), "plain_change_last": changes[-1] if changes else None,
+                "plain_change_min": min(changes) if changes else None}
+
+
+def time_to_error(ctx, set_cloud, rc, ref, live, *, target: float = 1e-6, floor: float = 1e-12,
+                  ng_period: int = 0, local_operator: bool = False, warm=None, max_passes: int = 3000,
+                  sync=None):
+    """Passes and wall time for one method to reach populations within
+    `target` of `ref` (rho^0_0 relative and rho^2_0 / rho^0_0).
+
+    set_cloud() must put the context back at the starting populations.  warm
+    is a WarmStart (its feature pass and prediction are part of the timed
+    run) or None.  Returns a dict: passes (the iteration's; the warm start's
+    feature pass is counted as one more), seconds of the timed run,
+    err_rho00 / err_rho20 of its result, and the errors after each chunk of
+    the search ("trace": passes, err_rho00, err_rho20)."""
+    chunk = ng_period if ng_period else 1
+    set_cloud()
+    sp = warm.start(ctx, rc) if warm is not None else None
+    passes, trace, reached = 0, [], False
+    while passes < max_passes:
+        pp, _, n, _, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=chunk, start_pops=sp, ng_period=ng_period,
+                                            local_operator=local_operator)
+        sp = None
+        passes += n
+        e0, e2 = rho_errors(pp, ref, live, floor)
+        trace.append((passes, e0, e2))
+        if e0 <= target and e2 <= target:
+            reached = True
+            break
+    # the timed run: the same passes in one call from the start
+    set_cloud()
+    if sync:
+        sync()
+    t0 = time.perf_counter()
+    sp = warm.start(ctx, rc) if warm is not None else None
+    pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=passes, start_pops=sp, ng_period=ng_period,
+                                          local_operator=local_operator)
+    if sync:
+        sync()
+    dt = time.perf_counter() - t0
+    e0, e2 = rho_errors(pp, ref, live, floor)
+    # the plain change per pass the method would see at its stopping point
+    return {"passes": int(n) + (1 if warm is not None else 0), "seconds": dt, "reached": reached,
+            "err_rho00": e0, "err_rho20": e2, "last_change": float(res[-1]), "pol_pops": pp,
+            "trace": [(int(a), float(b), float(c)) for a, b, c in trace[:: max(1, len(trace) // 40)]]}

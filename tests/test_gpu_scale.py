@@ -153,6 +153,7 @@ def test_sphere4k_full_image_cube(built_lib, sphere4k, sphere4k_oracle):
     _report("sphere4k image", **e)
     _report("sphere4k image chain", **ec)
     assert np.isfinite(cube[:4]).all()
+    assert not np.array_equal(chain[:4], cube[:4])   # the chain images other populations
     assert e["I"] < 1e-4 and e["tau"] < 1e-4 and e["QI"] < 1e-4 and e["UI"] < 1e-4
     assert ec["I"] < 1e-3 and ec["QI"] < 1e-4 and ec["UI"] < 1e-4
 

@@ -1,7 +1,5 @@
 """The learned warm start: target / start-population conversions (CPU), and
 what the trained network gains over the iteration without it (GPU)."""
-import time
-
 import numpy as np
 import pytest
 
@@ -52,13 +50,20 @@ def test_start_pops_are_never_masers_and_stay_in_the_training_range():
 @pytest.mark.gpu
 def test_trained_network_reduces_passes_to_the_same_fixed_point(built_lib):
     """Train on five seeded turbulent cubes (8,192 points, 10-level rotor),
-    then iterate a held-out cube from LTE and from the network's prediction,
-    plain and accelerated (local operator + Ng)."""
+    then converge a held-out cube from LTE and from the network's
+    prediction, plain and accelerated (local operator + Ng).  Converged
+    means within 1e-6 of a reference fixed point (rho^0_0 relative,
+    rho^2_0 relative to rho^0_0), measured, not inferred from the change per
+    pass; each method's Stokes image matches the FP64 oracle's image of the
+    reference populations (Q/I and U/I within 1e-4)."""
+    import oracle
     import portal_gb300 as pg
+    from portal_gb300 import convergence as conv
     from portal_gb300.warmstart import WarmStart
 
     mol = synth.linear_rotor(10)
     rc = synth.RunConfig(nth=12, nph=12, nvel=16, kmax=2, gvec=synth.gauge_vector(4))
+    im = dict(th_inc=0.78539816339, ph_az=0.0, nvel=8, dvel=100.0, v0=0.0, im_pix=16, im_size=0.7)
     with WarmStart(mol.j_lev, seed=1) as ws, pg.Context(0) as ctx:
         ctx.set_molecule(mol)
         Xs, Ys = [], []
@@ -71,26 +76,45 @@ def test_trained_network_reduces_passes_to_the_same_fixed_point(built_lib):
         losses = ws.fit(np.concatenate(Xs), np.concatenate(Ys), epochs=60)
         assert losses[-1] < 0.8 * losses[0]
         cl = synth.turbulent_cube(8192, 300, mol, grid=32)
+        live = np.zeros(cl.node_num, dtype=bool)
+        live[:cl.bulk_node_num] = cl.ab_all[:cl.bulk_node_num] > 0
+        ctx.set_cloud(cl)
+        ref, rec = conv.reference_solution(ctx, rc)
+        # the reference sits far below the target
+        assert rec["plain_change_last"] < 1e-7, rec
         runs = {}
         for name, warm, ng, lo in (("plain", False, 0, False), ("warm", True, 0, False),
                                    ("acc", False, 4, True), ("warm+acc", True, 4, True)):
-            ctx.set_cloud(cl)
-            t0 = time.perf_counter()
-            if warm:
-                pp, _, n, res, _ = ws.solve(ctx, rc, tol=1e-6, max_iter=2000, ng_period=ng, local_operator=lo)
-            else:
-                pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=2000, ng_period=ng,
-                                                      local_operator=lo)
-            runs[name] = (n, time.perf_counter() - t0, pp, res)
-    for name, (n, _, _, res) in runs.items():
-        assert res[-1] < 1e-6, name
-    ref = runs["plain"][2][:, 0::2]
-    for name in ("warm", "acc", "warm+acc"):
-        got = runs[name][2][:, 0::2]
-        assert np.abs(got - ref).max() <= 5e-5 * np.abs(ref).max(), name
+            runs[name] = conv.time_to_error(ctx, lambda: ctx.set_cloud(cl), rc, ref, live, ng_period=ng,
+                                            local_operator=lo, warm=ws if warm else None)
+        imgs = {}
+        for name, r in runs.items():
+            imgs[name], st = ctx.image([1], [2], im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
+                                       im["im_pix"], im["im_size"], pol_pops=r["pol_pops"])
+    for name, r in runs.items():
+        print("CONVERGENCE %s: passes %d, %.2f s, err rho00 %.2e rho20 %.2e" %
+              (name, r["passes"], r["seconds"], r["err_rho00"], r["err_rho20"]))
+        assert r["reached"] and r["err_rho00"] <= 1e-6 and r["err_rho20"] <= 1e-6, name
     # the network's gain: fewer passes from its prediction than from LTE,
     # with and without the accelerations (the feature pass counts as one)
-    assert runs["warm"][0] + 1 < 0.85 * runs["plain"][0]
-    assert runs["warm+acc"][0] + 1 <= runs["acc"][0]
+    assert runs["warm"]["passes"] < 0.85 * runs["plain"]["passes"]
+    assert runs["warm+acc"]["passes"] <= runs["acc"]["passes"]
     # the accelerated, warm-started iteration against the plain method
-    assert runs["plain"][1] > 3.0 * runs["warm+acc"][1]
+    assert runs["plain"]["seconds"] > 3.0 * runs["warm+acc"]["seconds"]
+    # the converged populations' image against the FP64 oracle's image of
+    # the reference fixed point
+    P = oracle.OracleProblem(cl, mol)
+    npx, nch = 2 * im["im_pix"] + 1, 2 * im["nvel"] + 1
+    ocube, _, nf = P.image([1], [2], ref, im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
+                           im["im_pix"], im["im_size"])
+    assert nf == 0
+    o = ocube.reshape(8, npx, npx, 1, nch).transpose(0, 3, 4, 2, 1)
+    oI = o[0, 0]
+    Ipk = np.abs(oI).max()
+    den = np.maximum(np.abs(oI), 1e-3 * Ipk)
+    for name, c in imgs.items():
+        qi = max((np.abs(c[1, 0] - o[1, 0]) / den).max(), (np.abs(c[2, 0] - o[2, 0]) / den).max())
+        print("CONVERGENCE %s image: Q/I, U/I abs err %.2e, I %.2e of peak" %
+              (name, qi, np.abs(c[0, 0] - oI).max() / Ipk))
+        assert qi < 1e-4, name
+        assert np.abs(c[0, 0] - oI).max() < 1e-4 * Ipk, name
