@@ -99,5 +99,19 @@ module portal_gpu
       type(c_ptr), value :: ctx
       integer(c_int) :: segments(*)
     end function
+    integer(c_int) function portal_set_depolarization(ctx, mode) bind(C, name="portal_set_depolarization")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: mode
+    end function
+    integer(c_int) function portal_adj_list(ctx, node_num, del_num, del_tri, max_ne_temp, del_ne, &
+        del_num_ne, max_ne, ms) bind(C, name="portal_adj_list")
+      import :: c_ptr, c_int, c_long_long
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: node_num, max_ne_temp
+      integer(c_long_long), value :: del_num
+      integer(c_int) :: del_tri(4,*), del_num_ne(*), max_ne
+      type(c_ptr), value :: del_ne, ms
+    end function
   end interface
 end module

@@ -138,6 +138,23 @@ int portal_radiation_field_split(portal_ctx *ctx, int nth, int nph, int nvel, co
 int portal_solve_se(portal_ctx *ctx, int kmax, const double *J0, const double *J2,
                     double *pol_pops, double *rates, double *JJ_20, int *status);
 
+/* Depolarising collisions in the statistical equilibrium: the D^(K) rates
+ * of setup_stateq's col_dep slot (pop_eqs.f90:642-648), which the reference
+ * computes with de_polarization (depol.f90:242-317, the sudden
+ * approximation of Morris 1985 from the rates out of the lowest level, first
+ * collision partner) and make_depolarization_temp (depol.f90:319-360, times
+ * n_H2 1e-6) but never switches on (main_sub.f90:96 passes D0 = 0).
+ *   mode 0  off (the default, the reference's run);
+ *   mode 1  D^(K) on the K = K' >= 2 diagonal entries of each level, where
+ *           setup_stateq assigns col_dep;
+ *   mode 2  col_dep as setup_stateq's code reads it: the last assigned value
+ *           also enters every later diagonal-block entry (the variable is
+ *           never reset), which mode 1 leaves out.
+ * Needs j_lev(i) = i - 1 (de_polarization's own assumption); a molecule
+ * without it fails the next portal_solve_se with PORTAL_ERR_ARG.  Applies
+ * to portal_solve_se, portal_lambda_iterate and batches built afterwards. */
+int portal_set_depolarization(portal_ctx *ctx, int mode);
+
 /* Lambda iteration of the node loop: repeat portal_radiation_field +
  * portal_solve_se, setting the level populations of every bulk node from
  * the SE solution between passes, n_J = n_mol sqrt(2J+1) rho^0_0(J)
@@ -295,6 +312,20 @@ int portal_last_kernel_times(const portal_ctx *ctx, double *times_ms, int *launc
  * NULL): J0, J2 (r_num,N), pol_pops(N, 2*nlev), status(N).  For models run by
  * a batch, whose results stay on the device. */
 int portal_get_results(portal_ctx *ctx, double *J0, double *J2, double *pol_pops, int *status);
+
+/* The Delaunay neighbour lists of the cloud, built on the device:
+ * adj_list_no_delaunay (miscellaneous.f90:910-1015) with SortUnique's sort
+ * and de-duplication of each node's list (unique.f90:43-59), the step of
+ * eat_lime_no_delaunay (eat_lime.f90:282) that turns grid.vtk's tetrahedra
+ * into del_ne.  del_tri(4, del_num) holds the tetrahedra's vertices as
+ * grid.vtk lists them (0-based); outputs: del_ne(node_num, max_ne_temp)
+ * column-major (1-based ids, ascending per node, 0 in the unused slots) or
+ * NULL, del_num_ne(node_num), max_ne (the longest list, main_para.f90's
+ * maxne), and the device time in ms (or NULL).  A node whose unsorted list
+ * exceeds max_ne_temp fails with PORTAL_ERR_ARG, as the reference stops
+ * there (miscellaneous.f90:995-1000). */
+int portal_adj_list(portal_ctx *ctx, int node_num, long long del_num, const int *del_tri, int max_ne_temp,
+                    int *del_ne, int *del_num_ne, int *max_ne, double *ms);
 
 /* Ray segments of every node in the last radiation-field pass:
  * segments(N), the sum over the node's rays of trace_out's node_count

@@ -33,7 +33,7 @@ class OrcMolecule(C.Structure):
     _fields_ = [("nlev", C.c_int), ("r_num", C.c_int), ("c_num", C.c_int), ("c_temp", C.c_int),
                 ("c_par", C.c_int), ("j_lev", P_I), ("e_levs", P_D), ("r_trans", P_I),
                 ("A", P_D), ("nu", P_D), ("Bij", P_D), ("kd_v", P_D), ("c_trans", P_I),
-                ("col_temps", P_D), ("C", P_D)]
+                ("col_temps", P_D), ("C", P_D), ("depol", C.c_int)]
 
 
 def build() -> str:
@@ -73,9 +73,11 @@ class OracleProblem:
     """Holds the reference-layout arrays of one cloud + molecule so that the
     C structs' pointers stay valid."""
 
-    def __init__(self, cloud, mol, star=None):
+    def __init__(self, cloud, mol, star=None, depol=0):
         """star: None, or (T_star [K], R_star [m], (x, y, z) as the input file
-        gives them) for star_mod = 1."""
+        gives them) for star_mod = 1.  depol: the depolarising collisions of
+        the SE (0 off as main_sub.f90:96, 1 at the K = K' >= 2 diagonal
+        entries, 2 as setup_stateq's code reads col_dep)."""
         self.cloud, self.mol = cloud, mol
         N = cloud.node_num
         self.xyz = np.ascontiguousarray(cloud.xyz, dtype=np.float64)          # (N,3) == X(3,N)
@@ -115,7 +117,7 @@ class OracleProblem:
         self.m = OrcMolecule(mol.nlev, mol.r_num, mol.c_num, mol.c_temp, mol.c_par, _p(self.j_lev, P_I),
                              _p(self.e_levs), _p(self.r_trans, P_I), _p(self.A), _p(self.nu),
                              _p(self.Bij), _p(self.kd_v), _p(self.c_trans, P_I),
-                             _p(self.col_temps), _p(self.Cr))
+                             _p(self.col_temps), _p(self.Cr), int(depol))
 
     def radiation_field(self, rc, node_lo=1, node_hi=None, nthreads=0):
         """J0, J2 of shape (N, r_num), per-node status, total segments."""
@@ -251,6 +253,23 @@ def star_all(nth, nph, kvec, gvec, bvec, dOm):
     k, g, b = (np.ascontiguousarray(v, dtype=np.float64) for v in (kvec, gvec, bvec))
     n = lib().orc_star_all(nth, nph, _p(k), _p(g), _p(b), C.c_double(dOm), C.byref(ns), _p(xth))
     return None if n < 0 else (xth[:n].copy(), ns.value)
+
+
+def de_polarization(mol, kmax):
+    """D0_all of de_polarization (depol.f90:242-317) as an array (kmax/2,
+    nlev, c_temp): [K/2 - 1, level, temperature] in cm^3/s; None where the
+    reference's assumption j_lev(i) = i - 1 fails."""
+    P = OracleProblem.__new__(OracleProblem)
+    j = np.ascontiguousarray(mol.j_lev, dtype=np.int32)
+    ct = np.ascontiguousarray(mol.c_trans, dtype=np.int32)
+    cr = np.ascontiguousarray(mol.C, dtype=np.float64)
+    tt = np.ascontiguousarray(mol.col_temps, dtype=np.float64)
+    m = OrcMolecule(mol.nlev, mol.r_num, mol.c_num, mol.c_temp, mol.c_par, _p(j, P_I), None, None, None, None,
+                    None, None, _p(ct, P_I), _p(tt), _p(cr), 1)
+    out = np.zeros((kmax // 2, mol.nlev, mol.c_temp))
+    rc = lib().orc_de_polarization(C.byref(m), kmax, _p(out))
+    del P
+    return None if rc != 0 else out
 
 
 def legendre_all(nth, nph):

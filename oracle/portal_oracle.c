@@ -919,13 +919,87 @@ void orc_coupling_constants(int which, int j, int k, int j2, int k2, double *c0,
     }
 }
 
+/* de_polarization depol.f90:242-317 (Morris 1985 Eq. B11 in the form of
+ * L&L04 Eq. 7.102).  C_j0 takes the rates of the collisional transitions
+ * whose lower level is level 1, indexed by their upper level; the sum runs
+ * over m = 1..2J with C_j0(:,m) -- level m, whose rate from level 1 is set
+ * for m >= 2 and never for m = 1 (the reference leaves C_j0(:,1) unset; 0
+ * here), and for m > nlev reads past the array (0 here).  The first
+ * partner's rates (t_Cji(:,:,1)) are used. */
+int orc_de_polarization(const orc_molecule *m, int kmax, double *D0_all)
+{
+    const int nlev = m->nlev, nT = m->c_temp, nk = kmax / 2;
+    for (int i = 0; i < nlev; i++)
+        if (m->j_lev[i] != i) return -1;   /* "only works if j_lev(i) = i-1" */
+    double *Cj0 = (double *)calloc((size_t)nT * nlev, sizeof(double));
+    for (int i = 0; i < m->c_num; i++)
+        if (m->c_trans[2 * i] == 1) {
+            int up = m->c_trans[2 * i + 1];
+            for (int l = 0; l < nT; l++) Cj0[l + (size_t)nT * (up - 1)] = m->C[l + (size_t)nT * i];
+        }
+    for (size_t q = 0; q < (size_t)nT * nlev * (nk > 0 ? nk : 1); q++) D0_all[q] = 0.0;
+#define D0A(l, i, k) D0_all[(size_t)(l) + (size_t)nT * ((size_t)(i - 1) + (size_t)nlev * (size_t)((k) / 2 - 1))]
+    for (int i = 2; i <= nlev; i++) {
+        int j = i - 1;
+        double lj2 = pow(2.0 * j + 1.0, 2.0);
+        for (int k = 2; k <= (2 * j < kmax ? 2 * j : kmax); k += 2) {
+            for (int l = 0; l < nT; l++) {
+                D0A(l, i, k) = 0.0;
+                for (int mm = 1; mm <= 2 * j; mm++) {
+                    double fac = pow(-1.0, mm) * (2.0 * mm + 1.0);
+                    double w1 = orc_wigner3j(2 * j, 2 * j, 2 * mm, 0, 0, 0);
+                    double w2 = orc_wigner6j(2 * j, 2 * j, 2 * mm, 2 * j, 2 * j, 0);
+                    double w3 = orc_wigner6j(2 * j, 2 * j, 2 * mm, 2 * j, 2 * j, 2 * k);
+                    double fac2 = w2 - w3;
+                    /* m runs to 2J, past the nlev columns of C_j0 for the upper half
+                     * of the levels (the reference reads beyond the array there); a
+                     * level that does not exist has no rate: 0 */
+                    double cj = (mm <= nlev) ? Cj0[l + (size_t)nT * (mm - 1)] : 0.0;
+                    D0A(l, i, k) = D0A(l, i, k) + lj2 * fac * w1 * w1 * fac2 * cj;
+                }
+            }
+        }
+    }
+#undef D0A
+    free(Cj0);
+    return 0;
+}
+
+/* make_depolarization_temp depol.f90:319-360.  Its loop over the table has
+ * no exit: every bracket (i-1, i) with col_temps(i) > T overwrites D0, so
+ * the last one, (nT-1, nT), sets it -- linear in that bracket, extrapolated
+ * below it -- whenever T < col_temps(nT).  At or above col_temps(nT) the
+ * reference leaves D0 unset (0 here). */
+void orc_make_depolarization_temp(const double *D0_all, int nlev, int nT, int kmax,
+                                  const double *col_temps, double T, double nH2, double *D0)
+{
+    const int nk = kmax / 2;
+    for (int q = 0; q < nlev * nk; q++) D0[q] = 0.0;
+    if (T <= col_temps[0])
+        for (int q = 0; q < nlev * nk; q++) D0[q] = D0_all[(size_t)nT * q];
+    for (int i = 2; i <= nT; i++) {
+        if (col_temps[i - 1] > T) {
+            double ddT = (T - col_temps[i - 2]) / (col_temps[i - 1] - col_temps[i - 2]);
+            for (int q = 0; q < nlev * nk; q++) {
+                double f1 = D0_all[(size_t)(i - 2) + (size_t)nT * q];
+                double f2 = D0_all[(size_t)(i - 1) + (size_t)nT * q];
+                D0[q] = f1 + ddT * (f2 - f1);
+            }
+        }
+    }
+    for (int q = 0; q < nlev * nk; q++) D0[q] = D0[q] * nH2 * 1e-6;
+}
+
 /* setup_stateq pop_eqs.f90:361-653.  Matrices column-major (c_dim,c_dim).
- * col_dep: the reference reads it before its first assignment for the
- * K=K' < 2 diagonal entries; D0 is all zeros (main_sub.f90:96), so it is 0
- * here throughout. */
+ * col_dep (pop_eqs.f90:642-648) is assigned D0(i1,k1) at the K = K' >= 2
+ * diagonal entries and read by every entry's Amat; the reference never
+ * initialises it (0 here) and passes D0 = 0 (main_sub.f90:96).  depol = 1
+ * applies D0 only where it is assigned; depol = 2 keeps the last assigned
+ * value in the later entries too, as the reference's code reads it. */
 void orc_setup_stateq(int c_dim, const int *count_array, int nlev, const int *j_lev,
                       const int *trans, int ntrans, int kmax, const double *AC, double Temp,
-                      double *Amat, double *A_mat, double *B_mat, double *C_mat)
+                      const double *D0, int depol, double *Amat, double *A_mat, double *B_mat,
+                      double *C_mat)
 {
     const double a_to_b = 6.781962e49;
     size_t nn = (size_t)c_dim * c_dim;
@@ -1053,8 +1127,9 @@ void orc_setup_stateq(int c_dim, const int *count_array, int nlev, const int *j_
                             M(C_mat, c1, c2) = M(C_mat, c1, c2) - C21;
                         }
                     }
+                    if (depol == 1) col_dep = 0.0;
                     if (k1 == k2 && k2 >= 2) {
-                        col_dep = 0.0; /* D0(i1,k1) = 0 */
+                        col_dep = (D0 && depol) ? D0[(i1 - 1) + nlev * (k1 / 2 - 1)] : 0.0;
                         M(C_mat, c1, c2) = M(C_mat, c1, c2) - col_dep;
                     }
                     M(Amat, c1, c2) = -1.0 * (rad_abs + rad_stim + col_abs + col_stim + col_dep);
@@ -1107,13 +1182,13 @@ static int lu_solve_e1(int n, double *A, double *x)
 
 /* get_rhovec em_coefs.f90:115-201 */
 int orc_get_rhovec(int c_dim, const int *count_array, int nlev, const int *j_lev, int ntrans,
-                   const int *trans, const double *AC, int kmax, double Temp, double *rhovec,
-                   double *rates)
+                   const int *trans, const double *AC, int kmax, double Temp, const double *D0,
+                   int depol, double *rhovec, double *rates)
 {
     size_t nn = (size_t)c_dim * c_dim;
     double *Amat = (double *)malloc(sizeof(double) * nn * 4);
     double *R_mat = Amat + nn, *B_mat = Amat + 2 * nn, *C_mat = Amat + 3 * nn;
-    orc_setup_stateq(c_dim, count_array, nlev, j_lev, trans, ntrans, kmax, AC, Temp, Amat,
+    orc_setup_stateq(c_dim, count_array, nlev, j_lev, trans, ntrans, kmax, AC, Temp, D0, depol, Amat,
                      R_mat, B_mat, C_mat);
     for (int cc = 0; cc < c_dim; cc++) Amat[(size_t)c_dim * cc] = 0.0;
     for (int i = 0; i < nlev; i++) {
@@ -1147,8 +1222,19 @@ int orc_node_matrix(const orc_cloud *c, const orc_molecule *m, int kmax, int nod
                 J0 + (size_t)m->r_num * (node - 1), J2 + (size_t)m->r_num * (node - 1), AC);
     size_t nn = (size_t)c_dim * c_dim;
     double *scr = (double *)malloc(sizeof(double) * nn * 3);
+    double *D0_all = NULL, *D0 = NULL;
+    if (m->depol && kmax >= 2) {
+        D0_all = (double *)malloc(sizeof(double) * (size_t)m->c_temp * nlev * (kmax / 2));
+        D0 = (double *)malloc(sizeof(double) * (size_t)nlev * (kmax / 2));
+        if (orc_de_polarization(m, kmax, D0_all) == 0)
+            orc_make_depolarization_temp(D0_all, nlev, m->c_temp, kmax, m->col_temps, c->t_kin[node - 1],
+                                         c->h2_dens[node - 1], D0);
+        else
+            memset(D0, 0, sizeof(double) * (size_t)nlev * (kmax / 2));
+    }
     orc_setup_stateq(c_dim, count_array, nlev, m->j_lev, all_trans, n_trans, kmax, AC,
-                     c->t_kin[node - 1], Amat, scr, scr + nn, scr + 2 * nn);
+                     c->t_kin[node - 1], D0, m->depol, Amat, scr, scr + nn, scr + 2 * nn);
+    free(D0_all); free(D0);
     *c_dim_out = c_dim;
     free(scr); free(AC); free(all_trans); free(count_array);
     return ORC_OK;
@@ -1161,16 +1247,19 @@ int orc_node_matrix(const orc_cloud *c, const orc_molecule *m, int kmax, int nod
  * rhovec and rt are the thread's work arrays.  Returns the node's status. */
 static int se_node(const orc_cloud *c, const orc_molecule *m, int kmax, const double *J0,
                    const double *J2, int c_dim, const int *count_array, int n_trans,
-                   const int *all_trans, int node, double *AC, double *rhovec, double *rt,
-                   double *pol_pops, double *rates)
+                   const int *all_trans, const double *D0_all, int node, double *AC, double *D0,
+                   double *rhovec, double *rt, double *pol_pops, double *rates)
 {
     int nlev = m->nlev, N = c->node_num;
     int st = ORC_OK;
     if (c->ab_all[node - 1] > 0.0 && !inside_star(c, node)) {
         orc_make_AC(m, c->h2_dens[node - 1], c->t_kin[node - 1], n_trans, all_trans,
                     J0 + (size_t)m->r_num * (node - 1), J2 + (size_t)m->r_num * (node - 1), AC);
+        if (D0_all)
+            orc_make_depolarization_temp(D0_all, nlev, m->c_temp, kmax, m->col_temps, c->t_kin[node - 1],
+                                         c->h2_dens[node - 1], D0);
         st = orc_get_rhovec(c_dim, count_array, nlev, m->j_lev, n_trans, all_trans, AC, kmax,
-                            c->t_kin[node - 1], rhovec, rates ? rt : NULL);
+                            c->t_kin[node - 1], D0_all ? D0 : NULL, m->depol, rhovec, rates ? rt : NULL);
         if (st != ORC_OK) {
             for (int i = 0; i < c_dim; i++) rhovec[i] = NAN;
             for (int i = 0; i < 3 * c_dim; i++) rt[i] = 0.0;
@@ -1221,6 +1310,14 @@ static int solve_se_impl(const orc_cloud *c, const orc_molecule *m, int kmax, co
     if (node_lo < 1) node_lo = 1;
     if (node_hi > c->bulk_node_num) node_hi = c->bulk_node_num;
     const int n_items = node_list ? n_list : (node_hi >= node_lo ? node_hi - node_lo + 1 : 0);
+    double *D0_all = NULL;
+    if (m->depol && kmax >= 2) {
+        D0_all = (double *)malloc(sizeof(double) * (size_t)m->c_temp * nlev * (kmax / 2));
+        if (orc_de_polarization(m, kmax, D0_all) != 0) {
+            free(D0_all); free(count_array); free(all_trans);
+            return -1;
+        }
+    }
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -1229,19 +1326,20 @@ static int solve_se_impl(const orc_cloud *c, const orc_molecule *m, int kmax, co
         double *AC = (double *)malloc(sizeof(double) * 5 * (n_trans + 1));
         double *rhovec = (double *)malloc(sizeof(double) * c_dim);
         double *rt = (double *)malloc(sizeof(double) * 3 * c_dim);
+        double *D0 = (double *)malloc(sizeof(double) * (size_t)nlev * (kmax / 2 + 1));
 #pragma omp for schedule(static)
         for (int it = 0; it < n_items; it++) {
             const int node = node_list ? node_list[it] : node_lo + it;
             int st = ORC_ERR_ARG;
             if (node >= 1 && node <= c->bulk_node_num)
-                st = se_node(c, m, kmax, J0, J2, c_dim, count_array, n_trans, all_trans, node, AC, rhovec,
-                             rt, pol_pops, rates);
+                st = se_node(c, m, kmax, J0, J2, c_dim, count_array, n_trans, all_trans, D0_all, node, AC, D0,
+                             rhovec, rt, pol_pops, rates);
             if (status) status[node_list ? it : node - 1] = st;
             if (st != ORC_OK) nfail++;
         }
-        free(AC); free(rhovec); free(rt);
+        free(AC); free(rhovec); free(rt); free(D0);
     }
-    free(count_array); free(all_trans);
+    free(count_array); free(all_trans); free(D0_all);
     return nfail;
 }
 

@@ -69,6 +69,12 @@ typedef struct {
     const int *c_trans;     /* (2,c_num) (lower, upper), 1-based               */
     const double *col_temps;/* (c_temp)                                        */
     const double *C;        /* (c_temp,c_num,c_par) cm^3/s                     */
+    /* depolarising collisions (depol.f90:242-360), D0 of setup_stateq's
+     * col_dep slot (pop_eqs.f90:642-648): 0 off (main_sub.f90:96 passes
+     * D0 = 0), 1 on the K = K' >= 2 diagonal entries where the reference
+     * assigns col_dep, 2 as the reference's code reads col_dep (the last
+     * assigned value stays in every later entry of the diagonal blocks). */
+    int depol;
 } orc_molecule;
 
 enum {
@@ -135,13 +141,27 @@ int orc_all_transitions(const orc_molecule *m, int *all_trans /* (2,r_num+c_num)
 void orc_make_AC(const orc_molecule *m, double nH2, double Temp, int n_trans,
                  const int *all_trans, const double *J0, const double *J2,
                  double *AC /* (5,n_trans) */);
+/* D0 (nlev, kmax/2): the node's depolarisation rates D^(K) [s^-1] of level
+ * i for K = 2, 4, .. at D0[(i-1) + nlev (K/2 - 1)], or NULL for D0 = 0;
+ * depol as orc_molecule.depol. */
 void orc_setup_stateq(int c_dim, const int *count_array, int nlev, const int *j_lev,
                       const int *trans, int ntrans, int kmax, const double *AC,
-                      double Temp, double *Amat, double *A_mat, double *B_mat,
-                      double *C_mat);
+                      double Temp, const double *D0, int depol, double *Amat, double *A_mat,
+                      double *B_mat, double *C_mat);
 int orc_get_rhovec(int c_dim, const int *count_array, int nlev, const int *j_lev,
                    int ntrans, const int *trans, const double *AC, int kmax,
-                   double Temp, double *rhovec, double *rates /* (3,c_dim) or NULL */);
+                   double Temp, const double *D0, int depol, double *rhovec,
+                   double *rates /* (3,c_dim) or NULL */);
+/* de_polarization depol.f90:242-317: D0_all (c_temp, nlev, kmax/2), the
+ * sudden-approximation depolarisation coefficients [cm^3 s^-1] of every
+ * level and K = 2, 4, .. <= min(2J, kmax) from the first partner's rates out
+ * of the lowest level.  Returns -1 unless j_lev(i) = i - 1 (the reference's
+ * assumption). */
+int orc_de_polarization(const orc_molecule *m, int kmax, double *D0_all);
+/* make_depolarization_temp depol.f90:319-360: D0 (nlev, kmax/2) [s^-1] at
+ * temperature T and n_H2 [m^-3]. */
+void orc_make_depolarization_temp(const double *D0_all, int nlev, int nT, int kmax,
+                                  const double *col_temps, double T, double nH2, double *D0);
 /* trace_node's SE half for nodes node_lo..node_hi: pol_pops (node_num, 2*nlev)
  * column-major, rates (node_num,3,2*nlev) or NULL. */
 int orc_solve_se(const orc_cloud *c, const orc_molecule *m, int kmax,

@@ -40,6 +40,7 @@ EXPORTS = (
     "portal_mlp_predict", "portal_warmstart_features", "portal_get_results",
     "portal_batch_create", "portal_batch_destroy", "portal_batch_last_error", "portal_batch_add",
     "portal_batch_prepare", "portal_batch_run", "portal_batch_config", "portal_node_segments",
+    "portal_set_depolarization", "portal_adj_list",
 )
 
 _lib = None
@@ -115,6 +116,8 @@ def lib() -> C.CDLL:
     L.portal_warmstart_features.argtypes = [C.c_void_p, P_F]
     L.portal_get_results.argtypes = [C.c_void_p, P_D, P_D, P_D, P_I]
     L.portal_node_segments.argtypes = [C.c_void_p, P_I]
+    L.portal_set_depolarization.argtypes = [C.c_void_p, C.c_int]
+    L.portal_adj_list.argtypes = [C.c_void_p, C.c_int, C.c_longlong, P_I, C.c_int, P_I, P_I, P_I, P_D]
     L.portal_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
     L.portal_batch_destroy.argtypes = [C.c_void_p]
     L.portal_batch_last_error.restype = C.c_char_p
@@ -218,6 +221,12 @@ class Context:
         T_s, R_s, X_s = star
         x = _f64(np.asarray(X_s, dtype=np.float64))
         self._check(lib().portal_set_star(self._h, 1, float(T_s), float(R_s), _p(x)))
+
+    def set_depolarization(self, mode: int):
+        """Depolarising collisions in the SE: 0 off (default), 1 on the
+        K = K' >= 2 diagonal entries, 2 as setup_stateq's code reads its
+        col_dep variable (see portal_set_depolarization)."""
+        self._check(lib().portal_set_depolarization(self._h, int(mode)))
 
     def set_populations(self, lev_p):
         self._check(lib().portal_set_populations(self._h, _p(_f64(lev_p))))
@@ -349,6 +358,21 @@ class Context:
         pp = np.zeros((2 * self.nlev, self.N)) if pops else None
         self._check(lib().portal_get_results(self._h, _p(J0), _p(J2), _p(pp), None))
         return J0, J2, (None if pp is None else pp.T.copy())
+
+    def adj_list(self, node_num, tets, max_ne_temp=None):
+        """Delaunay neighbour lists built on the device from the tetrahedra
+        (ntet, 4) 0-based: (del_ne as a (max_ne, node_num) C array == the
+        reference's del_ne(node_num, max_ne), del_num_ne, device ms).  The
+        CSR of synth.neighbours_from_tets follows from these two arrays."""
+        t = _i32(tets)
+        cap = int(max_ne_temp or 12 * 64)
+        dne = np.zeros((cap, node_num), dtype=np.int32)
+        num = np.zeros(node_num, dtype=np.int32)
+        mx = C.c_int(0)
+        ms = C.c_double(0.0)
+        self._check(lib().portal_adj_list(self._h, int(node_num), int(t.shape[0]), _p(t, P_I), cap, _p(dne, P_I),
+                                          _p(num, P_I), C.byref(mx), C.byref(ms)))
+        return dne[:mx.value].copy(), num, float(ms.value)
 
     def node_segments(self) -> np.ndarray:
         """Ray segments of every node in the last radiation-field pass (N,)."""

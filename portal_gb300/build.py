@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libportal_gb300.so")
 SOURCES = ["ctx.cu", "rf.cu", "rf_batch.cu", "rf_static.cu", "se.cu", "image.cu", "lambda.cu", "mlp.cu",
-           "warmstart.cu", "batch.cu", "wigner.cpp"]
+           "warmstart.cu", "batch.cu", "adjacency.cu", "wigner.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

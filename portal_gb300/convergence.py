@@ -6,10 +6,8 @@ says little about the distance to the fixed point: with a contraction rate
 q per pass the remaining error is about residual * q / (1 - q), 25x the
 residual at q = 0.96.  This module measures the distance itself:
 
-* ``reference_solution`` converges the iteration far past the target (the
-  accelerated iteration, then plain passes until the change stops
-  shrinking) and reports the plain change per pass it ends at, the noise
-  floor of the FP32 radiation field;
+* ``reference_solution`` runs the accelerated iteration far past the point
+  where its change per pass stops falling;
 * ``rho_errors`` is the largest relative error of rho^0_0 and the largest
   error of rho^2_0 relative to rho^0_0 over the live nodes and their
   significant levels (those above ``floor`` of the node's largest rho^0_0,
@@ -22,7 +20,13 @@ residual at q = 0.96.  This module measures the distance itself:
 
 The methods are those of ``lambda_iterate`` (plain, Ng, local operator) and
 the learned warm start (``WarmStart``), each an independent route to the
-same fixed point.
+same fixed point -- in exact arithmetic.  With the FP32 radiation field (J
+to ~5e-7 relative) each method's map has its own limit: a perturbation dJ
+of the plain map moves its fixed point by about dJ / (1 - q), q ~ 0.97 per
+pass on the turbulent cubes, so the plain and Ng limits lie ~2e-5 from the
+accelerated one (whose preconditioned map is far better conditioned) and
+no target below that is reachable by all methods.  The default target,
+3e-5, is the tightest one every method meets.
 """
 from __future__ import annotations
 
@@ -52,26 +56,18 @@ def rho_errors(pp, ref, live, floor: float = 1e-12):
             float(np.inf) if bad2.any() else float(e2.max()))
 
 
-def reference_solution(ctx, rc, *, tol: float = 1e-10, max_iter: int = 600, extra_plain: int = 40):
-    """A fixed point of the plain pass to well below 1e-6: the accelerated
-    iteration (local operator + Ng every 4 passes) to tol, then plain passes
-    while their change keeps falling (at most extra_plain).  Returns
-    (pol_pops, record) where record holds the passes and the last plain
-    change per pass."""
-    pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=tol, max_iter=max_iter, ng_period=4, local_operator=True)
-    changes = []
-    for _ in range(extra_plain):
-        pp2, _, _, r, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=1)
-        changes.append(float(r[0]))
-        pp = pp2
-        if len(changes) >= 3 and changes[-1] >= 0.9 * min(changes[:-1]):
-            break
-    return pp, {"accelerated_passes": int(n), "accelerated_last_change": float(res[-1]),
-                "plain_passes": len(changes), "plain_change_last": changes[-1] if changes else None,
-                "plain_change_min": min(changes) if changes else None}
+def reference_solution(ctx, rc, *, passes: int = 160):
+    """The fixed point the methods are measured against: the accelerated
+    iteration (local operator + Ng every 4 passes) run for a fixed number of
+    passes, far past the point where its change per pass stops falling (its
+    floor, ~1e-7, is set by the FP32 radiation field).  Returns (pol_pops,
+    record) with the passes and the last changes per pass."""
+    pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=passes, ng_period=4, local_operator=True)
+    return pp, {"passes": int(n), "last_changes": [float(v) for v in res[-4:]],
+                "min_change": float(np.min(res))}
 
 
-def time_to_error(ctx, set_cloud, rc, ref, live, *, target: float = 1e-6, floor: float = 1e-12,
+def time_to_error(ctx, set_cloud, rc, ref, live, *, target: float = 3e-5, floor: float = 1e-12,
                   ng_period: int = 0, local_operator: bool = False, warm=None, max_passes: int = 3000,
                   sync=None):
     """Passes and wall time for one method to reach populations within
@@ -83,11 +79,14 @@ def time_to_error(ctx, set_cloud, rc, ref, live, *, target: float = 1e-6, floor:
     feature pass is counted as one more), seconds of the timed run,
     err_rho00 / err_rho20 of its result, and the errors after each chunk of
     the search ("trace": passes, err_rho00, err_rho20)."""
-    chunk = ng_period if ng_period else 1
+    base = ng_period if ng_period else 1   # whole Ng cycles per call keep a long run's extrapolations
     set_cloud()
     sp = warm.start(ctx, rc) if warm is not None else None
     passes, trace, reached = 0, [], False
+    e0 = e2 = np.inf
     while passes < max_passes:
+        # long chunks far from the target, single cycles near it
+        chunk = base * (8 if max(e0, e2) > 30.0 * target else 1)
         pp, _, n, _, _ = ctx.lambda_iterate(rc, tol=TINY_TOL, max_iter=chunk, start_pops=sp, ng_period=ng_period,
                                             local_operator=local_operator)
         sp = None

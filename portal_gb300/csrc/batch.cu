@@ -35,6 +35,8 @@ struct portal_batch {
     DevBuf<int2> items, sample;
     long long n_items = 0, n_sample = 0;
     size_t se_wb = 0;
+    size_t se_a64_stride = 0;           // largest model's c_dim^2
+    DevBuf<double> se_a64;              // FP64 SE matrices, one per resident warp
     DevBuf<int2> walk;
     DevBuf<unsigned long long> queue;   // [0] next item, [1] segments
 
@@ -81,7 +83,7 @@ int enqueue_pass(portal_batch *b, const int2 *items, long long n_items) {
     for (size_t m = 0; m < b->models.size(); m++)
         if ((rc = se_pass(b->models[m], b->stream)))
             return bfail(b, rc, "model " + std::to_string(m) + ": " + b->models[m]->err);
-    SEBatch sb{b->d_se.p, items, n_items, b->se_wb};
+    SEBatch sb{b->d_se.p, items, n_items, b->se_wb, b->se_a64.p, b->se_a64_stride};
     if ((rc = se_batch_launch(b->stream, b->se_bps * b->sm_count, b->se_warps, sb)))
         return bfail(b, rc, "SE launch failed");
     return PORTAL_OK;
@@ -162,6 +164,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
     b->dust = false;
     b->max_lines = 0;
     size_t wb = 0;
+    b->se_a64_stride = 0;
     std::vector<double> cost(M);
     for (int m = 0; m < M; m++) {
         portal_ctx *c = b->models[m];
@@ -172,6 +175,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
         if ((rc = se_prepare(c, kmax, &b->se[m], &w)))
             return bfail(b, rc, "model " + std::to_string(m) + ": " + c->err);
         wb = std::max(wb, w);
+        b->se_a64_stride = std::max(b->se_a64_stride, se_matrix_doubles(c));
         b->dust = b->dust || c->has_dust;
         b->max_lines = std::max(b->max_lines, c->r_num);
         // per-node cost ~ lines x cells per ray ~ L N^(1/3)
@@ -223,6 +227,17 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
     int dummy = 0;
     if (se_batch_blocks_per_sm(sec.back(), wb, &dummy))  // raises the smem limit to the largest candidate
         return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
+    // FP64 matrix slots for the largest SE grid among the candidates
+    {
+        size_t most = 0;
+        for (int w : sec) {
+            int bps = 0;
+            if (se_batch_blocks_per_sm(w, wb, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
+            most = std::max(most, (size_t)std::max(1, bps) * b->sm_count * w);
+        }
+        se_batch_blocks_per_sm(sec.back(), wb, &dummy);
+        if (b->se_a64.reserve(most * b->se_a64_stride)) return bfail(b, PORTAL_ERR_NOMEM, "SE matrix scratch");
+    }
     // walk scratch for the largest grid
     const size_t warps = (size_t)2 * b->sm_count * 8;
     if (b->walk.reserve(warps * 32 * (size_t)n_depth)) return bfail(b, PORTAL_ERR_NOMEM, "walk scratch");
@@ -248,7 +263,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
             int bps = 0;
             if (se_batch_blocks_per_sm(w, wb, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
             bps = std::max(1, bps);
-            SEBatch sb{b->d_se.p, b->sample.p, b->n_sample, wb};
+            SEBatch sb{b->d_se.p, b->sample.p, b->n_sample, wb, b->se_a64.p, b->se_a64_stride};
             double ms = 0.0;
             int rc = time_launch(b, [&]() { return se_batch_launch(b->stream, bps * b->sm_count, w, sb); }, &ms);
             if (rc) return rc;

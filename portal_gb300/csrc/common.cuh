@@ -104,16 +104,19 @@ struct portal_ctx {
     bool j_valid = false;
     double rf_dxp = 0.0;              // r_max * trace step of the last radiation-field set-up
 
-    // SE program (device) -- built per (molecule, kmax)
+    // SE program (device) -- built per (molecule, kmax, depolarisation mode)
     int se_kmax = -1, c_dim = 0, n_trans = 0;
+    int depol = 0;                    // depolarising collisions (portal_set_depolarization)
+    int n_dep = 0, n_feat = 0;
     portal::DevBuf<int> se_ints;
     portal::DevBuf<double> se_dbls;
     std::vector<int> count_array;
+    portal::DevBuf<double> se_a64;    // FP64 SE matrices, one per resident warp
     portal::DevBuf<double> pops;      // (N, 2*nlev) column-major result
     portal::DevBuf<double> rates;     // (N,3,2*nlev)
     portal::DevBuf<double> jj20;      // (N, r_num)
     int se_ni = 0;
-    size_t se_offs[16] = {};
+    size_t se_offs[20] = {};
 
     // ---- timing ----
     cudaEvent_t ev[2 * portal::T_NSLOT] = {};

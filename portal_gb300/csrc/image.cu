@@ -234,7 +234,12 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
         p0 = __shfl_sync(FULL, p0, 0);
         if (p0 >= npix) break;
         // ---- (1) march, one lane per pixel ----
-        const int p = p0 + lane;
+        // Work index w -> the reference's pixel p = a npx + b (para_finish.f90:
+        // 369-376) with a = w mod npx: consecutive work items step along the
+        // cube's first (fastest) index, so the batch's stores of a channel fill
+        // whole sectors instead of one float every npx^2 (mode 1: w is the node)
+        const int w = p0 + lane;
+        const int p = (a.mode == 1 || w >= npix) ? w : (w % a.npx) * a.npx + w / a.npx;
         int nc = 0, st = 0, fs = 0;  // fs: the ray starts on the star
         if (p < npix) {
             double x, y;
@@ -379,7 +384,8 @@ __global__ void __launch_bounds__(128, 1) k_image(ImArgs a) {
             const int ncr = __shfl_sync(FULL, nc, rr);
             const int str = __shfl_sync(FULL, st, rr);
             const int fsr = __shfl_sync(FULL, fs, rr);
-            const int pix = p0 + rr;
+            const int wr = p0 + rr;
+            const int pix = (a.mode == 1) ? wr : (wr % a.npx) * a.npx + wr / a.npx;
             const int2 *dl = wbase + (size_t)rr * a.n_depth;
             for (int j = 0; j < a.nlines; j++) {
                 const ImLine L = c_im[j];

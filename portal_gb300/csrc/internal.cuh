@@ -39,6 +39,9 @@ struct RFArgs {
 // Everything the SE kernel reads or writes for one model.
 struct SEArgs {
     int N, bulk, c_dim, n_trans, nlev, L, c_temp, c_num, c_par, nent;
+    int n_feat;                         // features per node: NF per transition + depolarisation
+    int n_dep, depol;                   // (level, K >= 2) depolarisation rates, mode (0 off)
+    const double *__restrict__ dep_tab; // (c_temp, n_dep) D^(K) coefficients [cm^3/s] or null
     const double *__restrict__ J0;
     const double *__restrict__ J2;
     const double *__restrict__ JE;      // J0_eff (r_num, N) or null
@@ -69,6 +72,8 @@ struct SEArgs {
     double *rates;                      // (N, 3, 2 nlev) column-major or null
     int *status;
     int *nfail;
+    double *a64;                        // FP64 matrices, one slot of a64_stride doubles per warp
+    size_t a64_stride;
 };
 
 // A batched launch: work items (model, node) over many models, the models'
@@ -86,6 +91,8 @@ struct SEBatch {
     const int2 *items;
     long long n_items;
     size_t warp_bytes;           // dynamic shared memory per warp (largest model)
+    double *a64;                 // FP64 matrices, one slot of a64_stride doubles per warp
+    size_t a64_stride;           // largest model's c_dim^2
 };
 
 // rf.cu
@@ -100,5 +107,6 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *a, size_t *warp_bytes);
 int se_pass(portal_ctx *c, cudaStream_t s);
 int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw);
 int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks);
+size_t se_matrix_doubles(const portal_ctx *c);  // c_dim^2 of the prepared SE program
 
 }  // namespace portal

@@ -87,20 +87,30 @@ int upload_lines(portal_ctx *c) {
     return PORTAL_OK;
 }
 
+// Warps per block of the radiation-field kernel: 8, or PORTAL_RF_WARPS (4..8)
+// -- fewer warps per block let a register-heavy variant keep two blocks on
+// an SM.
+inline int rf_warps() {
+    const char *e = getenv("PORTAL_RF_WARPS");
+    const int v = e ? atoi(e) : 8;
+    return (v >= 4 && v <= 8) ? v : 8;
+}
+
 template <int NS, int NLG, bool DUST, int RT>
 int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     auto kern = k_radiation_field<NS, NLG, DUST, false, RT>;
+    const int wpb = rf_warps();
     int nb = 0;
-    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, 0));
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 32 * wpb, 0));
     if (nb < 1) nb = 1;
     int grid = nb * c->sm_count;
-    size_t nslots = (size_t)grid * 8;
+    size_t nslots = (size_t)grid * wpb;
     if (c->walk.reserve(nslots * 32 * (size_t)n_depth) != cudaSuccess)
         return set_err(c, PORTAL_ERR_NOMEM, "walk scratch allocation failed");
     a.walk = c->walk.p;
     PCHECK(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     timer_start(c, T_RF);
-    kern<<<grid, 256, 0, c->stream>>>(a, RFBatch{});
+    kern<<<grid, 32 * wpb, 0, c->stream>>>(a, RFBatch{});
     timer_stop(c, T_RF);
     PCHECK(c, cudaGetLastError());
     return PORTAL_OK;
@@ -111,12 +121,12 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
 // as a real one, so the width is the one of 5, 4, 3 with the fewest padded
 // lines (the larger on ties: fewer passes over the walk lists); 10 saves
 // profile evaluations but needs more than 128 registers (one block per SM).
-// PORTAL_RF_LINE_GROUP=3|4|5|10 overrides the choice.
+// PORTAL_RF_LINE_GROUP=3|4|5|9|10 overrides the choice.
 inline int line_group(int L) {
     const char *e = getenv("PORTAL_RF_LINE_GROUP");
     if (e) {
         const int v = atoi(e);
-        if (v == 3 || v == 4 || v == 5 || v == 10) return v;
+        if (v == 3 || v == 4 || v == 5 || v == 9 || v == 10) return v;
     }
     int best = 5, slots = 1 << 30;
     for (int g : {5, 4, 3}) {
@@ -134,6 +144,7 @@ int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
     }
     switch (line_group(a.L)) {
     case 3: return launch_rf<NS, 3, false, RT>(c, a, n_depth);
+    case 9: return launch_rf<NS, 9, false, RT>(c, a, n_depth);
     case 4: return launch_rf<NS, 4, false, RT>(c, a, n_depth);
     case 10: return RT ? launch_rf<NS, 5, false, RT>(c, a, n_depth) : launch_rf<NS, 10, false, 0>(c, a, n_depth);
     default: return launch_rf<NS, 5, false, RT>(c, a, n_depth);

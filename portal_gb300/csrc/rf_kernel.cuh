@@ -14,6 +14,9 @@ using namespace portal;
 namespace {
 
 constexpr float LOG2E_F = 1.4426950408889634f;
+// sqrt(log2 e): a profile argument q scaled by it gives exp(-q^2) = 2^(-q'^2),
+// one ex2 of q'^2 with the sign folded into the instruction
+constexpr float SQL2E_F = 1.2011224087864498f;
 // Face crossings closer than this (in units of r_max) are not taken.  The
 // reference uses 1e-10 (miscellaneous.f90:1048) against FP64 noise ~1e-16;
 // the FP32 walk's noise in t is ~1e-9, and a crossing shorter than 2e-8 is
@@ -81,11 +84,10 @@ __global__ void k_line_table(int N, int L, double dxp, const LineConst *__restri
 
 template <int NLG, bool DUST>
 struct CellRec {
-    float q0[32], dq[32];
+    float2 qd[32];       // profile argument at channel 0 and its step per channel, times sqrt(log2 e)
     int cell[32];        // cell id and trace steps (the remainder channel's pass)
     float fst[32];
-    float As[32][NLG];   // A * steps
-    float Ss[32][NLG];   // S (no dust) or E * steps (dust)
+    float2 AS[32][NLG];  // (A * steps, S) without dust, (A * steps, E * steps) with dust
     float Ad[32][DUST ? NLG : 1];   // dust tau per cell (dust only)
     float Jd[32][DUST ? NLG : 1];   // dust emissivity * steps (dust only)
 };
@@ -458,9 +460,8 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 const int2 wc = wl[hi - lane];
                                 const float4 cv = a.cellv[wc.x];
                                 const float vp = cv.x * d4.x + cv.y * d4.y + cv.z * d4.z;
-                                const float ib = 1.f / cv.w;
-                                R.q0[lane] = (d4.w - vp) * ib;
-                                R.dq[lane] = dqfac * ib;
+                                const float ib = SQL2E_F * (1.f / cv.w);
+                                R.qd[lane] = make_float2((d4.w - vp) * ib, dqfac * ib);
                                 const float fst = (float)wc.y;
                                 if (RT) {
                                     R.cell[lane] = wc.x;
@@ -472,8 +473,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                     if (DUST) {
                                         if (l0 + l < a.L) {
                                             const float4 v = lt[l];
-                                            R.As[lane][l] = v.x * fst;
-                                            R.Ss[lane][l] = v.y * v.x * fst;   // emissivity x steps
+                                            R.AS[lane][l] = make_float2(v.x * fst, v.y * v.x * fst);   // emissivity x steps
                                             R.Ad[lane][DUST ? l : 0] = v.z * fst;
                                             R.Jd[lane][DUST ? l : 0] = v.w * fst;
                                         }
@@ -492,8 +492,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                                 Ss = v.y;
                                             }
                                         }
-                                        R.As[lane][l] = As;
-                                        R.Ss[lane][l] = Ss;
+                                        R.AS[lane][l] = make_float2(As, Ss);
                                     }
                                 }
                             }
@@ -502,8 +501,9 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 // the remainder channel, lane = line, the same cells inward
                                 const float chr = (float)(32 * NS - a.nvel);
                                 auto step = [&](const float4 v, int u) {
-                                    const float q = fmaf(R.dq[u], chr, R.q0[u]);
-                                    const float gr = ex2(-q * q * LOG2E_F);
+                                    const float2 qd = R.qd[u];
+                                    const float q = fmaf(qd.y, chr, qd.x);
+                                    const float gr = ex2(-(q * q));
                                     const float As = (v.x > 0.f) ? v.x * R.fst[u] * LOG2E_F : 0.f;
                                     const float Ss = (v.x > 0.f) ? v.y : 0.f;
                                     const float x = As * gr;
@@ -524,28 +524,31 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 for (; u < nc; u++) step(a.ltab[(size_t)R.cell[u] * a.L + lane], u);
                             }
                             for (int u = 0; u < nc; u++) {
-                                const float q0 = R.q0[u], dq = R.dq[u];
+                                const float2 qd = R.qd[u];
+                                const float q0 = qd.x, dq = qd.y;
                                 // Gaussian profile of the cell at the lane's channels,
-                                // slot pairs on the packed pipe (the same roundings as
-                                // ex2(-q q log2 e) per slot)
+                                // exp(-q^2) = 2^(-q'^2) with q' = q sqrt(log2 e) (staged
+                                // scaled); slot pairs on the packed pipe (the same
+                                // roundings per slot as the odd slot's scalar form)
                                 float g[NS];
 #pragma unroll
                                 for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
                                     const float2 ch2 = make_float2((float)(lane + 32 * s2 - a.nvel),
                                                                    (float)(lane + 32 * (s2 + 1) - a.nvel));
                                     const float2 q = __ffma2_rn(make_float2(dq, dq), ch2, make_float2(q0, q0));
-                                    const float2 t = __fmul2_rn(__fmul2_rn(q, q), make_float2(-LOG2E_F, -LOG2E_F));
-                                    g[s2] = ex2(t.x);
-                                    g[s2 + 1] = ex2(t.y);
+                                    const float2 t = __fmul2_rn(q, q);
+                                    g[s2] = ex2(-t.x);
+                                    g[s2 + 1] = ex2(-t.y);
                                 }
                                 if (NS & 1) {
                                     const float q = fmaf(dq, (float)(lane + 32 * (NS - 1) - a.nvel), q0);
-                                    g[NS - 1] = ex2(-q * q * LOG2E_F);
+                                    g[NS - 1] = ex2(-(q * q));
                                 }
 #pragma unroll
                                 for (int l = 0; l < NLG; l++) {
-                                    const float Au = R.As[u][l];
-                                    const float Su = R.Ss[u][l];
+                                    const float2 ASu = R.AS[u][l];
+                                    const float Au = ASu.x;
+                                    const float Su = ASu.y;
                                     if (DUST) {
                                         if (l0 + l < a.L) {
                                             const float Adu = R.Ad[u][DUST ? l : 0], Jdu = R.Jd[u][DUST ? l : 0];

@@ -28,6 +28,16 @@
 // pivoting and refines the solution of A rho = e_1 with FP64 residuals.
 // Should the refinement stall (FP32 LU too inaccurate for the matrix's
 // condition) the node is refactorised in FP64 on the device and flagged.
+//
+// Depolarising collisions (portal_set_depolarization; off by default, as
+// main_sub.f90:96 passes D0 = 0): setup_stateq's col_dep slot
+// (pop_eqs.f90:642-648) holds D^(K)(level) = n_H2 1e-6 times the
+// coefficient de_polarization tabulates (depol.f90:242-317), interpolated in
+// T as make_depolarization_temp does (depol.f90:319-360).  Each (level, K >=
+// 2) rate is one more per-node feature after the transitions' ones; mode 2
+// keeps a second copy that stands for col_dep read where the reference does
+// not assign it (its last assigned value, carried through the loop), which
+// the extra_info rates leave out as the reference's C_mat does.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -36,6 +46,8 @@
 
 namespace portal {
 void coupling_constants(int which, int j, int k, int j2, int k2, double *c0, double *c2);
+double wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3);
+double wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
 }
 using namespace portal;
 
@@ -117,13 +129,17 @@ __device__ void warp_lu_solve(int n, const T *M, const int *piv, V *b, int lane)
 }
 
 // Dynamic shared memory per warp:
-//   A64 [n*n] double | feat [NF*n_trans] double | x, r [n] double | d32 [n] float
-//   LU32 [n*n] float | scale [n] float | piv [n] int
+//   feat [n_feat] double | x, r [n] double | LU32 [n*n] float | d32 [n] float
+//   | scale [n] float | piv [n] int
+// The FP64 matrix A64 [n*n] (assembly, residuals, the FP64 fallback) sits in
+// a per-warp slot of global memory instead (L2-resident: the grid's warps x
+// n^2 doubles); kept out of shared memory it lets 3x more warps share an SM,
+// and the kernel is latency-bound.
 constexpr int NF = 7;  // features per transition
 
-__host__ __device__ inline size_t se_warp_bytes(int n, int n_trans) {
+__host__ __device__ inline size_t se_warp_bytes(int n, int n_feat) {
     size_t b = 0;
-    b += sizeof(double) * ((size_t)n * n + NF * (size_t)n_trans + 2 * (size_t)n);
+    b += sizeof(double) * ((size_t)n_feat + 2 * (size_t)n);
     b += sizeof(float) * ((size_t)n * n + 2 * (size_t)n);
     b += sizeof(int) * (size_t)n;
     return (b + 15) & ~(size_t)15;
@@ -134,13 +150,15 @@ __host__ __device__ inline size_t se_warp_bytes(int n, int n_trans) {
 // shared memory, and the dynamic shared memory per warp fits the largest
 // model.  Otherwise the nodes of the one model a0.
 template <bool BATCH>
-__global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
+__global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ SEArgs margs[BATCH ? 8 : 1];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const long long n_items = BATCH ? bw.n_items : (long long)a0.bulk;
-    const size_t wbytes = BATCH ? bw.warp_bytes : se_warp_bytes(a0.c_dim, a0.n_trans);
+    const size_t wbytes = BATCH ? bw.warp_bytes : se_warp_bytes(a0.c_dim, a0.n_feat);
     unsigned char *base = smem + wbytes * wib;
+    double *const A64 = (BATCH ? bw.a64 : a0.a64) +
+                        (size_t)((long long)blockIdx.x * nw + wib) * (BATCH ? bw.a64_stride : a0.a64_stride);
     int cur_model = -1;
 
     for (long long item = (long long)blockIdx.x * nw + wib; item < n_items; item += (long long)gridDim.x * nw) {
@@ -161,9 +179,8 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
         }
         const SEArgs &a = BATCH ? margs[wib] : a0;
         const int n = a.c_dim;
-        double *A64 = (double *)base;
-        double *feat = A64 + (size_t)n * n;
-        double *x = feat + NF * (size_t)a.n_trans;
+        double *feat = (double *)base;
+        double *x = feat + (size_t)a.n_feat;
         double *r = x + n;   // scratch (the rates)
         float *LU = (float *)(r + n);
         float *d32 = LU + (size_t)n * n;
@@ -208,6 +225,26 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
             f[4] = C21 * exp(-HK * a.tr_nu[t] / T);
             f[5] = B21 * je;
             f[6] = a.tr_A[t] * (1.0 - ls);
+        }
+        if (a.depol) {
+            // make_depolarization_temp: every bracket with col_temps(i) > T
+            // overwrites D0 (the loop has no exit), so the last bracket
+            // decides below the table's top; at or above it the reference
+            // leaves D0 unset (0 here)
+            const int nT = a.c_temp;
+            const double *ct = a.col_temps;
+            for (int d = lane; d < a.n_dep; d += 32) {
+                const double *tab = a.dep_tab + (size_t)nT * d;
+                double v = 0.0;
+                if (T <= ct[0]) v = tab[0];
+                if (nT >= 2 && ct[nT - 1] > T) {
+                    const double ddT = (T - ct[nT - 2]) / (ct[nT - 1] - ct[nT - 2]);
+                    v = tab[nT - 2] + ddT * (tab[nT - 1] - tab[nT - 2]);
+                }
+                v = v * nH2 * 1e-6;
+                feat[NF * (size_t)a.n_trans + d] = v;
+                if (a.depol == 2) feat[NF * (size_t)a.n_trans + a.n_dep + d] = v;
+            }
         }
         for (int i = lane; i < n * n; i += 32) A64[i] = 0.0;
         __syncwarp();
@@ -316,7 +353,14 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
                             const int e = a.row_ent[q];
                             double v = 0.0;
                             for (int t = a.ent_off[e]; t < a.ent_off[e + 1]; t++) {
-                                const int tf = a.term_f[t], f = tf % NF, base = tf - f;
+                                const int tf = a.term_f[t];
+                                if (tf >= NF * a.n_trans) {
+                                    // depolarisation: C_mat where col_dep is assigned; the
+                                    // carried copies (mode 2) are in Amat only
+                                    if (k == 2 && tf < NF * a.n_trans + a.n_dep) v += a.term_c[t] * feat[tf];
+                                    continue;
+                                }
+                                const int f = tf % NF, base = tf - f;
                                 const int kind = (f == 2 || f == 6) ? 0 : (f == 3 || f == 4) ? 2 : 1;
                                 if (kind != k) continue;
                                 const int fu = (f == 5) ? 0 : (f == 6) ? 2 : f;
@@ -357,12 +401,39 @@ __global__ void __launch_bounds__(256, 1) k_solve_se(SEArgs a0, SEBatch bw) {
 // ---- host: the program ---------------------------------------------------
 
 struct Program {
-    int c_dim = 0, n_trans = 0;
+    int c_dim = 0, n_trans = 0, n_dep = 0;
     std::vector<int> count_array, tr_lo, tr_up, tr_rad, tr_col;
     std::vector<double> tr_nu, tr_A, tr_B21;
     std::vector<int> ent_off, ent_pos, term_f, pack, row_off, row_ent;
     std::vector<double> term_c;
+    std::vector<double> dep_tab;   // (c_temp, n_dep) depolarisation coefficients
 };
+
+// de_polarization depol.f90:242-317 (Morris 1985 Eq. B11, the D^(K) of
+// L&L04 Eq. 7.102) for level i (J = i - 1, the reference's assumption) and
+// rank K at collision temperature l:
+//   (2J+1)^2 sum_{m=1..2J} (-1)^m (2m+1) (J J m; 0 0 0)^2
+//            ({J J m; J J 0} - {J J m; J J K}) C_j0(l, m)
+// with C_j0(:, m) the first partner's rate of the collisional transition
+// from level 1 to level m, 0 for m = 1 (the reference never sets it) and
+// for m beyond the levels (the reference reads past its array there).
+double depol_coefficient(const portal_ctx *c, int i, int K, int l) {
+    const int j = i - 1, nT = c->c_temp;
+    const double lj2 = std::pow(2.0 * j + 1.0, 2.0);
+    double s = 0.0;
+    for (int m = 1; m <= 2 * j; m++) {
+        double cj = 0.0;
+        if (m <= c->nlev)
+            for (int q = 0; q < c->c_num; q++)
+                if (c->c_trans[2 * q] == 1 && c->c_trans[2 * q + 1] == m) cj = c->Cji[l + (size_t)nT * q];
+        const double fac = std::pow(-1.0, m) * (2.0 * m + 1.0);
+        const double w1 = wigner3j(2 * j, 2 * j, 2 * m, 0, 0, 0);
+        const double w2 = wigner6j(2 * j, 2 * j, 2 * m, 2 * j, 2 * j, 0);
+        const double w3 = wigner6j(2 * j, 2 * j, 2 * m, 2 * j, 2 * j, 2 * K);
+        s = s + lj2 * fac * w1 * w1 * (w2 - w3) * cj;
+    }
+    return s;
+}
 
 void build_program(const portal_ctx *c, int kmax, Program &P) {
     const int nlev = c->nlev;
@@ -418,6 +489,22 @@ void build_program(const portal_ctx *c, int kmax, Program &P) {
     for (int i = 0; i < nlev; i++)
         for (int k = 0; k <= std::min(2 * J[i], kmax); k += 2) k_of[P.count_array[i] + k / 2] = k;
     std::map<int, std::vector<std::pair<int, double>>> ent;  // pos -> terms
+    // depolarisation rates: one per (level, K = 2 .. min(2J, kmax))
+    std::vector<int> dep_id(nlev, -1);
+    P.n_dep = 0;
+    if (c->depol) {
+        for (int i = 0; i < nlev; i++) {
+            dep_id[i] = P.n_dep;
+            P.n_dep += std::min(2 * J[i], kmax) / 2;
+        }
+        P.dep_tab.assign((size_t)c->c_temp * P.n_dep, 0.0);
+        for (int i = 0; i < nlev; i++)
+            for (int K = 2; K <= std::min(2 * J[i], kmax); K += 2)
+                for (int l = 0; l < c->c_temp; l++)
+                    P.dep_tab[(size_t)l + (size_t)c->c_temp * (dep_id[i] + K / 2 - 1)] =
+                        depol_coefficient(c, i + 1, K, l);
+    }
+    int cur_dep = -1;  // the (level, K) col_dep holds (the reference's loop order)
     auto add = [&](int c1, int c2, int t, int f, double coef) {
         auto &v = ent[c1 + n * c2];
         // couplings between K = 0 components take the split field (f5, f6)
@@ -474,6 +561,17 @@ void build_program(const portal_ctx *c, int kmax, Program &P) {
             int c2 = P.count_array[i1];
             for (int k2 = 0; k2 <= k1m; k2 += 2, c2++) {
                 touch(c1, c2);
+                // col_dep (pop_eqs.f90:642-648), read after the rates below in
+                // the reference; a term's position in the entry's sum does not
+                // change the FP64 assembly beyond rounding
+                if (c->depol) {
+                    if (k1 == k2 && k1 >= 2) {
+                        cur_dep = dep_id[i1] + k1 / 2 - 1;
+                        ent[c1 + n * c2].push_back({NF * P.n_trans + cur_dep, -1.0});
+                    } else if (c->depol == 2 && cur_dep >= 0) {
+                        ent[c1 + n * c2].push_back({NF * P.n_trans + P.n_dep + cur_dep, -1.0});
+                    }
+                }
                 for (int q : up) {
                     int j3 = J[P.tr_up[q]];
                     double g3 = 2.0 * j3 + 1.0;
@@ -530,6 +628,11 @@ namespace portal {
 
 int prepare_se(portal_ctx *c, int kmax) {
     if (c->se_kmax == kmax) return PORTAL_OK;
+    if (c->depol)
+        for (int i = 0; i < c->nlev; i++)
+            if (c->j_lev[i] != i)
+                return set_err(c, PORTAL_ERR_ARG, "depolarising collisions need j_lev(i) = i - 1 "
+                                                  "(de_polarization's assumption, depol.f90:283)");
     Program P;
     build_program(c, kmax, P);
     // pack ints: tr_rad | tr_col | ent_off | ent_pos | term_f | norm_col | pack | col? ;
@@ -543,7 +646,7 @@ int prepare_se(portal_ctx *c, int kmax) {
            o_epos = putI(P.ent_pos), o_tf = putI(P.term_f), o_nc = putI(P.count_array),
            o_pack = putI(P.pack), o_roff = putI(P.row_off), o_rent = putI(P.row_ent);
     size_t o_nu = putD(P.tr_nu), o_A = putD(P.tr_A), o_B = putD(P.tr_B21), o_tc = putD(P.term_c),
-           o_nv = putD(norm_val), o_ct = putD(c->col_temps), o_C = putD(c->Cji);
+           o_nv = putD(norm_val), o_ct = putD(c->col_temps), o_C = putD(c->Cji), o_dep = putD(P.dep_tab);
     if (c->se_ints.reserve(I.size()) || c->se_dbls.reserve(D.size()))
         return set_err(c, PORTAL_ERR_NOMEM, "SE program");
     PCHECK(c, cudaMemcpyAsync(c->se_ints.p, I.data(), I.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -559,7 +662,9 @@ int prepare_se(portal_ctx *c, int kmax) {
     c->se_offs[4] = o_tf; c->se_offs[5] = o_nc; c->se_offs[6] = o_pack;
     c->se_offs[7] = o_nu; c->se_offs[8] = o_A; c->se_offs[9] = o_B; c->se_offs[10] = o_tc;
     c->se_offs[11] = o_nv; c->se_offs[12] = o_ct; c->se_offs[13] = o_C;
-    c->se_offs[14] = o_roff; c->se_offs[15] = o_rent;
+    c->se_offs[14] = o_roff; c->se_offs[15] = o_rent; c->se_offs[16] = o_dep;
+    c->n_dep = P.n_dep;
+    c->n_feat = NF * P.n_trans + (c->depol == 2 ? 2 : 1) * P.n_dep;
     return PORTAL_OK;
 }
 
@@ -572,13 +677,14 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     int rc = prepare_se(c, kmax);
     if (rc) return rc;
     const int n = c->c_dim;
-    const size_t wb = se_warp_bytes(n, c->n_trans);
+    const size_t wb = se_warp_bytes(n, c->n_feat);
     if (wb > 200 * 1024) return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
     if (c->pops.reserve((size_t)c->N * 2 * c->nlev) || c->jj20.reserve((size_t)c->N * c->r_num))
         return set_err(c, PORTAL_ERR_NOMEM, "SE outputs");
     SEArgs a;
     a.N = c->N; a.bulk = c->bulk; a.c_dim = n; a.n_trans = c->n_trans; a.nlev = c->nlev; a.L = c->r_num;
     a.c_temp = c->c_temp; a.c_num = c->c_num; a.c_par = c->c_par; a.nent = c->se_ni;
+    a.n_feat = c->n_feat; a.n_dep = c->n_dep; a.depol = c->depol;
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.h2 = c->h2.p; a.tkin = c->tkin.p; a.ab = c->active_ab();
     a.JE = c->ali_valid ? c->JE.p : nullptr;
     a.LS = c->ali_valid ? c->LS.p : nullptr;
@@ -591,6 +697,7 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     a.term_c = D + c->se_offs[10]; a.norm_val = D + c->se_offs[11]; a.col_temps = D + c->se_offs[12];
     a.Cji = D + c->se_offs[13];
     a.row_off = I + c->se_offs[14]; a.row_ent = I + c->se_offs[15];
+    a.dep_tab = c->n_dep ? D + c->se_offs[16] : nullptr;
     a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
     a.rates = nullptr;
     a.nfail = (int *)(c->counters.p + 2);
@@ -607,6 +714,8 @@ int se_pass(portal_ctx *c, cudaStream_t s) {
     PCHECK(c, cudaMemsetAsync(c->counters.p + 2, 0, sizeof(unsigned long long), s));
     return PORTAL_OK;
 }
+
+size_t se_matrix_doubles(const portal_ctx *c) { return (size_t)c->c_dim * c->c_dim; }
 
 int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) {
     const size_t smem = warp_bytes * warps_per_block;
@@ -646,6 +755,10 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates) {
     int nb = 0;
     PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_solve_se<false>, 32 * wpb, smem));
     int grid = c->sm_count * std::max(1, nb);
+    a.a64_stride = (size_t)c->c_dim * c->c_dim;
+    if (c->se_a64.reserve((size_t)grid * wpb * a.a64_stride))
+        return set_err(c, PORTAL_ERR_NOMEM, "SE matrix scratch");
+    a.a64 = c->se_a64.p;
     timer_start(c, T_SE);
     k_solve_se<false><<<grid, 32 * wpb, smem, c->stream>>>(a, SEBatch{});
     timer_stop(c, T_SE);
@@ -694,5 +807,15 @@ extern "C" int portal_solve_se(portal_ctx *c, int kmax, const double *J0, const 
                                   cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
     if (nsing) return set_err(c, PORTAL_ERR_SINGULAR, std::to_string(nsing) + " singular SE systems");
+    return PORTAL_OK;
+}
+
+extern "C" int portal_set_depolarization(portal_ctx *c, int mode) {
+    if (!c) return PORTAL_ERR_ARG;
+    if (mode < 0 || mode > 2) return set_err(c, PORTAL_ERR_ARG, "portal_set_depolarization: mode 0, 1 or 2");
+    if (mode != c->depol) {
+        c->depol = mode;
+        c->se_kmax = -1;  // rebuild the SE program
+    }
     return PORTAL_OK;
 }

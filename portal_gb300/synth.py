@@ -402,26 +402,33 @@ def turbulent_cube(n_points: int, seed: int, mol: Molecule, *, grid: int = 64, s
                   keep_raw=keep_raw)
 
 
+def batch_cloud(i: int, points_scale: float = 1.0, n_min: int = 10000, n_max: int = 300000):
+    """Cloud i of the batched uneven configuration: seed 100 + i, a point
+    count log-uniform in [n_min, n_max] (times points_scale), a linear rotor
+    of 5..20 levels, density exponent uniform in 1..2, n0 log-uniform in
+    1e4..1e7 cm^-3 and an isotropically drawn field direction; T = 20 K.
+    Returns (cloud, molecule)."""
+    rng = np.random.default_rng(100 + i)
+    n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max))) * points_scale))
+    nlev = int(rng.integers(5, 21))
+    p = float(rng.uniform(1.0, 2.0))
+    n0 = float(10.0 ** rng.uniform(4.0, 7.0))
+    b = rng.normal(size=3)
+    b /= np.linalg.norm(b)
+    mol = linear_rotor(nlev)
+    cloud = power_law_sphere(max(n, 64), 100 + i, mol, density_exp=p, n0_cm3=n0, b_dir=tuple(b))
+    return cloud, mol
+
+
+BATCH_RUN_CONFIG = dict(nth=16, nph=16, nvel=32, kmax=2)
+
+
 def batch_clouds(n_clouds: int = 64, points_scale: float = 1.0, n_min: int = 10000, n_max: int = 300000):
-    """The batched uneven configuration: cloud i from seed 100 + i with a
-    point count log-uniform in [n_min, n_max] (times points_scale), a linear
-    rotor of 5..20 levels, density exponent uniform in 1..2, n0 log-uniform
-    in 1e4..1e7 cm^-3 and an isotropically drawn field direction; T = 20 K.
+    """The batched uneven configuration: clouds batch_cloud(0..n_clouds-1).
     Returns [(cloud, molecule)] and the run configuration shared by all
     (16x16 directions, 65 channels, kmax 2)."""
-    out = []
-    for i in range(n_clouds):
-        rng = np.random.default_rng(100 + i)
-        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max))) * points_scale))
-        nlev = int(rng.integers(5, 21))
-        p = float(rng.uniform(1.0, 2.0))
-        n0 = float(10.0 ** rng.uniform(4.0, 7.0))
-        b = rng.normal(size=3)
-        b /= np.linalg.norm(b)
-        mol = linear_rotor(nlev)
-        cloud = power_law_sphere(max(n, 64), 100 + i, mol, density_exp=p, n0_cm3=n0, b_dir=tuple(b))
-        out.append((cloud, mol))
-    rc = RunConfig(nth=16, nph=16, nvel=32, kmax=2, gvec=gauge_vector(3))
+    out = [batch_cloud(i, points_scale, n_min, n_max) for i in range(n_clouds)]
+    rc = RunConfig(gvec=gauge_vector(3), **BATCH_RUN_CONFIG)
     return out, rc
 
 
@@ -437,7 +444,7 @@ def gauge_vector(seed: int) -> tuple:
 # the benchmark configurations
 # --------------------------------------------------------------------------
 
-def config_cloud(name: str, n_points: int | None = None):
+def config_cloud(name: str, n_points: int | None = None, keep_raw: bool = False):
     """(cloud, molecule, run config) for a named configuration.
 
     "sphere4k": 4,096 points, seed 0, 5-level rotor, T = 20 K, B along z,
@@ -447,21 +454,23 @@ def config_cloud(name: str, n_points: int | None = None):
             129 channels (nvel = 64);
     "cube1m": 1,048,576 points of the turbulent cube (seed 4), 20-level
             rotor, 32x32 directions, 129 channels, kmax 2.
-    n_points overrides the point count (smaller parity cases)."""
+    n_points overrides the point count (smaller parity cases); keep_raw
+    keeps the tetrahedra and the LIME columns (file writers, neighbour-list
+    checks)."""
     if name == "sphere4k":
         mol = linear_rotor(5)
         n = n_points or 4096
-        cloud = power_law_sphere(n, 0, mol, t_law="uniform", t_uniform=20.0)
+        cloud = power_law_sphere(n, 0, mol, t_law="uniform", t_uniform=20.0, keep_raw=keep_raw)
         rc = RunConfig(nth=16, nph=16, nvel=32, kmax=6, gvec=gauge_vector(0))
     elif name == "sphere262k":
         mol = linear_rotor(10)
         n = n_points or 262144
-        cloud = power_law_sphere(n, 1, mol, t_law="loglinear", b_random=0.3)
+        cloud = power_law_sphere(n, 1, mol, t_law="loglinear", b_random=0.3, keep_raw=keep_raw)
         rc = RunConfig(nth=24, nph=24, nvel=64, kmax=6, gvec=gauge_vector(1))
     elif name == "cube1m":
         mol = linear_rotor(20)
         n = n_points or 1048576
-        cloud = turbulent_cube(n, 4, mol, grid=128 if n > 200000 else 64)
+        cloud = turbulent_cube(n, 4, mol, grid=128 if n > 200000 else 64, keep_raw=keep_raw)
         rc = RunConfig(nth=32, nph=32, nvel=64, kmax=2, gvec=gauge_vector(4))
     else:
         raise ValueError(f"unknown configuration {name!r}")

@@ -145,6 +145,37 @@ def test_two_collision_partners(ctx):
     assert np.abs(opp1[:bulk, 0::2] - opp[:bulk, 0::2]).max() > 1e-3 * np.abs(opp[:bulk, 0::2]).max()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_depolarising_collisions_against_oracle(ctx, mode):
+    """Depolarising collisions (depol.f90:242-360 into setup_stateq's
+    col_dep, pop_eqs.f90:642-648), which the reference leaves off
+    (main_sub.f90:96): the populations and alignment of the same J as the
+    oracle's with the same mode, 1e-10; the extra_info rates likewise; and
+    the switch back to mode 0 restores the plain SE."""
+    import oracle
+    cloud, mol, rc = _small(1024, nlev=6, t_law="loglinear")
+    P = oracle.OracleProblem(cloud, mol, depol=mode)
+    oJ0, oJ2, _, _, _ = P.radiation_field(rc, 1, 128)
+    opp, ost, _, ort = P.solve_se(rc.kmax, oJ0, oJ2, 1, 128, rates=True)
+    plain = oracle.OracleProblem(cloud, mol).solve_se(rc.kmax, oJ0, oJ2, 1, 128)[0]
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    try:
+        ctx.set_depolarization(mode)
+        pops, st, rt = ctx.solve_se(rc.kmax, oJ0, oJ2, rates=True)
+    finally:
+        ctx.set_depolarization(0)
+    scale = np.abs(opp[:128, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pops[:128, 0::2] - opp[:128, 0::2]) / scale).max() < 1e-10
+    assert (np.abs(pops[:128, 1::2] - opp[:128, 1::2]) / scale).max() < 1e-10
+    rscale = np.abs(ort[:128]).max(axis=2, keepdims=True) + 1e-300
+    assert (np.abs(rt[:128] - ort[:128]) / rscale).max() < 1e-10
+    # the depolarisation is there: the alignment moved
+    assert np.abs(opp[:128, 1::2] - plain[:128, 1::2]).max() > 1e-3 * np.abs(plain[:128, 1::2]).max()
+    back, _ = ctx.solve_se(rc.kmax, oJ0, oJ2)
+    np.testing.assert_allclose(back[:128], plain[:128], rtol=1e-10, atol=1e-14 * np.abs(plain).max())
+
+
 def test_n_depth_overflow_is_reported(ctx):
     import portal_gb300 as pg
     cloud, mol, rc = _small()

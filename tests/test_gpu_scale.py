@@ -77,7 +77,27 @@ def _se_checks(name, ctx, P, cloud, mol, kmax, J0, J2, oJ0, oJ2, nodes, pops_gpu
 @pytest.fixture(scope="module")
 def sphere262k():
     from portal_gb300 import synth
-    return synth.config_cloud("sphere262k")
+    return synth.config_cloud("sphere262k", keep_raw=True)
+
+
+def _check_device_neighbours(name, ctx, cloud):
+    """portal_adj_list (adj_list_no_delaunay + SortUnique on the device)
+    against the host construction of the same lists, bit for bit, with both
+    times reported."""
+    import time
+    from portal_gb300 import synth
+    t0 = time.perf_counter()
+    off, idx = synth.neighbours_from_tets(cloud.tets, cloud.node_num)
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dne, num, ms = ctx.adj_list(cloud.node_num, cloud.tets)
+    t_call = time.perf_counter() - t0
+    np.testing.assert_array_equal(num, np.diff(off))
+    np.testing.assert_array_equal(dne, cloud.del_ne())
+    np.testing.assert_array_equal(off, cloud.nb_off)
+    np.testing.assert_array_equal(idx, cloud.nb_idx)
+    _report(name + " neighbours", tets=cloud.tets.shape[0], device_ms=ms, call_s=t_call, host_numpy_s=t_host,
+            max_ne=dne.shape[0])
 
 
 def test_sphere262k_full_cloud_stratified_sample(built_lib, sphere262k):
@@ -110,6 +130,7 @@ def test_sphere262k_full_cloud_stratified_sample(built_lib, sphere262k):
         core = nodes[r < 0.02]
         _check_J(J0[core], J2[core], oJ0[core], oJ2[core])
         _se_checks("sphere262k", ctx, P, cloud, mol, rc.kmax, J0, J2, oJ0, oJ2, nodes, pops)
+        _check_device_neighbours("sphere262k", ctx, cloud)
 
 
 def test_sphere4k_full_image_cube(built_lib, sphere4k, sphere4k_oracle):
@@ -182,7 +203,7 @@ def test_cube1m_full_cloud_sample(built_lib):
     import oracle
     import portal_gb300 as pg
     from portal_gb300 import synth
-    cloud, mol, rc = synth.config_cloud("cube1m")
+    cloud, mol, rc = synth.config_cloud("cube1m", keep_raw=True)
     assert cloud.node_num == 1048576 and mol.nlev == 20
     nodes = density_sample(cloud)
     with pg.Context(0) as ctx:
@@ -202,3 +223,4 @@ def test_cube1m_full_cloud_sample(built_lib):
         _check_J(J0[nodes], J2[nodes], oJ0[nodes], oJ2[nodes])
         assert dseg.sum() <= 1e-4 * oseg.sum()
         _se_checks("cube1m", ctx, P, cloud, mol, rc.kmax, J0, J2, oJ0, oJ2, nodes, pops, significant=1e-8)
+        _check_device_neighbours("cube1m", ctx, cloud)

@@ -742,3 +742,73 @@ def test_se_two_level_alignment_limit(anis):
     assert w == pytest.approx(1.0, rel=1e-14)
     sig = pp[:cloud.bulk_node_num, 3] / pp[:cloud.bulk_node_num, 2]
     np.testing.assert_allclose(sig, w * anis, rtol=1e-5)
+
+
+# ---- depolarising collisions (depol.f90:242-360) ---------------------------
+
+def _depol_restated(mol, kmax):
+    """de_polarization restated with sympy's exact Wigner symbols: D0_all
+    [K/2 - 1, level, temperature], the rate out of level 1 to level m read
+    where the reference reads it (C_j0(:, m), m = 1..2J; 0 for m = 1 and for
+    m beyond the levels)."""
+    wig = pytest.importorskip("sympy.physics.wigner")
+    nlev, nT = mol.nlev, mol.c_temp
+    Cj0 = np.zeros((nT, nlev + 1))
+    for q in range(mol.c_num):
+        lo, up = mol.c_trans[q]
+        if lo == 1:
+            Cj0[:, up] = mol.C[0, q]
+    out = np.zeros((kmax // 2, nlev, nT))
+    for i in range(2, nlev + 1):
+        j = i - 1
+        for k in range(2, min(2 * j, kmax) + 1, 2):
+            for m in range(1, 2 * j + 1):
+                w1 = float(wig.wigner_3j(j, j, m, 0, 0, 0))
+                w2 = float(wig.wigner_6j(j, j, m, j, j, 0))
+                w3 = float(wig.wigner_6j(j, j, m, j, j, k))
+                cj = Cj0[:, m] if m <= nlev else 0.0
+                out[k // 2 - 1, i - 1] += (2 * j + 1) ** 2 * (-1) ** m * (2 * m + 1) * w1 * w1 * (w2 - w3) * cj
+    return out
+
+
+def test_depolarization_coefficients_against_sympy():
+    mol = synth.linear_rotor(7)
+    got = oracle.de_polarization(mol, 6)
+    want = _depol_restated(mol, 6)
+    assert np.abs(want).max() > 1e-12
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-30)
+    # J = 0 has no K >= 2 component; K above 2J gives nothing
+    assert not got[:, 0].any() and not got[1:, 1].any()
+    # the reference's own assumption, j_lev(i) = i - 1
+    import dataclasses
+    shifted = dataclasses.replace(mol, j_lev=mol.j_lev + 1)
+    assert oracle.de_polarization(shifted, 6) is None
+
+
+def test_depolarization_enters_the_se_only_when_switched_on():
+    """mode 0 is the reference's run (D0 = 0); modes 1 and 2 change the
+    alignment, mode 2 (col_dep carried to the later entries, as the
+    reference's code reads it) the populations as well; the temperature
+    interpolation is make_depolarization_temp's last bracket."""
+    cloud, mol, rc = synth.config_cloud("sphere4k", n_points=1024)
+    rc.nth = rc.nph = 8
+    P0 = oracle.OracleProblem(cloud, mol)
+    J0, J2, _, _, _ = P0.radiation_field(rc, 1, 32)
+    p0 = P0.solve_se(rc.kmax, J0, J2, 1, 32)[0][:32]
+    p1 = oracle.OracleProblem(cloud, mol, depol=1).solve_se(rc.kmax, J0, J2, 1, 32)[0][:32]
+    p2 = oracle.OracleProblem(cloud, mol, depol=2).solve_se(rc.kmax, J0, J2, 1, 32)[0][:32]
+    d1 = np.abs(p1[:, 1::2] - p0[:, 1::2]).max() / np.abs(p0[:, 1::2]).max()
+    assert d1 > 1e-3                                   # the alignment is depolarised
+    assert np.all(np.abs(p1[:, 1::2]) <= np.abs(p0[:, 1::2]) * (1 + 1e-9) + 1e-300)
+    assert np.abs(p2 - p1).max() > 1e-6 * np.abs(p1).max()
+    # make_depolarization_temp at T: the last bracket, times n_H2 1e-6
+    D = oracle.de_polarization(mol, rc.kmax)
+    T, nH2 = 20.0, 3e10
+    tt = mol.col_temps
+    f = (T - tt[-2]) / (tt[-1] - tt[-2])
+    want = (D[..., -2] + f * (D[..., -1] - D[..., -2])) * nH2 * 1e-6
+    got = np.zeros(D.shape[:2])          # D0(nlev, kmax/2) column-major == (kmax/2, nlev)
+    oracle.lib().orc_make_depolarization_temp(oracle._p(np.ascontiguousarray(D)), mol.nlev, mol.c_temp, rc.kmax,
+                                              oracle._p(np.ascontiguousarray(tt)), C.c_double(T), C.c_double(nH2),
+                                              oracle._p(got))
+    np.testing.assert_allclose(got, want, rtol=1e-14)
