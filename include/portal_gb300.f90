@@ -113,5 +113,10 @@ module portal_gpu
       integer(c_int) :: del_tri(4,*), del_num_ne(*), max_ne
       type(c_ptr), value :: del_ne, ms
     end function
+    integer(c_int) function portal_field_moments(ctx, moments) bind(C, name="portal_field_moments")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      real(c_double) :: moments(6,*)
+    end function
   end interface
 end module

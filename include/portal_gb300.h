@@ -415,12 +415,23 @@ int portal_mlp_predict(portal_mlp *mlp, const float *X, int B, float *Y);
  *   0 log10 n_H2 [cm^-3], 1 log10 T_kin [K],
  *   2 log10 |grad v| [s^-1] (Frobenius norm of the least-squares velocity
  *     gradient over the node's neighbours),
- *   3 cos^2 of the angle between the field and the principal axis of the
- *     symmetric velocity gradient,
+ *   3 cos^2 of the angle between the field and the local J^2_0 axis of
+ *     line 1 (the principal axis of the traceless part of the second
+ *     moment portal_field_moments returns),
  *   4, 5 log10 J^0_0 / B_nu(T_kin) of lines 1 and 2,
  *   6, 7 100 J^2_0 / J^0_0 of lines 1 and 2
  * (line 1 again for a one-line molecule). */
 int portal_warmstart_features(portal_ctx *ctx, float *features);
+
+/* The second moment of line 1's radiation field at every node from the last
+ * portal_radiation_field call: moments(6, N) = sum over the node's rays of
+ * w Ibar n n (components xx, yy, zz, xy, xz, yz in the cloud's frame; n the
+ * ray direction, w its quadrature weight, Ibar its profile-averaged
+ * intensity, as J^0_0 = sum w Ibar).  Its traceless part holds J^2_Q in any
+ * frame: along a unit vector b, J^2_0 = (3 b.M.b - trace M) / (2 sqrt 2).
+ * No reference counterpart (the reference forms J^2_0 in the field frame
+ * only, inverse_rt.f90:128-129); 0 for skipped nodes. */
+int portal_field_moments(portal_ctx *ctx, double *moments);
 
 /* ---- utilities -------------------------------------------------------- */
 

@@ -40,7 +40,7 @@ EXPORTS = (
     "portal_mlp_predict", "portal_warmstart_features", "portal_get_results",
     "portal_batch_create", "portal_batch_destroy", "portal_batch_last_error", "portal_batch_add",
     "portal_batch_prepare", "portal_batch_run", "portal_batch_config", "portal_node_segments",
-    "portal_set_depolarization", "portal_adj_list",
+    "portal_set_depolarization", "portal_adj_list", "portal_field_moments",
 )
 
 _lib = None
@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
     L.portal_get_results.argtypes = [C.c_void_p, P_D, P_D, P_D, P_I]
     L.portal_node_segments.argtypes = [C.c_void_p, P_I]
     L.portal_set_depolarization.argtypes = [C.c_void_p, C.c_int]
+    L.portal_field_moments.argtypes = [C.c_void_p, P_D]
     L.portal_adj_list.argtypes = [C.c_void_p, C.c_int, C.c_longlong, P_I, C.c_int, P_I, P_I, P_I, P_D]
     L.portal_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
     L.portal_batch_destroy.argtypes = [C.c_void_p]
@@ -373,6 +374,13 @@ class Context:
         self._check(lib().portal_adj_list(self._h, int(node_num), int(t.shape[0]), _p(t, P_I), cap, _p(dne, P_I),
                                           _p(num, P_I), C.byref(mx), C.byref(ms)))
         return dne[:mx.value].copy(), num, float(ms.value)
+
+    def field_moments(self) -> np.ndarray:
+        """Second moment of line 1's field per node (N, 6): xx yy zz xy xz yz
+        of sum w Ibar n n from the last radiation_field call."""
+        m = np.zeros((self.N, 6))
+        self._check(lib().portal_field_moments(self._h, _p(m)))
+        return m
 
     def node_segments(self) -> np.ndarray:
         """Ray segments of every node in the last radiation-field pass (N,)."""

@@ -97,6 +97,7 @@ struct portal_ctx {
     bool ali_valid = false;           // JE / LS belong to the current J0 (the SE splits the field)
     portal::DevBuf<int> status;       // N
     portal::DevBuf<int> nodeseg;      // N: ray segments of each node in the last radiation field
+    portal::DevBuf<float> kmom;       // (6, N): second moment of line 1's field per node
     portal::DevBuf<int2> walk;        // per-warp walk scratch
     portal::DevBuf<unsigned long long> counters;  // [0] work, [1] segments, [2..] misc
     portal::DevBuf<double> dirtab;    // direction table

@@ -32,6 +32,7 @@ struct RFArgs {
     double *JE, *LS;                  // split field (accelerated Lambda iteration) or null
     int *status;
     int *segs;                        // (N) ray segments of each node (sum of node_count) or null
+    float *kmom;                      // (6, N) second moment sum w I n n of line 1 (xx yy zz xy xz yz) or null
     int2 *walk;
     unsigned long long *counters;
 };

@@ -121,12 +121,12 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
 // as a real one, so the width is the one of 5, 4, 3 with the fewest padded
 // lines (the larger on ties: fewer passes over the walk lists); 10 saves
 // profile evaluations but needs more than 128 registers (one block per SM).
-// PORTAL_RF_LINE_GROUP=3|4|5|9|10 overrides the choice.
+// PORTAL_RF_LINE_GROUP=3|4|5|10 overrides the choice.
 inline int line_group(int L) {
     const char *e = getenv("PORTAL_RF_LINE_GROUP");
     if (e) {
         const int v = atoi(e);
-        if (v == 3 || v == 4 || v == 5 || v == 9 || v == 10) return v;
+        if (v == 3 || v == 4 || v == 5 || v == 10) return v;
     }
     int best = 5, slots = 1 << 30;
     for (int g : {5, 4, 3}) {
@@ -144,7 +144,6 @@ int dispatch_nlg(portal_ctx *c, RFArgs &a, int n_depth) {
     }
     switch (line_group(a.L)) {
     case 3: return launch_rf<NS, 3, false, RT>(c, a, n_depth);
-    case 9: return launch_rf<NS, 9, false, RT>(c, a, n_depth);
     case 4: return launch_rf<NS, 4, false, RT>(c, a, n_depth);
     case 10: return RT ? launch_rf<NS, 5, false, RT>(c, a, n_depth) : launch_rf<NS, 10, false, 0>(c, a, n_depth);
     default: return launch_rf<NS, 5, false, RT>(c, a, n_depth);
@@ -259,7 +258,7 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
     }
     if (c->dirtab.reserve(dt.size()) || c->chtab.reserve(ct.size()) ||
         c->ltab.reserve((size_t)L * N) || c->J0.reserve((size_t)L * N) || c->J2.reserve((size_t)L * N) ||
-        c->nodeseg.reserve((size_t)N))
+        c->nodeseg.reserve((size_t)N) || c->kmom.reserve((size_t)6 * N))
         return set_err(c, PORTAL_ERR_NOMEM, "radiation-field buffers");
     if (split && (c->JE.reserve((size_t)L * N) || c->LS.reserve((size_t)L * N)))
         return set_err(c, PORTAL_ERR_NOMEM, "split-field buffers");
@@ -283,6 +282,7 @@ int rf_prepare(portal_ctx *c, int nth, int nph, int nvel, const double *gvec, do
     a.bbs = c->bbstar.p;
     a.J0 = c->J0.p; a.J2 = c->J2.p; a.status = c->status.p; a.counters = c->counters.p;
     a.segs = c->nodeseg.p;
+    a.kmom = c->kmom.p;
     a.JE = split ? c->JE.p : nullptr;
     a.LS = split ? c->LS.p : nullptr;
     a.walk = nullptr;
@@ -300,6 +300,7 @@ int rf_pass(portal_ctx *c, const RFArgs &a, cudaStream_t s) {
     PCHECK(c, cudaMemsetAsync(c->J2.p, 0, (size_t)L * N * sizeof(double), s));
     PCHECK(c, cudaMemsetAsync(c->status.p, 0, (size_t)N * sizeof(int), s));
     if (a.segs) PCHECK(c, cudaMemsetAsync(a.segs, 0, (size_t)N * sizeof(int), s));
+    if (a.kmom) PCHECK(c, cudaMemsetAsync(a.kmom, 0, (size_t)6 * N * sizeof(float), s));
     if (a.JE) {
         PCHECK(c, cudaMemsetAsync(c->JE.p, 0, (size_t)L * N * sizeof(double), s));
         PCHECK(c, cudaMemsetAsync(c->LS.p, 0, (size_t)L * N * sizeof(double), s));
@@ -410,5 +411,16 @@ extern "C" int portal_node_segments(portal_ctx *c, int *segments) {
     PCHECK(c, cudaMemcpyAsync(segments, c->nodeseg.p, (size_t)c->N * sizeof(int), cudaMemcpyDeviceToHost,
                               c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));
+    return PORTAL_OK;
+}
+
+extern "C" int portal_field_moments(portal_ctx *c, double *moments) {
+    if (!c || !moments) return PORTAL_ERR_ARG;
+    if (!c->j_valid || !c->kmom.p) return set_err(c, PORTAL_ERR_STATE, "no radiation field computed");
+    std::vector<float> h((size_t)6 * c->N);
+    PCHECK(c, cudaMemcpyAsync(h.data(), c->kmom.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    PCHECK(c, cudaStreamSynchronize(c->stream));
+    for (int n = 0; n < c->N; n++)
+        for (int k = 0; k < 6; k++) moments[6 * (size_t)n + k] = (double)h[(size_t)k * c->N + n];
     return PORTAL_OK;
 }

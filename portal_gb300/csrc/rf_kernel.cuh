@@ -98,6 +98,7 @@ struct RayBatch {
     double frame[13];    // b(3), x(3), w(3), node position(3), |p|^2
     float4 dir[32];      // (d_x, d_y, d_z, v_node . d) per ray
     int K[32];           // segments per ray (-1: n_depth overflow)
+    float km[6];         // the node's second moment of line 1 (lane 0 accumulates)
 };
 // The batched kernel's: also the per-node ray sets of star mode.
 struct RayBatchStar {
@@ -108,6 +109,7 @@ struct RayBatchStar {
     float4 dir[32];
     float2 wts[32];      // (w, w c_in / sqrt 2) per ray
     int K[32];
+    float km[6];
 };
 
 constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
@@ -297,6 +299,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                 f[0] = bx; f[1] = by; f[2] = bz; f[3] = xx; f[4] = xy; f[5] = xz;
                 f[6] = xy * bz - xz * by; f[7] = xz * bx - xx * bz; f[8] = xx * by - xy * bx;
                 f[9] = px; f[10] = py; f[11] = pz; f[12] = px * px + py * py + pz * pz;
+                for (int k = 0; k < 6; k++) B.km[k] = 0.f;
                 if constexpr (BATCH) {
                     if (a.star) {
                         star_node(B.sk, B.sn, a.xs, a.ys, a.zs, a.Rs, a.nth, a.nph, px, py, pz);
@@ -456,6 +459,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                         for (int hi = Kr - 1; hi >= 1; hi -= 32) {
                             const int nc = min(32, hi);
                             __syncwarp();
+                            bool thin_cell = true;   // every line of the group thin in this cell
                             if (lane < nc) {
                                 const int2 wc = wl[hi - lane];
                                 const float4 cv = a.cellv[wc.x];
@@ -493,9 +497,17 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                             }
                                         }
                                         R.AS[lane][l] = make_float2(As, Ss);
+                                        thin_cell = thin_cell && (As < OM_TAYLOR_X);
                                     }
                                 }
                             }
+                            // A chunk whose every (cell, line) has a line-centre optical
+                            // depth below the Taylor switch takes the Taylor form of
+                            // 1 - e^-tau in every channel (x = A g <= A, g <= 1): the
+                            // branch-free update would select exactly that value, so the
+                            // chunk skips the ex2 and the select.  Decided per chunk of 32
+                            // cells, uniform over the warp.
+                            const bool thin = !DUST && __all_sync(FULL, thin_cell);
                             __syncwarp();
                             if (RT && l0 == 0 && lane < a.L) {
                                 // the remainder channel, lane = line, the same cells inward
@@ -523,7 +535,9 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 }
                                 for (; u < nc; u++) step(a.ltab[(size_t)R.cell[u] * a.L + lane], u);
                             }
-                            for (int u = 0; u < nc; u++) {
+                            // one cell's update of the group's lines in every channel slot
+                            auto cell_step = [&](auto thin_tag, int u) {
+                                constexpr bool THIN = decltype(thin_tag)::value;
                                 const float2 qd = R.qd[u];
                                 const float q0 = qd.x, dq = qd.y;
                                 // Gaussian profile of the cell at the lane's channels,
@@ -581,18 +595,24 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
 #pragma unroll
                                         for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
                                             const float2 x = __fmul2_rn(A2, make_float2(g[s2], g[s2 + 1]));
-                                            const float2 om = one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
+                                            const float2 om =
+                                                THIN ? om_taylor2(x) : one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
                                             float2 &Ip = I2[s2 >> 1][l];
                                             Ip = __ffma2_rn(om, __ffma2_rn(Ip, make_float2(-1.f, -1.f), S2), Ip);
                                         }
                                         if (NS & 1) {
                                             const float x = Au * g[NS - 1];
-                                            const float om = one_minus_exp(x, ex2(-x));
+                                            const float om = THIN ? om_taylor(x) : one_minus_exp(x, ex2(-x));
                                             float &Is = I2[NS >> 1][l].x;
                                             Is = fmaf(om, Su - Is, Is);
                                         }
                                     }
                                 }
+                            };
+                            if (thin) {
+                                for (int u = 0; u < nc; u++) cell_step(std::true_type{}, u);
+                            } else {
+                                for (int u = 0; u < nc; u++) cell_step(std::false_type{}, u);
                             }
                         }
                         // central cell (inverse_rt.f90:320-339): no gate, profile at
@@ -660,6 +680,17 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                     if (RT) v += remJ;   // this lane's line: its remainder channel
                                     acc0a.add(wgt * v);
                                     acc2a.add(wgt2 * v);
+                                    if (line == 0) {
+                                        // the full second moment of line 1's field, sum w I n n,
+                                        // whose traceless part is J^2_Q in any frame
+                                        const float wv = wgt * v;
+                                        B.km[0] = fmaf(wv * d4.x, d4.x, B.km[0]);
+                                        B.km[1] = fmaf(wv * d4.y, d4.y, B.km[1]);
+                                        B.km[2] = fmaf(wv * d4.z, d4.z, B.km[2]);
+                                        B.km[3] = fmaf(wv * d4.x, d4.y, B.km[3]);
+                                        B.km[4] = fmaf(wv * d4.x, d4.z, B.km[4]);
+                                        B.km[5] = fmaf(wv * d4.y, d4.z, B.km[5]);
+                                    }
                                 } else {
                                     acc0b.add(wgt * v);
                                     acc2b.add(wgt2 * v);
@@ -718,6 +749,9 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
         if (lane == 0) {
             a.status[node] = st;
             if (a.segs) a.segs[node] = node_seg;
+            if (a.kmom)
+                for (int k = 0; k < 6; k++)
+                    a.kmom[(size_t)k * a.N + node] = (st == 0 && a.ab[node] > 0.0) ? B.km[k] : 0.f;
         }
         nseg += (unsigned long long)node_seg;
         __syncwarp();

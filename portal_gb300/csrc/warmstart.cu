@@ -7,9 +7,12 @@
 //   1  log10 T_kin [K]
 //   2  log10 |grad v| [s^-1]: Frobenius norm of the least-squares velocity
 //      gradient over the node's Delaunay neighbours
-//   3  cos^2 of the angle between the field and the principal axis of the
-//      symmetric velocity gradient (the direction the line opacity is most
-//      anisotropic along)
+//   3  cos^2 of the angle between the magnetic field and the local J^2_0
+//      axis of line 1: the principal axis (largest |eigenvalue|) of the
+//      traceless part of the field's second moment sum_rays w I n n, whose
+//      five components are J^2_Q in any frame -- J^2_0 is extremal along it.
+//      The reference forms J^2_0 in each node's field frame only
+//      (inverse_rt.f90:128-129), so this direction has no counterpart there.
 //   4  log10 J^0_0 / B_nu(T_kin) of line 1
 //   5  log10 J^0_0 / B_nu(T_kin) of line 2 (line 1 again for one-line molecules)
 //   6  100 J^2_0 / J^0_0 of line 1
@@ -32,7 +35,7 @@ __global__ void k_features(int N, int L, double tx, double nu0, double nu1, cons
                            const double *__restrict__ vel, const double *__restrict__ bvec,
                            const double *__restrict__ h2, const double *__restrict__ tk,
                            const int *__restrict__ off, const int *__restrict__ idx, const double *__restrict__ J0,
-                           const double *__restrict__ J2, float *__restrict__ F) {
+                           const double *__restrict__ J2, const float *__restrict__ km, float *__restrict__ F) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     // least-squares gradient G (3x3): G = R M^-1, M = sum dx dx^T, R = sum dv dx^T
@@ -70,10 +73,12 @@ __global__ void k_features(int N, int L, double tx, double nu0, double nu1, cons
             G[3 * i + j] = s;
             gn += s * s;
         }
-    // principal axis of the symmetric part by power iteration on S^2
-    double S[9];
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) S[3 * i + j] = 0.5 * (G[3 * i + j] + G[3 * j + i]);
+    // the local J^2_0 axis: principal axis of the traceless second moment,
+    // by power iteration on its square
+    const double kxx = km[n], kyy = km[(size_t)N + n], kzz = km[2 * (size_t)N + n];
+    const double kxy = km[3 * (size_t)N + n], kxz = km[4 * (size_t)N + n], kyz = km[5 * (size_t)N + n];
+    const double tr3 = (kxx + kyy + kzz) / 3.0;
+    const double S[9] = {kxx - tr3, kxy, kxz, kxy, kyy - tr3, kyz, kxz, kyz, kzz - tr3};
     double v[3] = {0.57735, 0.57735, 0.57735};
     for (int it = 0; it < 20; it++) {
         double w[3], u[3];
@@ -110,10 +115,11 @@ extern "C" int portal_warmstart_features(portal_ctx *c, float *features) {
     const int N = c->N, L = c->r_num;
     DevBuf<float> F;
     if (F.reserve((size_t)N * 8)) return set_err(c, PORTAL_ERR_NOMEM, "features");
+    if (!c->kmom.p) return set_err(c, PORTAL_ERR_STATE, "no radiation field computed");
     const double nu1 = c->nu[L > 1 ? 1 : 0];
     k_features<<<(N + 127) / 128, 128, 0, c->stream>>>(N, L, c->tx, c->nu[0], nu1, c->pos64.p, c->vel64.p,
                                                        c->bvec64.p, c->h2.p, c->tkin.p, c->nb_off.p, c->nb_idx.p,
-                                                       c->J0.p, c->J2.p, F.p);
+                                                       c->J0.p, c->J2.p, c->kmom.p, F.p);
     PCHECK(c, cudaGetLastError());
     PCHECK(c, cudaMemcpyAsync(features, F.p, (size_t)N * 8 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));

@@ -110,3 +110,71 @@ def test_local_operator_reaches_the_plain_fixed_point(built_lib, sphere4k, ng):
     assert n1 < 0.5 * n0
     r0, r1 = pp0[:, 0::2], pp1[:, 0::2]
     assert np.abs(r1 - r0).max() <= 5e-5 * np.abs(r0).max()
+
+
+def _fixed_point_case():
+    """The 1,024-point turbulent cube and the FP64 oracle's fixed point of
+    its iterated node loop (tests/golden/make_fixed_point.py)."""
+    import os
+    from portal_gb300 import synth
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fixed_point_cube1k.npz")
+    z = np.load(path)
+    n_points, seed, grid, nlev, nth, nph, nvel, kmax, gauge_seed = (int(v) for v in z["case"])
+    mol = synth.linear_rotor(nlev)
+    cloud = synth.Cloud(xyz=z["xyz"], vel=z["vel"], b_all=z["b_all"], t_kin=z["t_kin"], t_dust=z["t_dust"],
+                        dust_p=z["dust_p"], h2_dens=z["h2_dens"], ab_all=z["ab_all"], lev_p=z["lev_p"],
+                        bvec=z["bvec"], nb_off=z["nb_off"], nb_idx=z["nb_idx"], tx=float(z["tx"]),
+                        bulk_node_num=int(z["bulk_node_num"]))
+    rc = synth.RunConfig(nth=nth, nph=nph, nvel=nvel, kmax=kmax, gvec=tuple(float(v) for v in z["gvec"]))
+    return cloud, mol, rc, z["pol_pops"], float(z["last_change"])
+
+
+def test_fixed_point_fixture_is_a_fixed_point_of_the_oracle():
+    """One more FP64 oracle pass from the fixture's populations changes them
+    by less than the fixture's last change (1e-13 scale)."""
+    import oracle
+    cloud, mol, rc, fp, last = _fixed_point_case()
+    assert last < 1e-12
+    n_mol = cloud.lev_p.sum(axis=1)
+    g = np.sqrt(2 * mol.j_lev + 1.0)
+    P = oracle.OracleProblem(cloud, mol)
+    P.lev_p[:] = n_mol[:, None] * g[None, :] * fp[:, 0::2]
+    J0, J2, _, _, _ = P.radiation_field(rc)
+    pp, _, _ = P.solve_se(rc.kmax, J0, J2)
+    assert np.max(np.abs(pp[:, 0::2] - fp[:, 0::2]) / np.abs(fp[:, 0::2])) < 1e-11
+
+
+@pytest.mark.gpu
+def test_iteration_limits_against_the_fp64_fixed_point(built_lib):
+    """Where each method of portal_lambda_iterate ends up, against the FP64
+    oracle's fixed point of the same iterated node loop: the accelerated
+    iteration (local operator + Ng) run to its floor, and the plain and Ng
+    iterations run to theirs (1,500 / 400 passes, far past their change-per-
+    pass floors).  With J in FP32 (~5e-7 relative) a perturbation dJ moves the
+    plain map's fixed point by ~dJ / (1 - q), q the contraction per pass,
+    while the preconditioned map is well conditioned: the accelerated limit
+    sits an order of magnitude closer to the FP64 fixed point.  The change-
+    per-pass rule (tol 1e-6) stops every method within 1e-4 of it."""
+    import portal_gb300 as pg
+    from portal_gb300 import convergence as conv
+    cloud, mol, rc, fp, _ = _fixed_point_case()
+    live = np.zeros(cloud.node_num, dtype=bool)
+    live[:cloud.bulk_node_num] = cloud.ab_all[:cloud.bulk_node_num] > 0
+    errs = {}
+    with pg.Context(0) as ctx:
+        ctx.set_molecule(mol)
+        for name, ng, lo, passes in (("plain", 0, False, 1500), ("ng", 4, False, 400),
+                                     ("accelerated", 4, True, 200)):
+            ctx.set_cloud(cloud)
+            pp, _, n, res, _ = ctx.lambda_iterate(rc, tol=conv.TINY_TOL, max_iter=passes, ng_period=ng,
+                                                  local_operator=lo)
+            errs[name] = conv.rho_errors(pp, fp, live)
+            ctx.set_cloud(cloud)
+            pr, _, nr, rr, _ = ctx.lambda_iterate(rc, tol=1e-6, max_iter=3000, ng_period=ng, local_operator=lo)
+            errs[name + " at tol 1e-6"] = conv.rho_errors(pr, fp, live)
+            print("LIMIT %s: %d passes -> err rho00 %.2e rho20 %.2e (last change %.1e); tol 1e-6 after %d "
+                  "passes -> %.2e %.2e" % (name, n, *errs[name], res[-1], nr, *errs[name + " at tol 1e-6"]))
+    assert errs["accelerated"][0] < 5e-6 and errs["accelerated"][1] < 2e-6
+    assert errs["plain"][0] < 1e-4 and errs["ng"][0] < 1e-4
+    for k, (e0, e2) in errs.items():
+        assert e0 < 1e-4 and e2 < 2e-5, k

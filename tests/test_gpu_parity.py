@@ -102,6 +102,27 @@ def test_node_loop_chain_sphere4k(ctx, sphere4k, sphere4k_oracle):
     assert (np.abs(pops[:, 1::2] - opp[:, 1::2]) / scale).max() < 2e-5
 
 
+def test_field_moments_hold_j20_in_every_frame(ctx, sphere4k):
+    """The second moment M = sum w Ibar n n of line 1 (the warm start's J^2_0
+    axis): its trace is J^0_0 and, along the node's field b, (3 b.M.b -
+    tr M) / (2 sqrt 2) is the field-frame J^2_0 of inverse_rt.f90:128-129."""
+    cloud, mol, rc = sphere4k
+    J0, J2, st, _ = _rf(ctx, cloud, mol, rc)
+    M = ctx.field_moments()
+    b = cloud.bvec
+    bMb = (M[:, 0] * b[:, 0] ** 2 + M[:, 1] * b[:, 1] ** 2 + M[:, 2] * b[:, 2] ** 2 +
+           2.0 * (M[:, 3] * b[:, 0] * b[:, 1] + M[:, 4] * b[:, 0] * b[:, 2] + M[:, 5] * b[:, 1] * b[:, 2]))
+    tr = M[:, 0] + M[:, 1] + M[:, 2]
+    live = cloud.ab_all > 0
+    live[cloud.bulk_node_num:] = False
+    j0 = J0[live, 0]
+    assert (np.abs(tr[live] - j0) / j0).max() < 1e-4
+    j20 = (3.0 * bMb - tr) / (2.0 * np.sqrt(2.0))
+    assert (np.abs(j20[live] - J2[live, 0]) / j0).max() < 1e-4
+    assert np.abs(J2[live, 0]).max() > 1e-3 * j0.max()   # an anisotropic field to test against
+    assert not M[~live].any()
+
+
 def test_deterministic(ctx, sphere4k):
     cloud, mol, rc = sphere4k
     a = _rf(ctx, cloud, mol, rc)
