@@ -355,6 +355,67 @@ def se_large_stage(device, cloud, nlev=20, kmax=6, reps=2):
             "singular": int(((st & pg.NODE_SINGULAR) != 0).sum())}
 
 
+def warmstart_1m_leg(device, n_train=8, train_points=16384, epochs=60):
+    """The learned warm start on a held-out cube of the 1M-point recipe
+    (1,048,576 points, seed 301): the network is trained as in the
+    convergence leg (eight 16,384-point cubes of the same recipe), then the
+    1M cube is converged by the accelerated iteration (local operator + Ng,
+    plain pass deciding at tol 1e-6) from LTE and from the network's start;
+    the 1025 x 1025 x 257 Stokes cube of the converged state follows.  16x16
+    directions and 65 channels (at 32x32 / 129 one pass takes ~53 s; the
+    plain iteration, ~370 passes, is not run at this size)."""
+    import torch
+    import portal_gb300 as pg
+    from portal_gb300 import synth
+    from portal_gb300.warmstart import WarmStart
+    mol = synth.linear_rotor(20)
+    rc = synth.RunConfig(nth=16, nph=16, nvel=32, kmax=2, gvec=synth.gauge_vector(4))
+    out = {"workload": "turbulent cube, 1,048,576 points (seed 301, 128^3 fields), 20-level rotor, 16x16 "
+                       "directions, 65 channels, kmax 2; network trained on %d cubes of %d points" %
+                       (n_train, train_points)}
+    with WarmStart(mol.j_lev, seed=1, device=device) as ws, pg.Context(device) as ctx:
+        ctx.set_molecule(mol)
+        t0 = time.perf_counter()
+        Xs, Ys = [], []
+        for i in range(n_train):
+            cl = synth.turbulent_cube(train_points, 200 + i, mol, grid=32)
+            ctx.set_cloud(cl)
+            X, Y, _ = ws.collect(ctx, rc, cl.ab_all, cl.bulk_node_num)
+            Xs.append(X)
+            Ys.append(Y)
+        t1 = time.perf_counter()
+        ws.fit(np.concatenate(Xs), np.concatenate(Ys), epochs=epochs)
+        out["training_seconds"] = {"data": t1 - t0, "fit": time.perf_counter() - t1}
+        t0 = time.perf_counter()
+        big = synth.turbulent_cube(1048576, 301, mol, grid=128)
+        out["cloud_generation_s"] = time.perf_counter() - t0
+        res = {}
+        for name, warm in (("accelerated", False), ("warm_accelerated", True)):
+            ctx.set_cloud(big)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if warm:
+                pp, _, n, r, nseg = ws.solve(ctx, rc, tol=1e-6, max_iter=400, ng_period=4, local_operator=True)
+            else:
+                pp, _, n, r, nseg = ctx.lambda_iterate(rc, tol=1e-6, max_iter=400, ng_period=4, local_operator=True)
+            torch.cuda.synchronize()
+            res[name] = pp
+            out[name] = {"passes": int(n) + (1 if warm else 0), "seconds": time.perf_counter() - t0,
+                         "last_change": float(r[-1]), "segments": int(nseg)}
+        a, w = res["accelerated"][:, 0::2], res["warm_accelerated"][:, 0::2]
+        sig = np.abs(a) >= 1e-12 * np.abs(a).max(axis=1, keepdims=True)
+        out["max_rel_diff_rho00"] = float((np.abs(w - a) / np.where(sig, np.abs(a), 1.0))[sig].max())
+        out["speedup_warm"] = out["accelerated"]["seconds"] / out["warm_accelerated"]["seconds"]
+        # the 1025 x 1025 x 257 Stokes cube of the converged state
+        ctx.image([1], [2], 0.78539816339, 0.0, 128, 50.0, 0.0, 512, 0.7, pol_pops=res["warm_accelerated"],
+                  quantities=4)
+        kt = ctx.kernel_times()
+        im_ms = kt["emcoefs"][0] + kt["image_walk"][0] + kt["image_rt"][0]
+        out["image"] = {"cube": "1025 x 1025 pixels x 257 channels, line 1-0, 45 degrees", "kernel_ms": im_ms,
+                        "pixel_channels_per_s": 1025 * 1025 * 257 / (im_ms * 1e-3)}
+    return out
+
+
 def _batch_cloud_worker(i):
     from portal_gb300 import synth
     return synth.batch_cloud(i)
@@ -687,6 +748,8 @@ def gpu_arm(args, rank, world, local_rank):
         line["batch64"] = batch_leg(local_rank)
     if rank == 0 and world == 1 and not args.no_convergence:
         line["convergence"] = convergence_leg(local_rank)
+    if rank == 0 and world == 1 and args.warmstart_1m:
+        line["warmstart_1m"] = warmstart_1m_leg(local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -710,6 +773,8 @@ def main():
                     help="skip the 1,048,576-point turbulent-cube pass")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-cloud batch (persistent launch under a CUDA graph)")
+    ap.add_argument("--warmstart-1m", action="store_true",
+                    help="also run the learned warm start on a held-out 1,048,576-point cube (~10 min)")
     ap.add_argument("--no-se-large", action="store_true",
                     help="skip the 74 x 74 SE throughput stage (20-level rotor, kmax 6)")
     ap.add_argument("--no-convergence", action="store_true",

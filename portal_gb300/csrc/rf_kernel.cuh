@@ -17,6 +17,10 @@ constexpr float LOG2E_F = 1.4426950408889634f;
 // sqrt(log2 e): a profile argument q scaled by it gives exp(-q^2) = 2^(-q'^2),
 // one ex2 of q'^2 with the sign folded into the instruction
 constexpr float SQL2E_F = 1.2011224087864498f;
+// line-centre optical depth (log2 units) below which every channel of a cell
+// takes the Taylor form: the switch OM_TAYLOR_X less 0.5 %, far more than the
+// few ulp by which ex2 may return a profile value above 1
+constexpr float OM_THIN_A = 0.0625f;
 // Face crossings closer than this (in units of r_max) are not taken.  The
 // reference uses 1e-10 (miscellaneous.f90:1048) against FP64 noise ~1e-16;
 // the FP32 walk's noise in t is ~1e-9, and a crossing shorter than 2e-8 is
@@ -497,16 +501,18 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                             }
                                         }
                                         R.AS[lane][l] = make_float2(As, Ss);
-                                        thin_cell = thin_cell && (As < OM_TAYLOR_X);
+                                        thin_cell = thin_cell && (As < OM_THIN_A);
                                     }
                                 }
                             }
                             // A chunk whose every (cell, line) has a line-centre optical
                             // depth below the Taylor switch takes the Taylor form of
-                            // 1 - e^-tau in every channel (x = A g <= A, g <= 1): the
-                            // branch-free update would select exactly that value, so the
-                            // chunk skips the ex2 and the select.  Decided per chunk of 32
-                            // cells, uniform over the warp.
+                            // 1 - e^-tau in every channel (x = A g <= A: the profile g
+                            // is at most 1, to within the ex2 rounding that the margin of
+                            // OM_THIN_A covers): the branch-free update would select
+                            // exactly that value, so the chunk skips the ex2 and the
+                            // select.  Decided per chunk of 32 cells, uniform over the
+                            // warp.
                             const bool thin = !DUST && __all_sync(FULL, thin_cell);
                             __syncwarp();
                             if (RT && l0 == 0 && lane < a.L) {
@@ -584,11 +590,12 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                         // (inverse_rt.f90:308) needs no test: lines with kv <= 0
                                         // carry A = S = 0 and leave I unchanged exactly, and
                                         // 0 < tau < 2^-54 rounds to a zero weight as in FP64.
-                                        // Branch-free, so the NS x NLG update chains of a cell
-                                        // interleave: a warp-uniform branch to a Taylor-only
-                                        // path for lines thin in the whole cell measured 24 %
-                                        // slower in spite of skipping the ex2 (1.45e9 against
-                                        // 1.90e9 segments/s).  Channel-slot pairs go through
+                                        // Branch-free inside a cell, so the NS x NLG update
+                                        // chains interleave: a warp-uniform branch per cell to
+                                        // a Taylor-only path measured 24 % slower in spite of
+                                        // skipping the ex2 (1.45e9 against 1.90e9 segments/s);
+                                        // decided once per chunk of 32 cells (THIN) it gains
+                                        // (1.96e9 -> 2.03e9).  Channel-slot pairs go through
                                         // the packed FP32x2 pipe (one issue slot for two
                                         // updates).
                                         const float2 A2 = make_float2(Au, Au), S2 = make_float2(Su, Su);

@@ -89,8 +89,14 @@ def test_trained_network_reduces_passes_to_the_same_fixed_point(built_lib):
                                    ("acc", False, 4, True), ("warm+acc", True, 4, True)):
             runs[name] = conv.time_to_error(ctx, lambda: ctx.set_cloud(cl), rc, ref, live, ng_period=ng,
                                             local_operator=lo, warm=ws if warm else None)
+        # finish_portal takes rho^0_0 from the level populations and only the
+        # alignment ratio from pol_pops (para_finish.f90:226-239): each image
+        # runs on its own converged populations
+        n_mol = cl.lev_p.sum(axis=1)
+        g = np.sqrt(2.0 * mol.j_lev + 1.0)
         imgs = {}
         for name, r in runs.items():
+            ctx.set_populations(n_mol[:, None] * g[None, :] * r["pol_pops"][:, 0::2])
             imgs[name], st = ctx.image([1], [2], im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
                                        im["im_pix"], im["im_size"], pol_pops=r["pol_pops"])
     for name, r in runs.items():
@@ -107,6 +113,7 @@ def test_trained_network_reduces_passes_to_the_same_fixed_point(built_lib):
     # the converged populations' image against the FP64 oracle's image of
     # the reference fixed point
     P = oracle.OracleProblem(cl, mol)
+    P.lev_p[:] = n_mol[:, None] * g[None, :] * ref[:, 0::2]
     npx, nch = 2 * im["im_pix"] + 1, 2 * im["nvel"] + 1
     ocube, _, nf = P.image([1], [2], ref, im["th_inc"], im["ph_az"], im["nvel"], im["dvel"], im["v0"],
                            im["im_pix"], im["im_size"])
