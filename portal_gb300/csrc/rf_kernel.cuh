@@ -35,13 +35,17 @@ constexpr int MAX_LINES = 64;
 
 // Compensated (Kahan) FP32 sum: J of one node is a sum of a few hundred ray
 // contributions; the compensation keeps it to ~1e-7 of the sum of magnitudes
-// without the FP64 pipe.
+// without the FP64 pipe.  The terms are passed as explicitly rounded products
+// (__fmul_rn at the call sites) and summed with explicit roundings: a
+// multiply the compiler fuses into the first subtraction in one kernel
+// variant and not in another would make the result depend on the line
+// grouping of the variant.
 struct KahanF {
     float s = 0.f, c = 0.f;
     __device__ __forceinline__ void add(float x) {
-        const float y = x - c;
-        const float t = s + y;
-        c = (t - s) - y;
+        const float y = __fsub_rn(x, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
         s = t;
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
@@ -467,7 +471,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             if (lane < nc) {
                                 const int2 wc = wl[hi - lane];
                                 const float4 cv = a.cellv[wc.x];
-                                const float vp = cv.x * d4.x + cv.y * d4.y + cv.z * d4.z;
+                                const float vp = fmaf(cv.z, d4.z, fmaf(cv.y, d4.y, __fmul_rn(cv.x, d4.x)));
                                 const float ib = SQL2E_F * (1.f / cv.w);
                                 R.qd[lane] = make_float2((d4.w - vp) * ib, dqfac * ib);
                                 const float fst = (float)wc.y;
@@ -632,10 +636,10 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             const float g0 = ex2(-q0c * q0c * LOG2E_F);
                             const float x = v.x * g0 * fst0 * LOG2E_F;
                             const float om = one_minus_exp(x, ex2(-x));
-                            remJ = a.chw[ch] * fmaf(om, v.y - Irem, Irem);
+                            remJ = __fmul_rn(a.chw[ch], fmaf(om, v.y - Irem, Irem));
                             if (split) {
-                                remE = a.chw[ch] * fmaf(om, -Irem, Irem);
-                                remL = a.chw[ch] * om;
+                                remE = __fmul_rn(a.chw[ch], fmaf(om, -Irem, Irem));
+                                remL = __fmul_rn(a.chw[ch], om);
                             }
                         }
                         float part[NLG], pe[NLG], pl[NLG];
@@ -684,13 +688,13 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             const int line = l0 + l;
                             if (line < a.L && (line & 31) == lane) {
                                 if (line < 32) {
-                                    if (RT) v += remJ;   // this lane's line: its remainder channel
-                                    acc0a.add(wgt * v);
-                                    acc2a.add(wgt2 * v);
+                                    if (RT) v = __fadd_rn(v, remJ);   // this lane's line: its remainder channel
+                                    acc0a.add(__fmul_rn(wgt, v));
+                                    acc2a.add(__fmul_rn(wgt2, v));
                                     if (line == 0) {
                                         // the full second moment of line 1's field, sum w I n n,
                                         // whose traceless part is J^2_Q in any frame
-                                        const float wv = wgt * v;
+                                        const float wv = __fmul_rn(wgt, v);
                                         B.km[0] = fmaf(wv * d4.x, d4.x, B.km[0]);
                                         B.km[1] = fmaf(wv * d4.y, d4.y, B.km[1]);
                                         B.km[2] = fmaf(wv * d4.z, d4.z, B.km[2]);
@@ -699,8 +703,8 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                         B.km[5] = fmaf(wv * d4.y, d4.z, B.km[5]);
                                     }
                                 } else {
-                                    acc0b.add(wgt * v);
-                                    acc2b.add(wgt2 * v);
+                                    acc0b.add(__fmul_rn(wgt, v));
+                                    acc2b.add(__fmul_rn(wgt2, v));
                                 }
                             }
                         }
@@ -717,14 +721,14 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 if (line < a.L && (line & 31) == lane) {
                                     if (line < 32) {
                                         if (RT) {
-                                            ve += remE;
-                                            vl += remL;
+                                            ve = __fadd_rn(ve, remE);
+                                            vl = __fadd_rn(vl, remL);
                                         }
-                                        accEa.add(wgt * ve);
-                                        accLa.add(wgt * vl);
+                                        accEa.add(__fmul_rn(wgt, ve));
+                                        accLa.add(__fmul_rn(wgt, vl));
                                     } else {
-                                        accEb.add(wgt * ve);
-                                        accLb.add(wgt * vl);
+                                        accEb.add(__fmul_rn(wgt, ve));
+                                        accLb.add(__fmul_rn(wgt, vl));
                                     }
                                 }
                             }
