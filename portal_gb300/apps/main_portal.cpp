@@ -94,7 +94,31 @@ int main(int argc, char **argv) {
     if (in.star_mod != 0 && in.star_mod != 1) return fail("star_mod must be 0 or 1");
     Molecule m;
     Cloud c;
-    if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err)) return fail(err);
+    // the neighbour lists are built on the device (portal_adj_list), by the
+    // context the run then uses; PORTAL_HOST_NEIGHBOURS=1 builds them on the
+    // host instead (the same lists); the dump of the ingested
+    // arrays (PORTAL_DUMP_INGESTED) needs no device and builds them on the host
+    const int dev = getenv("PORTAL_DEVICE") ? atoi(getenv("PORTAL_DEVICE")) : 0;
+    portal_ctx *ctx = nullptr;
+    const bool device_lists = !getenv("PORTAL_DUMP_INGESTED") && !getenv("PORTAL_HOST_NEIGHBOURS");
+    if (device_lists && portal_create(&ctx, dev))
+        return fail(std::string("portal_create: ") + portal_last_error(nullptr));
+    const NeighbourBuilder on_device = [&](int N, const std::vector<int> &tets, int max_ne_temp, Cloud &cl,
+                                           std::string &e) {
+        int mx = 0;
+        cl.del_ne.assign((size_t)N * max_ne_temp, 0);
+        cl.del_num_ne.assign(N, 0);
+        if (portal_adj_list(ctx, N, (long long)(tets.size() / 4), tets.data(), max_ne_temp, cl.del_ne.data(),
+                            cl.del_num_ne.data(), &mx, nullptr)) {
+            e = std::string("neighbour lists: ") + portal_last_error(ctx);
+            return false;
+        }
+        cl.maxne = mx;
+        cl.del_ne.resize((size_t)N * mx);  // main_para.f90:124-128: the first maxne columns
+        return true;
+    };
+    if (!read_lime(pop, grid, mol, dust, 0.01, in.max_ne_temp, m, c, err, device_lists ? &on_device : nullptr))
+        return fail(err);
     std::vector<double> bvec;
     if (const char *bf = getenv("PORTAL_BVEC_FILE")) {
         std::vector<double> rows;  // (N,3) column-major: N lines of 3 numbers
@@ -119,10 +143,7 @@ int main(int argc, char **argv) {
                m.nlev, dd);
         return 0;
     }
-    const int dev = getenv("PORTAL_DEVICE") ? atoi(getenv("PORTAL_DEVICE")) : 0;
-    portal_ctx *ctx = nullptr;
-    int rc = portal_create(&ctx, dev);
-    if (rc) return fail(std::string("portal_create: ") + portal_last_error(nullptr));
+    if (!ctx && portal_create(&ctx, dev)) return fail(std::string("portal_create: ") + portal_last_error(nullptr));
     auto chk = [&](int r, const char *what) {
         if (r) {
             fprintf(stderr, "main_portal: %s: %s (%s)\n", what, portal_strerror(r), portal_last_error(ctx));

@@ -319,41 +319,14 @@ bool read_finish_input(const std::string &path, FinishInput &in, std::string &er
 // LIME / LAMDA / dust
 // ---------------------------------------------------------------------------
 
-bool read_lime(const std::string &pop, const std::string &grid, const std::string &mol,
-               const std::string &dust, double dust_ii_gas, int max_ne_temp, Molecule &m, Cloud &c,
-               std::string &err) {
-    (void)dust_ii_gas;  // the per-node gas-to-dust column of the .pop is what eat_lime uses
-    std::vector<std::string> t;
-    std::vector<double> vd;
-    g_bad.clear();
-    // ---- grid.vtk: points (eat_lime_dim eat_lime.f90:21-34, :124-136) ----
-    ListReader g(grid);
-    if (!g.ok()) { err = "cannot open " + grid; return false; }
-    for (int k = 0; k < 4; k++) g.skip();
-    if (!g.read(t, 2)) { err = grid + ": POINTS line"; return false; }
-    const int N = to_int(t[1]);
-    if (N < 1) { err = grid + ": no points"; return false; }
-    c.node_num = N;
-    c.xyz.resize(3 * (size_t)N);
-    const int nth = io_threads();
-    const size_t np = g.read_block_doubles(c.xyz.data(), (size_t)N, 3, nth);
-    if (np < (size_t)N) { err = grid + ": point " + std::to_string(np + 1); return false; }
-    g.skip();
-    if (!g.read(t, 2)) { err = grid + ": CELLS line"; return false; }
-    const int ntet = to_int(t[1]);
-    std::vector<int> cells(5 * (size_t)std::max(ntet, 0));
-    const size_t nc = g.read_block_ints(cells.data(), (size_t)std::max(ntet, 0), 5, nth);
-    if (nc < (size_t)std::max(ntet, 0)) { err = grid + ": cell " + std::to_string(nc + 1); return false; }
-    for (size_t q = 0; q < nc; q++)
-        for (int k = 0; k < 4; k++) {
-            const int v = cells[5 * q + 1 + k] + 1;
-            if (v < 1 || v > N) { err = grid + ": cell vertex out of range"; return false; }
-        }
-    // adj_list_no_delaunay miscellaneous.f90:910-1015: each tetrahedron gives
-    // its vertices the other three; SortUnique then sorts and de-duplicates.
-    // Built as a CSR: incidence counts, offsets, the raw lists (filled in
-    // tetrahedron order per thread range, so the per-node lists are the same
-    // multiset whatever the thread count), then a per-node sort + unique.
+// adj_list_no_delaunay miscellaneous.f90:910-1015 on the host: each
+// tetrahedron gives its vertices the other three; SortUnique then sorts and
+// de-duplicates.  Built as a CSR: incidence counts, offsets, the raw lists
+// (filled in tetrahedron order per thread range, so the per-node lists are
+// the same multiset whatever the thread count), then a per-node sort +
+// unique.  cells: nc records of (4, v0..v3), 0-based vertices.
+static bool host_neighbours(int N, const std::vector<int> &cells, size_t nc, int max_ne_temp, int nth, Cloud &c,
+                            std::string &err) {
     std::vector<long long> roff((size_t)N + 1, 0);
     for (size_t q = 0; q < nc; q++)
         for (int k = 0; k < 4; k++) roff[(size_t)cells[5 * q + 1 + k] + 1] += 3;
@@ -395,6 +368,47 @@ bool read_lime(const std::string &pop, const std::string &grid, const std::strin
     c.del_ne.assign((size_t)N * maxne, 0);  // main_para.f90:124-128
     for (int i = 0; i < N; i++)
         for (int s2 = 0; s2 < c.del_num_ne[i]; s2++) c.del_ne[(size_t)i + (size_t)N * s2] = raw[(size_t)roff[i] + s2];
+    return true;
+}
+
+bool read_lime(const std::string &pop, const std::string &grid, const std::string &mol,
+               const std::string &dust, double dust_ii_gas, int max_ne_temp, Molecule &m, Cloud &c,
+               std::string &err, const NeighbourBuilder *build_neighbours) {
+    (void)dust_ii_gas;  // the per-node gas-to-dust column of the .pop is what eat_lime uses
+    std::vector<std::string> t;
+    std::vector<double> vd;
+    g_bad.clear();
+    // ---- grid.vtk: points (eat_lime_dim eat_lime.f90:21-34, :124-136) ----
+    ListReader g(grid);
+    if (!g.ok()) { err = "cannot open " + grid; return false; }
+    for (int k = 0; k < 4; k++) g.skip();
+    if (!g.read(t, 2)) { err = grid + ": POINTS line"; return false; }
+    const int N = to_int(t[1]);
+    if (N < 1) { err = grid + ": no points"; return false; }
+    c.node_num = N;
+    c.xyz.resize(3 * (size_t)N);
+    const int nth = io_threads();
+    const size_t np = g.read_block_doubles(c.xyz.data(), (size_t)N, 3, nth);
+    if (np < (size_t)N) { err = grid + ": point " + std::to_string(np + 1); return false; }
+    g.skip();
+    if (!g.read(t, 2)) { err = grid + ": CELLS line"; return false; }
+    const int ntet = to_int(t[1]);
+    std::vector<int> cells(5 * (size_t)std::max(ntet, 0));
+    const size_t nc = g.read_block_ints(cells.data(), (size_t)std::max(ntet, 0), 5, nth);
+    if (nc < (size_t)std::max(ntet, 0)) { err = grid + ": cell " + std::to_string(nc + 1); return false; }
+    for (size_t q = 0; q < nc; q++)
+        for (int k = 0; k < 4; k++) {
+            const int v = cells[5 * q + 1 + k] + 1;
+            if (v < 1 || v > N) { err = grid + ": cell vertex out of range"; return false; }
+        }
+    if (build_neighbours) {
+        std::vector<int> tets(4 * nc);
+        for (size_t q = 0; q < nc; q++)
+            for (int k = 0; k < 4; k++) tets[4 * q + k] = cells[5 * q + 1 + k];
+        if (!(*build_neighbours)(N, tets, max_ne_temp, c, err)) return false;
+    } else if (!host_neighbours(N, cells, nc, max_ne_temp, nth, c, err)) {
+        return false;
+    }
 
     if (!numbers_ok(grid, err)) return false;
     // ---- LAMDA (eat_lime_dim :38-62, eat_lime_no_delaunay :151-196) ----

@@ -5,6 +5,7 @@
 // into the same values.
 #pragma once
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -93,9 +94,17 @@ struct Cloud {
     std::vector<double> xyz, vel, b_all, temp_all, dust_p, h2_dens, ab_all, lev_p;  // Fortran layouts
     std::vector<int> del_ne, del_num_ne;   // del_ne(N,maxne) column-major, 1-based
 };
+// Builds del_ne / del_num_ne / maxne of a cloud of N nodes from its
+// tetrahedra (4 vertices each, 0-based as grid.vtk lists them): the step of
+// adj_list_no_delaunay (miscellaneous.f90:910-1015).  Returns false with err
+// set on failure.
+using NeighbourBuilder = std::function<bool(int N, const std::vector<int> &tets, int max_ne_temp, Cloud &c,
+                                            std::string &err)>;
+// build_neighbours: the construction of the neighbour lists, or null for the
+// host's (parallel CSR + per-node sort / unique)
 bool read_lime(const std::string &pop, const std::string &grid, const std::string &mol,
                const std::string &dust, double dust_ii_gas, int max_ne_temp, Molecule &m, Cloud &c,
-               std::string &err);
+               std::string &err, const NeighbourBuilder *build_neighbours = nullptr);
 
 // global_magfield / dipole_magfield miscellaneous.f90:553-641
 void magfield(const Cloud &c, double x1, double x2, double x3, double x_dip, std::vector<double> &bvec);
