@@ -335,6 +335,17 @@ __global__ void k_mse(int n, const float *__restrict__ Yp, const float *__restri
     if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
+// the epoch's loss on the device: one minibatch's block partial sums added,
+// in block order, to a running FP64 total (read once per epoch instead of a
+// stream synchronisation per minibatch)
+__global__ void k_loss_accum(int nb, const float *__restrict__ part, double *__restrict__ acc) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < nb; b++) s += part[b];
+        *acc += s;
+    }
+}
+
 __global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m,
                        float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -367,6 +378,7 @@ struct portal_mlp {
     DevBuf<float> params, grads, adam_m, adam_v, stats;
     DevBuf<float> act;   // activations / pre-activations for one batch
     DevBuf<float> xbuf, ybuf, part;
+    DevBuf<double> lossacc;  // the running loss of a training epoch
     DevBuf<int> idx;
     DevBuf<int> tc_err;  // set by a tensor-core GEMM whose completion wait timed out
     int cap_batch = 0;
@@ -653,9 +665,12 @@ extern "C" int portal_mlp_train(portal_mlp *m, const float *X, const float *Y, i
     if (pidx.reserve(M)) return mlp_fail(m, PORTAL_ERR_NOMEM, "MLP permutation");
     for (int ep = 0; ep < epochs; ep++) {
         std::shuffle(perm.begin(), perm.end(), rng);
-        double eloss = 0.0;
         int nbatch = 0;
         MCHECK(m, cudaMemcpyAsync(pidx.p, perm.data(), (size_t)M * sizeof(int), cudaMemcpyHostToDevice, m->stream));
+        if (loss_per_epoch) {
+            if (m->lossacc.reserve(1)) return mlp_fail(m, PORTAL_ERR_NOMEM, "loss accumulator");
+            MCHECK(m, cudaMemsetAsync(m->lossacc.p, 0, sizeof(double), m->stream));
+        }
         MCHECK(m, cudaStreamSynchronize(m->stream));  // perm is rewritten next epoch
         for (int b0 = 0; b0 + B <= M; b0 += B) {
             k_gather<<<(B + 127) / 128, 128, 0, m->stream>>>(B, nin, nout, pidx.p + b0, dX.p, dY.p, m->stats.p, w.X,
@@ -669,17 +684,16 @@ extern "C" int portal_mlp_train(portal_mlp *m, const float *X, const float *Y, i
             k_adam<<<(int)((m->n_params + 255) / 256), 256, 0, m->stream>>>((int)m->n_params, m->params.p, m->grads.p,
                                                                           m->adam_m.p, m->adam_v.p, lr, b1, b2,
                                                                           eps, c1, c2);
-            if (loss_per_epoch) {
-                std::vector<float> parts(nb);
-                MCHECK(m, cudaMemcpyAsync(parts.data(), m->part.p, nb * sizeof(float), cudaMemcpyDeviceToHost,
-                                          m->stream));
-                MCHECK(m, cudaStreamSynchronize(m->stream));
-                for (float p : parts) eloss += p;
-            }
+            if (loss_per_epoch) k_loss_accum<<<1, 32, 0, m->stream>>>(nb, m->part.p, m->lossacc.p);
             nbatch++;
         }
         MCHECK(m, cudaGetLastError());
-        if (loss_per_epoch) loss_per_epoch[ep] = (float)(eloss / std::max(nbatch, 1));
+        if (loss_per_epoch) {
+            double eloss = 0.0;
+            MCHECK(m, cudaMemcpyAsync(&eloss, m->lossacc.p, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+            MCHECK(m, cudaStreamSynchronize(m->stream));
+            loss_per_epoch[ep] = (float)(eloss / std::max(nbatch, 1));
+        }
     }
     MCHECK(m, cudaStreamSynchronize(m->stream));
     return tc_status(m);
