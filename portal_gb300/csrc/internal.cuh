@@ -86,6 +86,7 @@ struct RFBatch {
     unsigned long long *queue;   // [0] next item, [1] segments walked
     int2 *walk;                  // per warp: 32 rays x n_depth
     int n_depth;
+    int rem_lines;               // lines of the remainder channel's shared table (largest model)
 };
 struct SEBatch {
     const SEArgs *models;

@@ -100,8 +100,11 @@ template <int NS, int NLG, bool DUST, int RT>
 int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     auto kern = k_radiation_field<NS, NLG, DUST, false, RT>;
     const int wpb = rf_warps();
+    // the remainder channel's (cell, line) tables, one per warp
+    const size_t dyn = RT ? (size_t)wpb * 32 * rem_row_stride(a.L) * sizeof(float2) : 0;
+    if (dyn) PCHECK(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int nb = 0;
-    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 32 * wpb, 0));
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 32 * wpb, dyn));
     if (nb < 1) nb = 1;
     int grid = nb * c->sm_count;
     size_t nslots = (size_t)grid * wpb;
@@ -110,7 +113,7 @@ int launch_rf(portal_ctx *c, RFArgs &a, int n_depth) {
     a.walk = c->walk.p;
     PCHECK(c, cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     timer_start(c, T_RF);
-    kern<<<grid, 32 * wpb, 0, c->stream>>>(a, RFBatch{});
+    kern<<<grid, 32 * wpb, dyn, c->stream>>>(a, RFBatch{});
     timer_stop(c, T_RF);
     PCHECK(c, cudaGetLastError());
     return PORTAL_OK;

@@ -42,10 +42,21 @@ const void *rf_batch_kernel_ptr(int nch, bool dust, int nlg, int max_lines) {
     return batch_kernel(nch, dust, nlg, max_lines);
 }
 
+// dynamic shared memory of a 256-thread block: the remainder channel's
+// (cell, line) table of each of its 8 warps, rows for the largest model
+static size_t batch_dyn_smem(int nch, bool dust, int max_lines) {
+    return chan_layout(nch, dust, max_lines).rt ? (size_t)8 * 32 * rem_row_stride(max_lines) * sizeof(float2) : 0;
+}
+
+// Also raises the kernel's dynamic shared-memory limit: called for every
+// candidate before the pass is captured.
 int rf_batch_blocks_per_sm(int nch, bool dust, int nlg, int max_lines, int *blocks) {
     const void *k = batch_kernel(nch, dust, nlg, max_lines);
+    const size_t dyn = batch_dyn_smem(nch, dust, max_lines);
     *blocks = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 256, 0);
+    if (dyn && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+        return PORTAL_ERR_CUDA;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 256, dyn);
     return e == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
 }
 
@@ -53,8 +64,9 @@ int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, int m
     const void *k = batch_kernel(nch, dust, nlg, max_lines);
     RFArgs a0{};
     RFBatch b = bw;
+    b.rem_lines = max_lines;
     void *args[] = {&a0, &b};
-    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(256), args, 0, s);
+    cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(256), args, batch_dyn_smem(nch, dust, max_lines), s);
     return e == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
 }
 

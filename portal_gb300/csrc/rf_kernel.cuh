@@ -18,8 +18,10 @@ constexpr float LOG2E_F = 1.4426950408889634f;
 // one ex2 of q'^2 with the sign folded into the instruction
 constexpr float SQL2E_F = 1.2011224087864498f;
 // line-centre optical depth (log2 units) below which every channel of a cell
-// takes the Taylor form: the switch OM_TAYLOR_X less 0.5 %, far more than the
-// few ulp by which ex2 may return a profile value above 1
+// takes the Taylor form: x = A g <= A with the profile g = ex2(-q'^2) <= 1
+// (ex2 of a non-positive argument does not exceed 1: checked over every float
+// of [-1/16, 0]), below the switch OM_TAYLOR_X of one_minus_exp with 0.5 % to
+// spare
 constexpr float OM_THIN_A = 0.0625f;
 // Face crossings closer than this (in units of r_max) are not taken.  The
 // reference uses 1e-10 (miscellaneous.f90:1048) against FP64 noise ~1e-16;
@@ -50,6 +52,11 @@ struct KahanF {
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+
+// Row stride (float2 per cell) of the remainder channel's (cell, line)
+// table: odd, so the staging lanes' 64-bit row stores of a half-warp fall in
+// distinct banks.
+__host__ __device__ __forceinline__ int rem_row_stride(int lines) { return lines | 1; }
 
 __device__ __forceinline__ float ex2(float x) {
     float y;
@@ -93,8 +100,6 @@ __global__ void k_line_table(int N, int L, double dxp, const LineConst *__restri
 template <int NLG, bool DUST>
 struct CellRec {
     float2 qd[32];       // profile argument at channel 0 and its step per channel, times sqrt(log2 e)
-    int cell[32];        // cell id and trace steps (the remainder channel's pass)
-    float fst[32];
     float2 AS[32][NLG];  // (A * steps, S) without dust, (A * steps, E * steps) with dust
     float Ad[32][DUST ? NLG : 1];   // dust tau per cell (dust only)
     float Jd[32][DUST ? NLG : 1];   // dust emissivity * steps (dust only)
@@ -243,7 +248,10 @@ __device__ __noinline__ double star_exit(double sexit, double px, double py, dou
 // (the reference's 2 nvel + 1 channels with nvel a multiple of 16): the
 // last channel (nv = +nvel) is integrated lanes-over-lines (lane = line,
 // L <= 32) in the first line-group pass instead of costing a whole slot of
-// 32 lanes for one channel.
+// 32 lanes for one channel.  Its transfer weights (1 - e^-tau, S) per (cell,
+// line) are formed by the staging lanes (lane = cell) into a per-warp table
+// of dynamic shared memory, rem_row_stride(L) float2 per cell; the
+// lanes-over-lines pass then only runs the recurrence.
 // BATCH: the work items are (model, node) pairs of many models (RFBatch);
 // each warp copies the argument block of its current model into shared
 // memory.  Otherwise the nodes of the one model a0.
@@ -259,8 +267,11 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
     using RB = typename std::conditional<BATCH, RayBatchStar, RayBatch>::type;
     __shared__ RB rbs[8];
     __shared__ RFArgs margs[BATCH ? 8 : 1];
+    extern __shared__ float2 rem_dyn[];
     CellRec<NLG, DUST> &R = recs[wib];
     RB &B = rbs[wib];
+    const int rem_ld = rem_row_stride(BATCH ? bw.rem_lines : a0.L);
+    float2 *const remS = rem_dyn + (size_t)wib * 32 * rem_ld;   // RT: this warp's (cell, line) table
 
     unsigned long long nseg = 0;
     int cur_model = -1;
@@ -464,20 +475,38 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
 #pragma unroll
                             for (int s2 = 0; s2 < NS; s2++) IV(s2, l) = bb;
                         }
+                        // walk records of the chunk (lane = cell), the next chunk's
+                        // loaded while this one is integrated
+                        int2 wcp = make_int2(0, 0);
+                        if (lane < min(32, Kr - 1)) wcp = wl[Kr - 1 - lane];
                         for (int hi = Kr - 1; hi >= 1; hi -= 32) {
                             const int nc = min(32, hi);
+                            const int2 wc = wcp;
+                            if (lane < min(32, hi - 32)) wcp = wl[hi - 32 - lane];
                             __syncwarp();
                             bool thin_cell = true;   // every line of the group thin in this cell
                             if (lane < nc) {
-                                const int2 wc = wl[hi - lane];
                                 const float4 cv = a.cellv[wc.x];
                                 const float vp = fmaf(cv.z, d4.z, fmaf(cv.y, d4.y, __fmul_rn(cv.x, d4.x)));
                                 const float ib = SQL2E_F * (1.f / cv.w);
-                                R.qd[lane] = make_float2((d4.w - vp) * ib, dqfac * ib);
+                                const float2 qdl = make_float2((d4.w - vp) * ib, dqfac * ib);
+                                R.qd[lane] = qdl;
                                 const float fst = (float)wc.y;
-                                if (RT) {
-                                    R.cell[lane] = wc.x;
-                                    R.fst[lane] = fst;
+                                if (RT && l0 == 0) {
+                                    // the remainder channel's transfer weight and source
+                                    // function of this cell for every line
+                                    const float q = fmaf(qdl.y, (float)(32 * NS - a.nvel), qdl.x);
+                                    const float gr = ex2(-(q * q));
+                                    const float2 *lr = reinterpret_cast<const float2 *>(a.ltab + (size_t)wc.x * a.L);
+                                    float2 *dst = remS + lane * rem_ld;
+#pragma unroll 4
+                                    for (int l = 0; l < a.L; l++) {
+                                        const float2 v = lr[2 * l];
+                                        const float As = (v.x > 0.f) ? v.x * fst * LOG2E_F : 0.f;
+                                        const float Ss = (v.x > 0.f) ? v.y : 0.f;
+                                        const float x = As * gr;
+                                        dst[l] = make_float2(one_minus_exp(x, ex2(-x)), Ss);
+                                    }
                                 }
                                 const float4 *lt = a.ltab + (size_t)wc.x * a.L + l0;
 #pragma unroll
@@ -510,10 +539,8 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 }
                             }
                             // A chunk whose every (cell, line) has a line-centre optical
-                            // depth below the Taylor switch takes the Taylor form of
-                            // 1 - e^-tau in every channel (x = A g <= A: the profile g
-                            // is at most 1, to within the ex2 rounding that the margin of
-                            // OM_THIN_A covers): the branch-free update would select
+                            // depth below OM_THIN_A takes the Taylor form of 1 - e^-tau
+                            // in every channel: the branch-free update would select
                             // exactly that value, so the chunk skips the ex2 and the
                             // select.  Decided per chunk of 32 cells, uniform over the
                             // warp.
@@ -521,29 +548,10 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             __syncwarp();
                             if (RT && l0 == 0 && lane < a.L) {
                                 // the remainder channel, lane = line, the same cells inward
-                                const float chr = (float)(32 * NS - a.nvel);
-                                auto step = [&](const float4 v, int u) {
-                                    const float2 qd = R.qd[u];
-                                    const float q = fmaf(qd.y, chr, qd.x);
-                                    const float gr = ex2(-(q * q));
-                                    const float As = (v.x > 0.f) ? v.x * R.fst[u] * LOG2E_F : 0.f;
-                                    const float Ss = (v.x > 0.f) ? v.y : 0.f;
-                                    const float x = As * gr;
-                                    Irem = fmaf(one_minus_exp(x, ex2(-x)), Ss - Irem, Irem);
-                                };
-                                // four cells' line-table reads are issued together
-                                int u = 0;
-                                for (; u + 4 <= nc; u += 4) {
-                                    const float4 v0 = a.ltab[(size_t)R.cell[u] * a.L + lane];
-                                    const float4 v1 = a.ltab[(size_t)R.cell[u + 1] * a.L + lane];
-                                    const float4 v2 = a.ltab[(size_t)R.cell[u + 2] * a.L + lane];
-                                    const float4 v3 = a.ltab[(size_t)R.cell[u + 3] * a.L + lane];
-                                    step(v0, u);
-                                    step(v1, u + 1);
-                                    step(v2, u + 2);
-                                    step(v3, u + 3);
+                                for (int u = 0; u < nc; u++) {
+                                    const float2 r = remS[u * rem_ld + lane];
+                                    Irem = fmaf(r.x, r.y - Irem, Irem);
                                 }
-                                for (; u < nc; u++) step(a.ltab[(size_t)R.cell[u] * a.L + lane], u);
                             }
                             // one cell's update of the group's lines in every channel slot
                             auto cell_step = [&](auto thin_tag, int u) {
@@ -620,9 +628,16 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                     }
                                 }
                             };
+                            // two cells per iteration: the second cell's profile and
+                            // transfer weights do not depend on the first's update and
+                            // fill its dependency stalls (2.10e9 -> 2.22e9 segments/s on
+                            // the benchmark sphere with the walk-record prefetch above;
+                            // 4 cells per iteration: 2.21e9)
                             if (thin) {
+#pragma unroll 2
                                 for (int u = 0; u < nc; u++) cell_step(std::true_type{}, u);
                             } else {
+#pragma unroll 2
                                 for (int u = 0; u < nc; u++) cell_step(std::false_type{}, u);
                             }
                         }
