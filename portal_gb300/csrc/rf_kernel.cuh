@@ -58,6 +58,31 @@ struct KahanF {
 // distinct banks.
 __host__ __device__ __forceinline__ int rem_row_stride(int lines) { return lines | 1; }
 
+// Line groups up to these widths run the cell loop two cells per iteration,
+// and instantiate it for every count of Taylor-only lines; wider groups one
+// cell per iteration, all or none of the lines Taylor-only (the larger
+// bodies cost more in instruction fetch than they gain).
+constexpr int UNROLL_MAX_NLG = 4;
+constexpr int SUFFIX_MAX_NLG = 3;
+
+// f(std::integral_constant<int, k>) for the run-time count k in [0, NLG] of
+// Taylor-only lines: every k for groups up to SUFFIX_MAX_NLG lines, 0 or NLG
+// for wider ones, 0 alone with dust
+template <int NLG, bool DUST, int K = 0, typename F>
+__device__ __forceinline__ void with_thin_lines(int k, F &f) {
+    if constexpr (DUST) {
+        f(std::integral_constant<int, 0>{});
+    } else if constexpr (NLG > SUFFIX_MAX_NLG) {
+        if (k == NLG) f(std::integral_constant<int, NLG>{});
+        else f(std::integral_constant<int, 0>{});
+    } else if constexpr (K < NLG) {
+        if (k == K) f(std::integral_constant<int, K>{});
+        else with_thin_lines<NLG, DUST, K + 1>(k, f);
+    } else {
+        f(std::integral_constant<int, NLG>{});
+    }
+}
+
 __device__ __forceinline__ float ex2(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -484,7 +509,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             const int2 wc = wcp;
                             if (lane < min(32, hi - 32)) wcp = wl[hi - 32 - lane];
                             __syncwarp();
-                            bool thin_cell = true;   // every line of the group thin in this cell
+                            unsigned thin_m = (1u << NLG) - 1u;   // the group's lines thin in this cell
                             if (lane < nc) {
                                 const float4 cv = a.cellv[wc.x];
                                 const float vp = fmaf(cv.z, d4.z, fmaf(cv.y, d4.y, __fmul_rn(cv.x, d4.x)));
@@ -534,17 +559,24 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                             }
                                         }
                                         R.AS[lane][l] = make_float2(As, Ss);
-                                        thin_cell = thin_cell && (As < OM_THIN_A);
+                                        if (!(As < OM_THIN_A)) thin_m &= ~(1u << l);
                                     }
                                 }
                             }
-                            // A chunk whose every (cell, line) has a line-centre optical
-                            // depth below OM_THIN_A takes the Taylor form of 1 - e^-tau
-                            // in every channel: the branch-free update would select
-                            // exactly that value, so the chunk skips the ex2 and the
+                            // A line whose line-centre optical depth is below OM_THIN_A
+                            // in every cell of the chunk takes the Taylor form of
+                            // 1 - e^-tau in every channel: the branch-free update would
+                            // select exactly that value, so it skips the ex2 and the
                             // select.  Decided per chunk of 32 cells, uniform over the
-                            // warp.
-                            const bool thin = !DUST && __all_sync(FULL, thin_cell);
+                            // warp, for the group's last tk lines (a rotor's higher lines
+                            // are the thinner ones); the cell loop is instantiated per tk
+                            // (groups of at most 5 lines; wider groups: none or all).
+                            int tk = 0;
+                            if (!DUST) {
+                                const unsigned tm = __reduce_and_sync(FULL, thin_m);
+                                tk = __clz(~(tm << (32 - NLG)));   // trailing run of thin lines
+                                if (NLG > SUFFIX_MAX_NLG && tk != NLG) tk = 0;
+                            }
                             __syncwarp();
                             if (RT && l0 == 0 && lane < a.L) {
                                 // the remainder channel, lane = line, the same cells inward
@@ -554,8 +586,8 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                 }
                             }
                             // one cell's update of the group's lines in every channel slot
-                            auto cell_step = [&](auto thin_tag, int u) {
-                                constexpr bool THIN = decltype(thin_tag)::value;
+                            auto cell_step = [&](auto tk_tag, int u) {
+                                constexpr int TK = decltype(tk_tag)::value;   // the last TK lines: Taylor only
                                 const float2 qd = R.qd[u];
                                 const float q0 = qd.x, dq = qd.y;
                                 // Gaussian profile of the cell at the lane's channels,
@@ -606,7 +638,7 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                                         // chains interleave: a warp-uniform branch per cell to
                                         // a Taylor-only path measured 24 % slower in spite of
                                         // skipping the ex2 (1.45e9 against 1.90e9 segments/s);
-                                        // decided once per chunk of 32 cells (THIN) it gains
+                                        // decided once per chunk of 32 cells (TK) it gains
                                         // (1.96e9 -> 2.03e9).  Channel-slot pairs go through
                                         // the packed FP32x2 pipe (one issue slot for two
                                         // updates).
@@ -614,14 +646,14 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
 #pragma unroll
                                         for (int s2 = 0; s2 + 1 < NS; s2 += 2) {
                                             const float2 x = __fmul2_rn(A2, make_float2(g[s2], g[s2 + 1]));
-                                            const float2 om =
-                                                THIN ? om_taylor2(x) : one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
+                                            const float2 om = (l >= NLG - TK) ? om_taylor2(x)
+                                                                              : one_minus_exp2(x, ex2(-x.x), ex2(-x.y));
                                             float2 &Ip = I2[s2 >> 1][l];
                                             Ip = __ffma2_rn(om, __ffma2_rn(Ip, make_float2(-1.f, -1.f), S2), Ip);
                                         }
                                         if (NS & 1) {
                                             const float x = Au * g[NS - 1];
-                                            const float om = THIN ? om_taylor(x) : one_minus_exp(x, ex2(-x));
+                                            const float om = (l >= NLG - TK) ? om_taylor(x) : one_minus_exp(x, ex2(-x));
                                             float &Is = I2[NS >> 1][l].x;
                                             Is = fmaf(om, Su - Is, Is);
                                         }
@@ -633,13 +665,16 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                             // fill its dependency stalls (2.10e9 -> 2.22e9 segments/s on
                             // the benchmark sphere with the walk-record prefetch above;
                             // 4 cells per iteration: 2.21e9)
-                            if (thin) {
+                            auto run = [&](auto tk_tag) {
+                                if constexpr (NLG <= UNROLL_MAX_NLG) {
 #pragma unroll 2
-                                for (int u = 0; u < nc; u++) cell_step(std::true_type{}, u);
-                            } else {
-#pragma unroll 2
-                                for (int u = 0; u < nc; u++) cell_step(std::false_type{}, u);
-                            }
+                                    for (int u = 0; u < nc; u++) cell_step(tk_tag, u);
+                                } else {
+#pragma unroll 1
+                                    for (int u = 0; u < nc; u++) cell_step(tk_tag, u);
+                                }
+                            };
+                            with_thin_lines<NLG, DUST>(tk, run);
                         }
                         // central cell (inverse_rt.f90:320-339): no gate, profile at
                         // the node's own b, then the weighted channel sum
