@@ -40,6 +40,7 @@
 // the extra_info rates leave out as the reference's C_mat does.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 
 #include "internal.cuh"
@@ -128,6 +129,67 @@ __device__ void warp_lu_solve(int n, const T *M, const int *piv, V *b, int lane)
     }
 }
 
+// The same factorisation by a team of TW warps (TW = 1: warp_lu itself):
+// the pivot search over the team (warp argmax, then across the warps through
+// red_v / red_i, the first row of largest modulus as before), the row swap
+// and column scaling strided over the team, the trailing update over (row,
+// column) pairs.  Every element sees the operations of warp_lu in the same
+// order, so the factors are the same.
+template <typename T, int TW>
+__device__ bool team_lu(int n, T *M, int *piv, int tid, double *red_v, int *red_i) {
+    if constexpr (TW == 1) {
+        return warp_lu<T>(n, M, piv, tid);
+    } else {
+        constexpr int TS = 32 * TW;
+        const int lane = tid & 31, w = tid >> 5;
+        bool ok = true;
+        for (int k = 0; k < n; k++) {
+            T best = (T)-1;
+            int bi = n;
+            for (int i = k + tid; i < n; i += TS) {
+                T v = fabs(M[i + (size_t)n * k]);
+                if (v > best) { best = v; bi = i; }
+            }
+            for (int o = 16; o >= 1; o >>= 1) {
+                T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) { red_v[w] = (double)best; red_i[w] = bi; }
+            __syncthreads();
+            best = (T)red_v[0];
+            bi = red_i[0];
+            for (int q = 1; q < TW; q++) {
+                const T ob = (T)red_v[q];
+                const int oi = red_i[q];
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (bi >= n) bi = k;
+            if (tid == 0) piv[k] = bi;
+            if (!(best > (T)0)) { ok = false; }
+            if (bi != k)
+                for (int j = tid; j < n; j += TS) {
+                    T t = M[k + (size_t)n * j];
+                    M[k + (size_t)n * j] = M[bi + (size_t)n * j];
+                    M[bi + (size_t)n * j] = t;
+                }
+            __syncthreads();   // also orders this step's reads of red_v / red_i before the next step's writes
+            const T d = M[k + (size_t)n * k];
+            const T r = (d != (T)0) ? (T)1 / d : (T)0;
+            for (int i = k + 1 + tid; i < n; i += TS) M[i + (size_t)n * k] *= r;
+            __syncthreads();
+            const int m = n - k - 1;
+            for (int idx = tid; idx < m * m; idx += TS) {
+                const int i = k + 1 + idx % m, j = k + 1 + idx / m;
+                const T lik = M[i + (size_t)n * k];
+                if (lik != (T)0) M[i + (size_t)n * j] -= lik * M[k + (size_t)n * j];
+            }
+            __syncthreads();
+        }
+        return ok;
+    }
+}
+
 // Dynamic shared memory per warp:
 //   feat [n_feat] double | x, r [n] double | LU32 [n*n] float | d32 [n] float
 //   | scale [n] float | piv [n] int
@@ -145,32 +207,60 @@ __host__ __device__ inline size_t se_warp_bytes(int n, int n_feat) {
     return (b + 15) & ~(size_t)15;
 }
 
-// One warp per node.  BATCH: the work items are (model, node) pairs of many
-// models (SEBatch); each warp copies its current model's argument block into
-// shared memory, and the dynamic shared memory per warp fits the largest
-// model.  Otherwise the nodes of the one model a0.
-template <bool BATCH>
-__global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
+// A team of TW warps per node.  TW = 1: every warp of the block is a team
+// (the systems of up to ~50 unknowns); TW > 1: the block is one team, whose
+// warps share the factorisation's pivot search, row operations and trailing
+// updates, the FP64 residuals, the assembly and the packing (larger
+// systems, whose one-warp solve is latency-bound at a few warps per SM).
+// The triangular solves of the refinement run on the team's first warp.
+// BATCH (TW = 1 only): the work items are (model, node) pairs of many models
+// (SEBatch); each warp copies its current model's argument block into shared
+// memory, and the dynamic shared memory per warp fits the largest model.
+// Otherwise the nodes of the one model a0.
+template <int TW, bool BATCH>
+__global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW) k_solve_se(SEArgs a0, SEBatch bw) {
+    static_assert(TW == 1 || !BATCH, "teams of several warps run the single-model kernel");
+    constexpr int TS = 32 * TW;   // threads per team
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ SEArgs margs[BATCH ? 8 : 1];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ double red_v[TW];  // cross-warp reductions of a team
+    __shared__ int red_i[TW];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int tid = (TW == 1) ? lane : (int)threadIdx.x;    // thread within the team
+    const int teams = (TW == 1) ? (int)(blockDim.x >> 5) : 1;
+    const int team = (TW == 1) ? wib : 0;
+    auto tsync = [&]() {
+        if constexpr (TW == 1) __syncwarp();
+        else __syncthreads();
+    };
+    auto team_max = [&](double v) {
+        v = warp_max(v);
+        if constexpr (TW > 1) {
+            if (lane == 0) red_v[wib] = v;
+            __syncthreads();
+            v = red_v[0];
+            for (int q = 1; q < TW; q++) v = fmax(v, red_v[q]);
+            __syncthreads();
+        }
+        return v;
+    };
     const long long n_items = BATCH ? bw.n_items : (long long)a0.bulk;
     const size_t wbytes = BATCH ? bw.warp_bytes : se_warp_bytes(a0.c_dim, a0.n_feat);
-    unsigned char *base = smem + wbytes * wib;
+    unsigned char *base = smem + wbytes * team;
     double *const A64 = (BATCH ? bw.a64 : a0.a64) +
-                        (size_t)((long long)blockIdx.x * nw + wib) * (BATCH ? bw.a64_stride : a0.a64_stride);
+                        (size_t)((long long)blockIdx.x * teams + team) * (BATCH ? bw.a64_stride : a0.a64_stride);
     int cur_model = -1;
 
-    for (long long item = (long long)blockIdx.x * nw + wib; item < n_items; item += (long long)gridDim.x * nw) {
+    for (long long item = (long long)blockIdx.x * teams + team; item < n_items; item += (long long)gridDim.x * teams) {
         int node;
         if (BATCH) {
             const int2 wi = bw.items[item];
             if (wi.x != cur_model) {
-                __syncwarp();
+                tsync();
                 const int *src = reinterpret_cast<const int *>(bw.models + wi.x);
                 int *dst = reinterpret_cast<int *>(&margs[wib]);
-                for (int k = lane; k < (int)(sizeof(SEArgs) / sizeof(int)); k += 32) dst[k] = src[k];
-                __syncwarp();
+                for (int k = tid; k < (int)(sizeof(SEArgs) / sizeof(int)); k += TS) dst[k] = src[k];
+                tsync();
                 cur_model = wi.x;
             }
             node = wi.y;
@@ -189,7 +279,7 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
         if (!(a.ab[node] > 0.0)) continue;  // main_para.f90:213 (pops stay 0)
         const double T = a.tkin[node], nH2 = a.h2[node];
         // ---- features (make_AC miscellaneous.f90:331-390) ----
-        for (int t = lane; t < a.n_trans; t += 32) {
+        for (int t = tid; t < a.n_trans; t += TS) {
             const int rr = a.tr_rad[t], cc = a.tr_col[t];
             const double B21 = a.tr_B21[t];
             double j0 = 0.0, j2 = 0.0, je = 0.0, ls = 0.0, C21 = 0.0;
@@ -233,7 +323,7 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
             // leaves D0 unset (0 here)
             const int nT = a.c_temp;
             const double *ct = a.col_temps;
-            for (int d = lane; d < a.n_dep; d += 32) {
+            for (int d = tid; d < a.n_dep; d += TS) {
                 const double *tab = a.dep_tab + (size_t)nT * d;
                 double v = 0.0;
                 if (T <= ct[0]) v = tab[0];
@@ -246,59 +336,60 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
                 if (a.depol == 2) feat[NF * (size_t)a.n_trans + a.n_dep + d] = v;
             }
         }
-        for (int i = lane; i < n * n; i += 32) A64[i] = 0.0;
-        __syncwarp();
+        for (int i = tid; i < n * n; i += TS) A64[i] = 0.0;
+        tsync();
         // ---- assembly (setup_stateq) ----
-        for (int e = lane; e < a.nent; e += 32) {
+        for (int e = tid; e < a.nent; e += TS) {
             double v = 0.0;
             for (int q = a.ent_off[e]; q < a.ent_off[e + 1]; q++) v += a.term_c[q] * feat[a.term_f[q]];
             A64[a.ent_pos[e]] = v;
         }
-        __syncwarp();
+        tsync();
         // ---- normalisation row (em_coefs.f90:158-164) ----
-        for (int j = lane; j < n; j += 32) A64[(size_t)n * j] = 0.0;
-        __syncwarp();
-        if (lane == 0)
+        for (int j = tid; j < n; j += TS) A64[(size_t)n * j] = 0.0;
+        tsync();
+        if (tid == 0)
             for (int i = 0; i < a.nlev; i++) A64[(size_t)n * a.norm_col[i]] = a.norm_val[i];
-        __syncwarp();
+        tsync();
         // ---- FP32 LU of the row-scaled matrix ----
-        for (int i = lane; i < n; i += 32) {
+        for (int i = tid; i < n; i += TS) {
             double m = 0.0;
             for (int j = 0; j < n; j++) m = fmax(m, fabs(A64[i + (size_t)n * j]));
             scl[i] = (m > 0.0) ? (float)(1.0 / m) : 1.f;
         }
-        __syncwarp();
-        for (int idx = lane; idx < n * n; idx += 32) {
+        tsync();
+        for (int idx = tid; idx < n * n; idx += TS) {
             const int i = idx % n;
             LU[idx] = (float)(A64[idx] * (double)scl[i]);
         }
-        __syncwarp();
+        tsync();
         int st = 0;
-        bool ok = warp_lu<float>(n, LU, piv, lane);
+        bool ok = team_lu<float, TW>(n, LU, piv, tid, red_v, red_i);
         bool conv = false;
         if (ok) {
-            for (int i = lane; i < n; i += 32) x[i] = 0.0;
-            __syncwarp();
+            for (int i = tid; i < n; i += TS) x[i] = 0.0;
+            tsync();
             double xmax = 0.0, dprev = 1e300;
             for (int it = 0; it < 10; it++) {
                 // r = e_1 - A x (FP64)
-                for (int i = lane; i < n; i += 32) {
+                for (int i = tid; i < n; i += TS) {
                     double s = (i == 0) ? 1.0 : 0.0;
                     for (int j = 0; j < n; j++) s -= A64[i + (size_t)n * j] * x[j];
                     d32[i] = (float)(s * (double)scl[i]);
                 }
-                __syncwarp();
-                warp_lu_solve<float, float>(n, LU, piv, d32, lane);
+                tsync();
+                if (TW == 1 || wib == 0) warp_lu_solve<float, float>(n, LU, piv, d32, lane);
+                tsync();
                 double dm = 0.0;
-                for (int i = lane; i < n; i += 32) {
+                for (int i = tid; i < n; i += TS) {
                     x[i] += (double)d32[i];
                     dm = fmax(dm, fabs((double)d32[i]));
                 }
-                __syncwarp();
+                tsync();
                 double xm = 0.0;
-                for (int i = lane; i < n; i += 32) xm = fmax(xm, fabs(x[i]));
-                dm = warp_max(dm);
-                xmax = warp_max(xm);
+                for (int i = tid; i < n; i += TS) xm = fmax(xm, fabs(x[i]));
+                dm = team_max(dm);
+                xmax = team_max(xm);
                 if (!(dm == dm) || !(xmax == xmax)) break;  // NaN
                 // converged: the correction is at the level FP64 residuals can
                 // resolve (~cond(SA) * eps), or it stopped shrinking there
@@ -312,30 +403,31 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
             // is not available; re-assemble into A64 in place)
             double *M = A64;
             st |= ok ? PORTAL_NODE_REFINE : 0;
-            bool ok64 = warp_lu<double>(n, M, piv, lane);
+            bool ok64 = team_lu<double, TW>(n, M, piv, tid, red_v, red_i);
             if (!ok64) {
                 st |= PORTAL_NODE_SINGULAR;
             } else {
-                for (int i = lane; i < n; i += 32) x[i] = (i == 0) ? 1.0 : 0.0;
-                __syncwarp();
-                warp_lu_solve<double, double>(n, M, piv, x, lane);
+                for (int i = tid; i < n; i += TS) x[i] = (i == 0) ? 1.0 : 0.0;
+                tsync();
+                if (TW == 1 || wib == 0) warp_lu_solve<double, double>(n, M, piv, x, lane);
+                tsync();
                 st |= PORTAL_NODE_REFINE;
             }
         }
-        __syncwarp();
+        tsync();
         // ---- packing (main_sub.f90:112-137) ----
-        for (int c2 = lane; c2 < 2 * a.nlev; c2 += 32) {
+        for (int c2 = tid; c2 < 2 * a.nlev; c2 += TS) {
             const int p = a.pack[c2];
             double v = (p >= 0 && !(st & PORTAL_NODE_SINGULAR)) ? x[p] : 0.0;
             if (st & PORTAL_NODE_SINGULAR) v = 0.0;
             a.pops[(size_t)node + (size_t)a.N * c2] = v;
         }
-        __syncwarp();
-        if (lane < a.nlev) {
-            const double v0 = a.pops[(size_t)node + (size_t)a.N * (2 * lane)];
+        tsync();
+        for (int l = tid; l < a.nlev; l += TS) {
+            const double v0 = a.pops[(size_t)node + (size_t)a.N * (2 * l)];
             if (v0 != v0) {
-                a.pops[(size_t)node + (size_t)a.N * (2 * lane)] = 0.0;
-                a.pops[(size_t)node + (size_t)a.N * (2 * lane + 1)] = 0.0;
+                a.pops[(size_t)node + (size_t)a.N * (2 * l)] = 0.0;
+                a.pops[(size_t)node + (size_t)a.N * (2 * l + 1)] = 0.0;
             }
         }
         if (a.rates) {
@@ -346,7 +438,7 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
             // field's values (f0, f2) stand for f5, f6.  Row by row in
             // ascending column order, as the reference sums.
             for (int k = 0; k < 3; k++) {
-                for (int i = lane; i < n; i += 32) {
+                for (int i = tid; i < n; i += TS) {
                     double acc = 0.0;
                     if (!(st & PORTAL_NODE_SINGULAR))
                         for (int q = a.row_off[i]; q < a.row_off[i + 1]; q++) {
@@ -370,11 +462,11 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
                         }
                     r[i] = acc;
                 }
-                __syncwarp();
+                tsync();
                 // packing as the populations (main_sub.f90:116-135): K = 2
                 // components of J = 0 levels are 0; a NaN population zeroes the
                 // K = 2 rate entry (twice, as in the reference)
-                for (int c2 = lane; c2 < 2 * a.nlev; c2 += 32) {
+                for (int c2 = tid; c2 < 2 * a.nlev; c2 += TS) {
                     const int pidx = a.pack[c2];
                     double v = (pidx >= 0) ? r[pidx] : 0.0;
                     if (c2 & 1) {
@@ -383,18 +475,18 @@ __global__ void __launch_bounds__(256, 3) k_solve_se(SEArgs a0, SEBatch bw) {
                     }
                     a.rates[(size_t)node + (size_t)a.N * (k + 3 * (size_t)c2)] = v;
                 }
-                __syncwarp();
+                tsync();
             }
         }
         if (a.jj20)
-            for (int l = lane; l < a.L; l += 32)
+            for (int l = tid; l < a.L; l += TS)
                 a.jj20[(size_t)node + (size_t)a.N * l] =
                     a.J2[(size_t)node * a.L + l] / a.J0[(size_t)node * a.L + l];
-        if (lane == 0) {
+        if (tid == 0) {
             a.status[node] |= st;
             if (st & PORTAL_NODE_SINGULAR) atomicAdd(a.nfail, 1);
         }
-        __syncwarp();
+        tsync();
     }
 }
 
@@ -720,10 +812,10 @@ size_t se_matrix_doubles(const portal_ctx *c) { return (size_t)c->c_dim * c->c_d
 int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) {
     const size_t smem = warp_bytes * warps_per_block;
     *blocks = 0;
-    if (cudaFuncSetAttribute(k_solve_se<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    if (cudaFuncSetAttribute(k_solve_se<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return PORTAL_ERR_CUDA;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solve_se<true>, 32 * warps_per_block, smem) ==
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solve_se<1, true>, 32 * warps_per_block, smem) ==
                    cudaSuccess
                ? PORTAL_OK
                : PORTAL_ERR_CUDA;
@@ -733,8 +825,41 @@ int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) 
 // se_batch_blocks_per_sm for at least this many warps)
 int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw) {
     const size_t smem = bw.warp_bytes * warps_per_block;
-    k_solve_se<true><<<grid, 32 * warps_per_block, smem, s>>>(SEArgs{}, bw);
+    k_solve_se<1, true><<<grid, 32 * warps_per_block, smem, s>>>(SEArgs{}, bw);
     return cudaGetLastError() == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
+}
+
+// Warps per node: one up to SE_TEAM_MIN_N unknowns, a team of four above
+// (PORTAL_SE_TEAM=1|2|4 overrides).
+constexpr int SE_TEAM_MIN_N = 48;
+inline int se_team_warps(int n) {
+    const char *e = getenv("PORTAL_SE_TEAM");
+    if (e) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2 || v == 4) return v;
+    }
+    return n >= SE_TEAM_MIN_N ? 4 : 1;
+}
+
+// TW = 1: blocks of up to 8 independent warps; TW > 1: one team per block.
+// One FP64 matrix slot per team of the grid.
+template <int TW>
+int launch_se(portal_ctx *c, SEArgs &a, size_t wb) {
+    auto kern = k_solve_se<TW, false>;
+    const int teams = (TW == 1) ? (int)std::min<size_t>(8, (200 * 1024) / wb) : 1;
+    const size_t smem = wb * teams;
+    PCHECK(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 32 * TW * teams, smem));
+    const int grid = c->sm_count * std::max(1, nb);
+    if (c->se_a64.reserve((size_t)grid * teams * a.a64_stride))
+        return set_err(c, PORTAL_ERR_NOMEM, "SE matrix scratch");
+    a.a64 = c->se_a64.p;
+    timer_start(c, T_SE);
+    kern<<<grid, 32 * TW * teams, smem, c->stream>>>(a, SEBatch{});
+    timer_stop(c, T_SE);
+    PCHECK(c, cudaGetLastError());
+    return PORTAL_OK;
 }
 
 int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates) {
@@ -748,21 +873,14 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates) {
         PCHECK(c, cudaMemsetAsync(c->rates.p, 0, nr * sizeof(double), c->stream));
         a.rates = c->rates.p;
     }
-    const int wpb = (int)std::min<size_t>(8, (200 * 1024) / wb);
-    const size_t smem = wb * wpb;
-    PCHECK(c, cudaFuncSetAttribute(k_solve_se<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if ((rc = se_pass(c, c->stream))) return rc;
-    int nb = 0;
-    PCHECK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_solve_se<false>, 32 * wpb, smem));
-    int grid = c->sm_count * std::max(1, nb);
     a.a64_stride = (size_t)c->c_dim * c->c_dim;
-    if (c->se_a64.reserve((size_t)grid * wpb * a.a64_stride))
-        return set_err(c, PORTAL_ERR_NOMEM, "SE matrix scratch");
-    a.a64 = c->se_a64.p;
-    timer_start(c, T_SE);
-    k_solve_se<false><<<grid, 32 * wpb, smem, c->stream>>>(a, SEBatch{});
-    timer_stop(c, T_SE);
-    PCHECK(c, cudaGetLastError());
+    switch (se_team_warps(c->c_dim)) {
+    case 2: rc = launch_se<2>(c, a, wb); break;
+    case 4: rc = launch_se<4>(c, a, wb); break;
+    default: rc = launch_se<1>(c, a, wb); break;
+    }
+    if (rc) return rc;
     int nf = 0;
     PCHECK(c, cudaMemcpyAsync(&nf, c->counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     PCHECK(c, cudaStreamSynchronize(c->stream));

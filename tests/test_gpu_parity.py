@@ -197,6 +197,38 @@ def test_depolarising_collisions_against_oracle(ctx, mode):
     np.testing.assert_allclose(back[:128], plain[:128], rtol=1e-10, atol=1e-14 * np.abs(plain).max())
 
 
+@pytest.mark.parametrize("team", [2, 4])
+def test_se_team_of_warps_matches_one_warp_and_oracle(ctx, monkeypatch, team):
+    """74 x 74 systems (20-level rotor, kmax 6) solved by a team of warps per
+    node (the default above 48 unknowns) and by one warp: the factorisation
+    sees the same operations per element, so populations, alignment, rates
+    and status are identical; against the oracle (get_rhovec,
+    em_coefs.f90:115-201) on 64 nodes to 1e-10 from the same J (the local
+    Planck field with a small anisotropy)."""
+    import dataclasses
+    import oracle
+    import portal_gb300 as pg
+    from portal_gb300 import synth
+    cloud, mol, rc = _small(2048, nlev=20, t_law="loglinear")
+    frac = synth.lte_fractions(mol, np.maximum(cloud.t_kin, 1.0))
+    cloud = dataclasses.replace(cloud, lev_p=np.ascontiguousarray(frac * (cloud.ab_all * cloud.h2_dens)[:, None]))
+    nu = np.asarray(mol.nu)
+    J0 = 1.4744995e-50 * nu ** 3 / np.expm1(4.79924e-11 * nu / np.maximum(cloud.t_kin, 1.0)[:, None])
+    J2 = 1e-3 * J0 * np.cos(np.arange(cloud.node_num))[:, None]
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    monkeypatch.setenv("PORTAL_SE_TEAM", "1")
+    p1, s1, r1 = ctx.solve_se(rc.kmax, J0, J2, rates=True)
+    monkeypatch.setenv("PORTAL_SE_TEAM", str(team))
+    pt, st, rt = ctx.solve_se(rc.kmax, J0, J2, rates=True)
+    assert np.array_equal(p1, pt) and np.array_equal(s1, st) and np.array_equal(r1, rt)
+    assert not (st & pg.NODE_SINGULAR).any()
+    opp = oracle.OracleProblem(cloud, mol).solve_se(rc.kmax, J0, J2, 1, 64)[0]
+    scale = np.abs(opp[:64, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pt[:64, 0::2] - opp[:64, 0::2]) / scale).max() < 1e-10
+    assert (np.abs(pt[:64, 1::2] - opp[:64, 1::2]) / scale).max() < 1e-10
+
+
 def test_n_depth_overflow_is_reported(ctx):
     import portal_gb300 as pg
     cloud, mol, rc = _small()
