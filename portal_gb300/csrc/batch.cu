@@ -225,17 +225,17 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
         if (wb * w <= 200 * 1024) sec.push_back(w);
     if (sec.empty()) return bfail(b, PORTAL_ERR_ARG, "SE system too large for shared memory");
     int dummy = 0;
-    if (se_batch_blocks_per_sm(sec.back(), wb, &dummy))  // raises the smem limit to the largest candidate
+    if (se_batch_blocks_per_sm(sec.back(), wb, b->se_a64_stride, &dummy))  // raises the smem limit to the largest candidate
         return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
     // FP64 matrix slots for the largest SE grid among the candidates
     {
         size_t most = 0;
         for (int w : sec) {
             int bps = 0;
-            if (se_batch_blocks_per_sm(w, wb, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
+            if (se_batch_blocks_per_sm(w, wb, b->se_a64_stride, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
             most = std::max(most, (size_t)std::max(1, bps) * b->sm_count * w);
         }
-        se_batch_blocks_per_sm(sec.back(), wb, &dummy);
+        se_batch_blocks_per_sm(sec.back(), wb, b->se_a64_stride, &dummy);
         if (b->se_a64.reserve(most * b->se_a64_stride)) return bfail(b, PORTAL_ERR_NOMEM, "SE matrix scratch");
     }
     // walk scratch for the largest grid
@@ -261,7 +261,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
         best = 1e300;
         for (int w : sec) {
             int bps = 0;
-            if (se_batch_blocks_per_sm(w, wb, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
+            if (se_batch_blocks_per_sm(w, wb, b->se_a64_stride, &bps)) return bfail(b, PORTAL_ERR_CUDA, "SE occupancy query");
             bps = std::max(1, bps);
             SEBatch sb{b->d_se.p, b->sample.p, b->n_sample, wb, b->se_a64.p, b->se_a64_stride};
             double ms = 0.0;
@@ -270,7 +270,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
             b->tune.insert(b->tune.end(), {(double)w, (double)bps, ms});
             if (ms < best) { best = ms; b->se_warps = w; b->se_bps = bps; }
         }
-        se_batch_blocks_per_sm(sec.back(), wb, &dummy);
+        se_batch_blocks_per_sm(sec.back(), wb, b->se_a64_stride, &dummy);
     } else {
         b->nlg = 5;
         b->rf_bps = 1;
@@ -278,7 +278,7 @@ extern "C" int portal_batch_prepare(portal_batch *b, int nth, int nph, int nvel,
             if (c.nlg == 5) b->rf_bps = std::max(b->rf_bps, c.bps);
         b->se_warps = sec.back();
         int bps = 0;
-        se_batch_blocks_per_sm(b->se_warps, wb, &bps);
+        se_batch_blocks_per_sm(b->se_warps, wb, b->se_a64_stride, &bps);
         b->se_bps = std::max(1, bps);
     }
 

@@ -117,6 +117,7 @@ struct portal_ctx {
     portal::DevBuf<double> rates;     // (N,3,2*nlev)
     portal::DevBuf<double> jj20;      // (N, r_num)
     int se_ni = 0;
+    int se_nasm = 0;                  // entries with terms (the assembly's list)
     size_t se_offs[20] = {};
 
     // ---- timing ----

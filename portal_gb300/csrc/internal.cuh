@@ -68,6 +68,8 @@ struct SEArgs {
     const int *__restrict__ pack;       // (2 nlev) rho index or -1
     const int *__restrict__ row_off;    // (c_dim + 1) entries of each matrix row,
     const int *__restrict__ row_ent;    // ascending column (the rates' summation order)
+    const int4 *__restrict__ asm_rec;   // the entries with terms: (pos, first term, end, 0)
+    int n_asm;
     double *pops;                       // (N, 2 nlev) column-major
     double *jj20;                       // (N, L) or null
     double *rates;                      // (N, 3, 2 nlev) column-major or null
@@ -108,7 +110,7 @@ int rf_batch_launch(cudaStream_t s, int grid, int nch, bool dust, int nlg, int m
 int se_prepare(portal_ctx *c, int kmax, SEArgs *a, size_t *warp_bytes);
 int se_pass(portal_ctx *c, cudaStream_t s);
 int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw);
-int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks);
+int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, size_t a64_stride, int *blocks);
 size_t se_matrix_doubles(const portal_ctx *c);  // c_dim^2 of the prepared SE program
 
 }  // namespace portal

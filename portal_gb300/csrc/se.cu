@@ -57,10 +57,6 @@ namespace {
 constexpr double A_TO_B = 6.781962e49;  // pop_eqs.f90:419
 constexpr double HK = 4.79924e-11;      // pop_eqs.f90:535
 
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o >= 1; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -108,84 +104,129 @@ __device__ bool warp_lu(int n, T *M, int *piv, int lane) {
     return ok;
 }
 
-// Solve (LU) x = P b in place in b (length n, shared memory).
-template <typename T, typename V>
+// Solve (LU) x = P b in place in b (length n, shared memory), one warp.
+// The pivots are applied in shared memory; then lane l holds b[l + 32 m] in
+// register br[m], and step k broadcasts b[k] = br[k / 32] of lane k % 32
+// with a shuffle.  The steps run in blocks of 32 under an unrolled loop over
+// the register index, so every register is named at compile time (a
+// run-time index would put br in local memory).  The per-element operations
+// are those of the plain forward and back substitution (b[i] -= M[i,k] b[k];
+// b[k] /= M[k,k]).  MR rows per lane: n <= 32 MR.
+template <typename T, typename V, int MR>
 __device__ void warp_lu_solve(int n, const T *M, const int *piv, V *b, int lane) {
     if (lane == 0)
         for (int k = 0; k < n; k++)
             if (piv[k] != k) { V t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
     __syncwarp();
-    for (int k = 0; k < n; k++) {
-        const V bk = b[k];
-        for (int i = k + 1 + lane; i < n; i += 32) b[i] -= (V)M[i + (size_t)n * k] * bk;
-        __syncwarp();
+    V br[MR];
+#pragma unroll
+    for (int m = 0; m < MR; m++) br[m] = (lane + 32 * m < n) ? b[lane + 32 * m] : (V)0;
+#pragma unroll
+    for (int kb = 0; kb < MR; kb++) {
+        if (32 * kb >= n) break;
+        const int kend = min(32, n - 32 * kb);
+        for (int kk = 0; kk < kend; kk++) {
+            const int k = 32 * kb + kk;
+            const V bk = __shfl_sync(0xffffffffu, br[kb], kk);
+#pragma unroll
+            for (int m = kb; m < MR; m++) {
+                const int i = lane + 32 * m;
+                if (i > k && i < n) br[m] -= (V)M[i + (size_t)n * k] * bk;
+            }
+        }
     }
-    for (int k = n - 1; k >= 0; k--) {
-        if (lane == 0) b[k] /= (V)M[k + (size_t)n * k];
-        __syncwarp();
-        const V bk = b[k];
-        for (int i = lane; i < k; i += 32) b[i] -= (V)M[i + (size_t)n * k] * bk;
-        __syncwarp();
+#pragma unroll
+    for (int kb = MR - 1; kb >= 0; kb--) {
+        if (32 * kb >= n) continue;
+        const int kend = min(32, n - 32 * kb);
+        for (int kk = kend - 1; kk >= 0; kk--) {
+            const int k = 32 * kb + kk;
+            if (lane == kk) br[kb] /= (V)M[k + (size_t)n * k];
+            const V bk = __shfl_sync(0xffffffffu, br[kb], kk);
+#pragma unroll
+            for (int m = 0; m <= kb; m++) {
+                const int i = lane + 32 * m;
+                if (i < k) br[m] -= (V)M[i + (size_t)n * k] * bk;
+            }
+        }
     }
+#pragma unroll
+    for (int m = 0; m < MR; m++)
+        if (lane + 32 * m < n) b[lane + 32 * m] = br[m];
+    __syncwarp();
 }
 
-// The same factorisation by a team of TW warps (TW = 1: warp_lu itself):
-// the pivot search over the team (warp argmax, then across the warps through
-// red_v / red_i, the first row of largest modulus as before), the row swap
-// and column scaling strided over the team, the trailing update over (row,
-// column) pairs.  Every element sees the operations of warp_lu in the same
-// order, so the factors are the same.
-template <typename T, int TW>
+// The same factorisation by a team of TW warps (TW = 1: warp_lu itself).
+// Warp w owns the columns j = w (mod TW): it swaps their rows, applies the
+// trailing update to them and, for its own column k, runs the pivot search
+// (the first row of largest modulus, as before) and forms the multipliers.
+// Two barriers per step: the pivot row is published, the multipliers are.
+// Every element sees the operations of warp_lu in the same order, so the
+// factors are the same.  Rows are spread over the lanes (at most MR per
+// lane, the multipliers held in registers: n <= 32 MR).
+constexpr int SE_MAX_ROWS = 8;   // c_dim <= 256
+template <typename T, int TW, int MR>
 __device__ bool team_lu(int n, T *M, int *piv, int tid, double *red_v, int *red_i) {
     if constexpr (TW == 1) {
         return warp_lu<T>(n, M, piv, tid);
     } else {
-        constexpr int TS = 32 * TW;
         const int lane = tid & 31, w = tid >> 5;
         bool ok = true;
         for (int k = 0; k < n; k++) {
-            T best = (T)-1;
-            int bi = n;
-            for (int i = k + tid; i < n; i += TS) {
-                T v = fabs(M[i + (size_t)n * k]);
-                if (v > best) { best = v; bi = i; }
+            const bool own_k = (k % TW) == w;
+            if (own_k) {
+                T best = (T)-1;
+                int bi = n;
+                for (int i = k + lane; i < n; i += 32) {
+                    T v = fabs(M[i + (size_t)n * k]);
+                    if (v > best) { best = v; bi = i; }
+                }
+                for (int o = 16; o >= 1; o >>= 1) {
+                    T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (bi >= n) bi = k;  // NaN column: keep the diagonal
+                if (lane == 0) {
+                    red_v[0] = (double)best;
+                    red_i[0] = bi;
+                    piv[k] = bi;
+                }
             }
-            for (int o = 16; o >= 1; o >>= 1) {
-                T ob = __shfl_xor_sync(0xffffffffu, best, o);
-                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (lane == 0) { red_v[w] = (double)best; red_i[w] = bi; }
-            __syncthreads();
-            best = (T)red_v[0];
-            bi = red_i[0];
-            for (int q = 1; q < TW; q++) {
-                const T ob = (T)red_v[q];
-                const int oi = red_i[q];
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (bi >= n) bi = k;
-            if (tid == 0) piv[k] = bi;
-            if (!(best > (T)0)) { ok = false; }
+            __syncthreads();   // the pivot row is published (and the last step's updates are done)
+            const T best = (T)red_v[0];
+            const int bi = red_i[0];
+            if (!(best > (T)0)) ok = false;
             if (bi != k)
-                for (int j = tid; j < n; j += TS) {
+                for (int j = w + TW * lane; j < n; j += 32 * TW) {
                     T t = M[k + (size_t)n * j];
                     M[k + (size_t)n * j] = M[bi + (size_t)n * j];
                     M[bi + (size_t)n * j] = t;
                 }
-            __syncthreads();   // also orders this step's reads of red_v / red_i before the next step's writes
-            const T d = M[k + (size_t)n * k];
-            const T r = (d != (T)0) ? (T)1 / d : (T)0;
-            for (int i = k + 1 + tid; i < n; i += TS) M[i + (size_t)n * k] *= r;
-            __syncthreads();
-            const int m = n - k - 1;
-            for (int idx = tid; idx < m * m; idx += TS) {
-                const int i = k + 1 + idx % m, j = k + 1 + idx / m;
-                const T lik = M[i + (size_t)n * k];
-                if (lik != (T)0) M[i + (size_t)n * j] -= lik * M[k + (size_t)n * j];
+            if (own_k) {
+                __syncwarp();
+                const T d = M[k + (size_t)n * k];
+                const T r = (d != (T)0) ? (T)1 / d : (T)0;
+                for (int i = k + 1 + lane; i < n; i += 32) M[i + (size_t)n * k] *= r;
             }
-            __syncthreads();
+            __syncthreads();   // the multipliers are published
+            T l[MR];
+#pragma unroll
+            for (int m = 0; m < MR; m++) {
+                const int i = k + 1 + lane + 32 * m;
+                l[m] = (i < n) ? M[i + (size_t)n * k] : (T)0;
+            }
+            int j = k + 1 + ((w - (k + 1)) % TW + TW) % TW;   // this warp's first column after k
+            for (; j < n; j += TW) {
+                const T mkj = M[k + (size_t)n * j];
+#pragma unroll
+                for (int m = 0; m < MR; m++) {
+                    const int i = k + 1 + lane + 32 * m;
+                    if (i < n && l[m] != (T)0) M[i + (size_t)n * j] -= l[m] * mkj;
+                }
+            }
         }
+        __syncthreads();
         return ok;
     }
 }
@@ -217,7 +258,9 @@ __host__ __device__ inline size_t se_warp_bytes(int n, int n_feat) {
 // (SEBatch); each warp copies its current model's argument block into shared
 // memory, and the dynamic shared memory per warp fits the largest model.
 // Otherwise the nodes of the one model a0.
-template <int TW, bool BATCH>
+// MR: rows per lane of the triangular solves and the team factorisation
+// (c_dim <= 32 MR).
+template <int TW, bool BATCH, int MR>
 __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW) k_solve_se(SEArgs a0, SEBatch bw) {
     static_assert(TW == 1 || !BATCH, "teams of several warps run the single-model kernel");
     constexpr int TS = 32 * TW;   // threads per team
@@ -339,10 +382,22 @@ __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW
         for (int i = tid; i < n * n; i += TS) A64[i] = 0.0;
         tsync();
         // ---- assembly (setup_stateq) ----
-        for (int e = tid; e < a.nent; e += TS) {
-            double v = 0.0;
-            for (int q = a.ent_off[e]; q < a.ent_off[e + 1]; q++) v += a.term_c[q] * feat[a.term_f[q]];
-            A64[a.ent_pos[e]] = v;
+        // entries with terms, four records per thread in flight; each entry's
+        // terms summed in program order
+        for (int e0 = tid; e0 < a.n_asm; e0 += 4 * TS) {
+            int4 rec[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int e = e0 + u * TS;
+                rec[u] = (e < a.n_asm) ? a.asm_rec[e] : make_int4(-1, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (rec[u].x < 0) continue;
+                double v = 0.0;
+                for (int q = rec[u].y; q < rec[u].z; q++) v = fma(a.term_c[q], feat[a.term_f[q]], v);
+                A64[rec[u].x] = v;
+            }
         }
         tsync();
         // ---- normalisation row (em_coefs.f90:158-164) ----
@@ -355,16 +410,13 @@ __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW
         for (int i = tid; i < n; i += TS) {
             double m = 0.0;
             for (int j = 0; j < n; j++) m = fmax(m, fabs(A64[i + (size_t)n * j]));
-            scl[i] = (m > 0.0) ? (float)(1.0 / m) : 1.f;
-        }
-        tsync();
-        for (int idx = tid; idx < n * n; idx += TS) {
-            const int i = idx % n;
-            LU[idx] = (float)(A64[idx] * (double)scl[i]);
+            const float sc = (m > 0.0) ? (float)(1.0 / m) : 1.f;
+            scl[i] = sc;
+            for (int j = 0; j < n; j++) LU[i + (size_t)n * j] = (float)(A64[i + (size_t)n * j] * (double)sc);
         }
         tsync();
         int st = 0;
-        bool ok = team_lu<float, TW>(n, LU, piv, tid, red_v, red_i);
+        bool ok = team_lu<float, TW, MR>(n, LU, piv, tid, red_v, red_i);
         bool conv = false;
         if (ok) {
             for (int i = tid; i < n; i += TS) x[i] = 0.0;
@@ -378,7 +430,7 @@ __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW
                     d32[i] = (float)(s * (double)scl[i]);
                 }
                 tsync();
-                if (TW == 1 || wib == 0) warp_lu_solve<float, float>(n, LU, piv, d32, lane);
+                if (TW == 1 || wib == 0) warp_lu_solve<float, float, MR>(n, LU, piv, d32, lane);
                 tsync();
                 double dm = 0.0;
                 for (int i = tid; i < n; i += TS) {
@@ -403,13 +455,13 @@ __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW
             // is not available; re-assemble into A64 in place)
             double *M = A64;
             st |= ok ? PORTAL_NODE_REFINE : 0;
-            bool ok64 = team_lu<double, TW>(n, M, piv, tid, red_v, red_i);
+            bool ok64 = team_lu<double, TW, MR>(n, M, piv, tid, red_v, red_i);
             if (!ok64) {
                 st |= PORTAL_NODE_SINGULAR;
             } else {
                 for (int i = tid; i < n; i += TS) x[i] = (i == 0) ? 1.0 : 0.0;
                 tsync();
-                if (TW == 1 || wib == 0) warp_lu_solve<double, double>(n, M, piv, x, lane);
+                if (TW == 1 || wib == 0) warp_lu_solve<double, double, MR>(n, M, piv, x, lane);
                 tsync();
                 st |= PORTAL_NODE_REFINE;
             }
@@ -737,6 +789,14 @@ int prepare_se(portal_ctx *c, int kmax) {
     size_t o_rad = putI(P.tr_rad), o_col = putI(P.tr_col), o_eoff = putI(P.ent_off),
            o_epos = putI(P.ent_pos), o_tf = putI(P.term_f), o_nc = putI(P.count_array),
            o_pack = putI(P.pack), o_roff = putI(P.row_off), o_rent = putI(P.row_ent);
+    // the assembly's records (pos, first term, end, 0) of the entries that have
+    // terms, 16-byte aligned for one load each (the matrix is zeroed first)
+    std::vector<int> asm_rec;
+    for (size_t e = 0; e < P.ent_pos.size(); e++)
+        if (P.ent_off[e + 1] > P.ent_off[e])
+            asm_rec.insert(asm_rec.end(), {P.ent_pos[e], P.ent_off[e], P.ent_off[e + 1], 0});
+    while (I.size() % 4) I.push_back(0);
+    const size_t o_asm = putI(asm_rec);
     size_t o_nu = putD(P.tr_nu), o_A = putD(P.tr_A), o_B = putD(P.tr_B21), o_tc = putD(P.term_c),
            o_nv = putD(norm_val), o_ct = putD(c->col_temps), o_C = putD(c->Cji), o_dep = putD(P.dep_tab);
     if (c->se_ints.reserve(I.size()) || c->se_dbls.reserve(D.size()))
@@ -754,7 +814,8 @@ int prepare_se(portal_ctx *c, int kmax) {
     c->se_offs[4] = o_tf; c->se_offs[5] = o_nc; c->se_offs[6] = o_pack;
     c->se_offs[7] = o_nu; c->se_offs[8] = o_A; c->se_offs[9] = o_B; c->se_offs[10] = o_tc;
     c->se_offs[11] = o_nv; c->se_offs[12] = o_ct; c->se_offs[13] = o_C;
-    c->se_offs[14] = o_roff; c->se_offs[15] = o_rent; c->se_offs[16] = o_dep;
+    c->se_offs[14] = o_roff; c->se_offs[15] = o_rent; c->se_offs[16] = o_dep; c->se_offs[17] = o_asm;
+    c->se_nasm = (int)(asm_rec.size() / 4);
     c->n_dep = P.n_dep;
     c->n_feat = NF * P.n_trans + (c->depol == 2 ? 2 : 1) * P.n_dep;
     return PORTAL_OK;
@@ -770,7 +831,8 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     if (rc) return rc;
     const int n = c->c_dim;
     const size_t wb = se_warp_bytes(n, c->n_feat);
-    if (wb > 200 * 1024) return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
+    if (wb > 200 * 1024 || n > 32 * SE_MAX_ROWS)
+        return set_err(c, PORTAL_ERR_ARG, "SE system too large for shared memory");
     if (c->pops.reserve((size_t)c->N * 2 * c->nlev) || c->jj20.reserve((size_t)c->N * c->r_num))
         return set_err(c, PORTAL_ERR_NOMEM, "SE outputs");
     SEArgs a;
@@ -789,6 +851,8 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     a.term_c = D + c->se_offs[10]; a.norm_val = D + c->se_offs[11]; a.col_temps = D + c->se_offs[12];
     a.Cji = D + c->se_offs[13];
     a.row_off = I + c->se_offs[14]; a.row_ent = I + c->se_offs[15];
+    a.asm_rec = reinterpret_cast<const int4 *>(I + c->se_offs[17]);
+    a.n_asm = c->se_nasm;
     a.dep_tab = c->n_dep ? D + c->se_offs[16] : nullptr;
     a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
     a.rates = nullptr;
@@ -809,14 +873,19 @@ int se_pass(portal_ctx *c, cudaStream_t s) {
 
 size_t se_matrix_doubles(const portal_ctx *c) { return (size_t)c->c_dim * c->c_dim; }
 
-int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) {
+// The batched kernel's instance for the batch's largest system (a64_stride =
+// its c_dim^2): 3 rows per lane up to 96 unknowns, SE_MAX_ROWS above.
+static const void *se_batch_kernel(size_t a64_stride) {
+    return a64_stride <= 96 * 96 ? (const void *)k_solve_se<1, true, 3> : (const void *)k_solve_se<1, true, SE_MAX_ROWS>;
+}
+
+int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, size_t a64_stride, int *blocks) {
     const size_t smem = warp_bytes * warps_per_block;
+    const void *k = se_batch_kernel(a64_stride);
     *blocks = 0;
-    if (cudaFuncSetAttribute(k_solve_se<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return PORTAL_ERR_CUDA;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solve_se<1, true>, 32 * warps_per_block, smem) ==
-                   cudaSuccess
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 32 * warps_per_block, smem) == cudaSuccess
                ? PORTAL_OK
                : PORTAL_ERR_CUDA;
 }
@@ -825,27 +894,33 @@ int se_batch_blocks_per_sm(int warps_per_block, size_t warp_bytes, int *blocks) 
 // se_batch_blocks_per_sm for at least this many warps)
 int se_batch_launch(cudaStream_t s, int grid, int warps_per_block, const SEBatch &bw) {
     const size_t smem = bw.warp_bytes * warps_per_block;
-    k_solve_se<1, true><<<grid, 32 * warps_per_block, smem, s>>>(SEArgs{}, bw);
+    SEArgs a0{};
+    SEBatch b = bw;
+    void *args[] = {&a0, &b};
+    if (cudaLaunchKernel(se_batch_kernel(bw.a64_stride), dim3(grid), dim3(32 * warps_per_block), args, smem, s) !=
+        cudaSuccess)
+        return PORTAL_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? PORTAL_OK : PORTAL_ERR_CUDA;
 }
 
 // Warps per node: one up to SE_TEAM_MIN_N unknowns, a team of four above
-// (PORTAL_SE_TEAM=1|2|4 overrides).
+// (PORTAL_SE_TEAM=1|4 overrides).  Teams of two measured slower than either
+// on 34 x 34 and 74 x 74 systems.
 constexpr int SE_TEAM_MIN_N = 48;
 inline int se_team_warps(int n) {
     const char *e = getenv("PORTAL_SE_TEAM");
     if (e) {
         const int v = atoi(e);
-        if (v == 1 || v == 2 || v == 4) return v;
+        if (v == 1 || v == 4) return v;
     }
     return n >= SE_TEAM_MIN_N ? 4 : 1;
 }
 
 // TW = 1: blocks of up to 8 independent warps; TW > 1: one team per block.
 // One FP64 matrix slot per team of the grid.
-template <int TW>
+template <int TW, int MR>
 int launch_se(portal_ctx *c, SEArgs &a, size_t wb) {
-    auto kern = k_solve_se<TW, false>;
+    auto kern = k_solve_se<TW, false, MR>;
     const int teams = (TW == 1) ? (int)std::min<size_t>(8, (200 * 1024) / wb) : 1;
     const size_t smem = wb * teams;
     PCHECK(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -875,11 +950,11 @@ int run_solve_se(portal_ctx *c, int kmax, int *n_singular, bool rates) {
     }
     if ((rc = se_pass(c, c->stream))) return rc;
     a.a64_stride = (size_t)c->c_dim * c->c_dim;
-    switch (se_team_warps(c->c_dim)) {
-    case 2: rc = launch_se<2>(c, a, wb); break;
-    case 4: rc = launch_se<4>(c, a, wb); break;
-    default: rc = launch_se<1>(c, a, wb); break;
-    }
+    const bool few_rows = c->c_dim <= 96;
+    if (se_team_warps(c->c_dim) == 4)
+        rc = few_rows ? launch_se<4, 3>(c, a, wb) : launch_se<4, SE_MAX_ROWS>(c, a, wb);
+    else
+        rc = few_rows ? launch_se<1, 3>(c, a, wb) : launch_se<1, SE_MAX_ROWS>(c, a, wb);
     if (rc) return rc;
     int nf = 0;
     PCHECK(c, cudaMemcpyAsync(&nf, c->counters.p + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
