@@ -290,10 +290,6 @@ __global__ void __launch_bounds__(64, 1) k_rf_static(RsArgs a) {
     }
 }
 
-// per-device address of g_rf_scratch, looked up once per device
-std::mutex g_rs_mutex;
-unsigned char *g_rs_ptr[64] = {};
-
 // The host side of each call's line constants, direction and channel
 // tables.  Kept in static storage (not on the call's stack) so that the
 // memory a copy reads from stays valid after the call returns; filled and
@@ -322,16 +318,14 @@ extern "C" int portal_radiation_field_static(
         n_depth > RS_MAX_DEPTH)
         return PORTAL_ERR_ARG;  // beyond the static scratch (see portal_radiation_field_static_limits)
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PORTAL_ERR_NODEVICE;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return PORTAL_ERR_NODEVICE;
+    // the current device's address of g_rf_scratch, looked up on every call
+    // (a cached address would go stale when the module is reloaded)
     unsigned char *scratch = nullptr;
     {
-        std::lock_guard<std::mutex> lk(g_rs_mutex);
-        if (!g_rs_ptr[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_rf_scratch) != cudaSuccess || !p) return PORTAL_ERR_CUDA;
-            g_rs_ptr[dev] = (unsigned char *)p;
-        }
-        scratch = g_rs_ptr[dev];
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_rf_scratch) != cudaSuccess || !p) return PORTAL_ERR_CUDA;
+        scratch = (unsigned char *)p;
     }
     cudaStream_t st = (cudaStream_t)cuda_stream;
     for (int k = 0; k < r_num; k++) {

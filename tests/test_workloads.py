@@ -42,5 +42,5 @@ def test_bench_reads_the_profile_figures():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.profile_constant("dram_bytes_per_segment") == pytest.approx(0.40)
-    assert bench.profile_constant("warp_instructions_per_segment") == pytest.approx(407.0)
+    assert bench.profile_constant("warp_instructions_per_segment") == pytest.approx(373.0)
     assert bench.profile_constant("no_such_figure") is None
