@@ -75,8 +75,9 @@ struct SEArgs {
     double *rates;                      // (N, 3, 2 nlev) column-major or null
     int *status;
     int *nfail;
-    double *a64;                        // FP64 matrices, one slot of a64_stride doubles per warp
+    double *a64;                        // FP64 matrices, one slot of a64_stride doubles per team
     size_t a64_stride;
+    int fp64_only;                      // factorise every system in FP64 (no FP32 LU)
 };
 
 // A batched launch: work items (model, node) over many models, the models'

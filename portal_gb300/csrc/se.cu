@@ -406,18 +406,20 @@ __global__ void __launch_bounds__(TW == 1 ? 256 : 32 * TW, TW == 1 ? 3 : 24 / TW
         if (tid == 0)
             for (int i = 0; i < a.nlev; i++) A64[(size_t)n * a.norm_col[i]] = a.norm_val[i];
         tsync();
-        // ---- FP32 LU of the row-scaled matrix ----
-        for (int i = tid; i < n; i += TS) {
-            double m = 0.0;
-            for (int j = 0; j < n; j++) m = fmax(m, fabs(A64[i + (size_t)n * j]));
-            const float sc = (m > 0.0) ? (float)(1.0 / m) : 1.f;
-            scl[i] = sc;
-            for (int j = 0; j < n; j++) LU[i + (size_t)n * j] = (float)(A64[i + (size_t)n * j] * (double)sc);
-        }
-        tsync();
+        // ---- FP32 LU of the row-scaled matrix (skipped in FP64 mode) ----
         int st = 0;
-        bool ok = team_lu<float, TW, MR>(n, LU, piv, tid, red_v, red_i);
-        bool conv = false;
+        bool ok = false, conv = false;
+        if (!a.fp64_only) {
+            for (int i = tid; i < n; i += TS) {
+                double m = 0.0;
+                for (int j = 0; j < n; j++) m = fmax(m, fabs(A64[i + (size_t)n * j]));
+                const float sc = (m > 0.0) ? (float)(1.0 / m) : 1.f;
+                scl[i] = sc;
+                for (int j = 0; j < n; j++) LU[i + (size_t)n * j] = (float)(A64[i + (size_t)n * j] * (double)sc);
+            }
+            tsync();
+            ok = team_lu<float, TW, MR>(n, LU, piv, tid, red_v, red_i);
+        }
         if (ok) {
             for (int i = tid; i < n; i += TS) x[i] = 0.0;
             tsync();
@@ -857,6 +859,12 @@ int se_prepare(portal_ctx *c, int kmax, SEArgs *out, size_t *warp_bytes) {
     a.pops = c->pops.p; a.jj20 = c->jj20.p; a.status = c->status.p;
     a.rates = nullptr;
     a.nfail = (int *)(c->counters.p + 2);
+    // PORTAL_SE_FP64=1: every system factorised in FP64 (the refinement's
+    // fallback path), flagged PORTAL_NODE_REFINE
+    {
+        const char *e = getenv("PORTAL_SE_FP64");
+        a.fp64_only = (e && e[0] == '1') ? 1 : 0;
+    }
     *out = a;
     if (warp_bytes) *warp_bytes = wb;
     return PORTAL_OK;

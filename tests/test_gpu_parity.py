@@ -197,17 +197,11 @@ def test_depolarising_collisions_against_oracle(ctx, mode):
     np.testing.assert_allclose(back[:128], plain[:128], rtol=1e-10, atol=1e-14 * np.abs(plain).max())
 
 
-@pytest.mark.parametrize("team", [2, 4])
-def test_se_team_of_warps_matches_one_warp_and_oracle(ctx, monkeypatch, team):
-    """74 x 74 systems (20-level rotor, kmax 6) solved by a team of warps per
-    node (the default above 48 unknowns) and by one warp: the factorisation
-    sees the same operations per element, so populations, alignment, rates
-    and status are identical; against the oracle (get_rhovec,
-    em_coefs.f90:115-201) on 64 nodes to 1e-10 from the same J (the local
-    Planck field with a small anisotropy)."""
+def _se74():
+    """A 2,048-point sphere with a 20-level rotor at kmax 6 (74 x 74 SE
+    systems), LTE populations and the local Planck field with a small
+    anisotropy."""
     import dataclasses
-    import oracle
-    import portal_gb300 as pg
     from portal_gb300 import synth
     cloud, mol, rc = _small(2048, nlev=20, t_law="loglinear")
     frac = synth.lte_fractions(mol, np.maximum(cloud.t_kin, 1.0))
@@ -215,6 +209,26 @@ def test_se_team_of_warps_matches_one_warp_and_oracle(ctx, monkeypatch, team):
     nu = np.asarray(mol.nu)
     J0 = 1.4744995e-50 * nu ** 3 / np.expm1(4.79924e-11 * nu / np.maximum(cloud.t_kin, 1.0)[:, None])
     J2 = 1e-3 * J0 * np.cos(np.arange(cloud.node_num))[:, None]
+    return cloud, mol, rc, J0, J2
+
+
+def _against_oracle_se(pops, cloud, mol, rc, J0, J2, nodes=64, tol=1e-10):
+    import oracle
+    opp = oracle.OracleProblem(cloud, mol).solve_se(rc.kmax, J0, J2, 1, nodes)[0]
+    scale = np.abs(opp[:nodes, 0::2]).max(axis=1, keepdims=True)
+    assert (np.abs(pops[:nodes, 0::2] - opp[:nodes, 0::2]) / scale).max() < tol
+    assert (np.abs(pops[:nodes, 1::2] - opp[:nodes, 1::2]) / scale).max() < tol
+
+
+@pytest.mark.parametrize("team", [4])
+def test_se_team_of_warps_matches_one_warp_and_oracle(ctx, monkeypatch, team):
+    """74 x 74 systems (20-level rotor, kmax 6) solved by a team of warps per
+    node (the default above 48 unknowns) and by one warp: the factorisation
+    sees the same operations per element, so populations, alignment, rates
+    and status are identical; against the oracle (get_rhovec,
+    em_coefs.f90:115-201) on 64 nodes to 1e-10 from the same J."""
+    import portal_gb300 as pg
+    cloud, mol, rc, J0, J2 = _se74()
     ctx.set_molecule(mol)
     ctx.set_cloud(cloud)
     monkeypatch.setenv("PORTAL_SE_TEAM", "1")
@@ -223,10 +237,37 @@ def test_se_team_of_warps_matches_one_warp_and_oracle(ctx, monkeypatch, team):
     pt, st, rt = ctx.solve_se(rc.kmax, J0, J2, rates=True)
     assert np.array_equal(p1, pt) and np.array_equal(s1, st) and np.array_equal(r1, rt)
     assert not (st & pg.NODE_SINGULAR).any()
-    opp = oracle.OracleProblem(cloud, mol).solve_se(rc.kmax, J0, J2, 1, 64)[0]
-    scale = np.abs(opp[:64, 0::2]).max(axis=1, keepdims=True)
-    assert (np.abs(pt[:64, 0::2] - opp[:64, 0::2]) / scale).max() < 1e-10
-    assert (np.abs(pt[:64, 1::2] - opp[:64, 1::2]) / scale).max() < 1e-10
+    _against_oracle_se(pt, cloud, mol, rc, J0, J2)
+
+
+def test_se_fp64_mode_one_warp_and_team(ctx, monkeypatch):
+    """PORTAL_SE_FP64=1 factorises every system in FP64 on the device -- the
+    path the refinement falls back to when it stalls (the team's
+    factorisation and the register triangular solves in FP64), which the
+    well-conditioned workloads never reach otherwise.  Every live node is
+    flagged PORTAL_NODE_REFINE; one warp and a team of four give identical
+    results; both match the oracle to 1e-10 and the FP32-refined solve to
+    1e-10."""
+    import portal_gb300 as pg
+    cloud, mol, rc, J0, J2 = _se74()
+    ctx.set_molecule(mol)
+    ctx.set_cloud(cloud)
+    monkeypatch.setenv("PORTAL_SE_FP64", "0")
+    p32, s32 = ctx.solve_se(rc.kmax, J0, J2)
+    monkeypatch.setenv("PORTAL_SE_FP64", "1")
+    res = {}
+    for team in (1, 4):
+        monkeypatch.setenv("PORTAL_SE_TEAM", str(team))
+        res[team] = ctx.solve_se(rc.kmax, J0, J2)
+    (p1, s1), (p4, s4) = res[1], res[4]
+    assert np.array_equal(p1, p4) and np.array_equal(s1, s4)
+    live = cloud.ab_all[: cloud.bulk_node_num] > 0
+    assert ((s4[: cloud.bulk_node_num][live] & pg.NODE_REFINE) != 0).all()
+    assert not (s4 & pg.NODE_SINGULAR).any()
+    _against_oracle_se(p4, cloud, mol, rc, J0, J2)
+    scale = np.abs(p32[:, 0::2]).max(axis=1, keepdims=True) + 1e-300
+    assert (np.abs(p4[:, 0::2] - p32[:, 0::2]) / scale).max() < 1e-10
+    assert (np.abs(p4[:, 1::2] - p32[:, 1::2]) / scale).max() < 1e-10
 
 
 def test_n_depth_overflow_is_reported(ctx):
