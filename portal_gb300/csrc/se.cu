@@ -22,8 +22,9 @@
 // rate equations), still linear in the populations.  At the fixed point
 // (S unchanged) both forms are the same equations.  The host turns setup_stateq's loops into that program once per
 // (molecule, kmax): a CSR list over matrix entries of (feature, coefficient)
-// terms.  The kernel (one warp per node) evaluates the features, assembles
-// the matrix in shared memory (FP64), replaces row 1 by the normalisation
+// terms.  The kernel (one warp per node, or a team of four warps for
+// systems of 48 or more unknowns) evaluates the features, assembles the
+// matrix (FP64, in an L2-resident slot per team), replaces row 1 by the normalisation
 // sum sqrt(2J+1) rho^0_0 = 1, factorises a row-scaled FP32 copy with partial
 // pivoting and refines the solution of A rho = e_1 with FP64 residuals.
 // Should the refinement stall (FP32 LU too inaccurate for the matrix's
@@ -231,11 +232,11 @@ __device__ bool team_lu(int n, T *M, int *piv, int tid, double *red_v, int *red_
     }
 }
 
-// Dynamic shared memory per warp:
+// Dynamic shared memory per team (one warp, or the block's team of warps):
 //   feat [n_feat] double | x, r [n] double | LU32 [n*n] float | d32 [n] float
 //   | scale [n] float | piv [n] int
 // The FP64 matrix A64 [n*n] (assembly, residuals, the FP64 fallback) sits in
-// a per-warp slot of global memory instead (L2-resident: the grid's warps x
+// a per-team slot of global memory instead (L2-resident: the grid's teams x
 // n^2 doubles); kept out of shared memory it lets 3x more warps share an SM,
 // and the kernel is latency-bound.
 constexpr int NF = 7;  // features per transition
