@@ -166,7 +166,11 @@ constexpr double PI_D = 3.141592653589793;  // acos(-1.d0)
 // frame as inverse_rt rebuilds it (find_dir of acos(mu), ph) and stores the
 // weights (w, w c_in / sqrt 2) in *wts.  Out of line: the default path
 // keeps the kernel's own code.
-__device__ __noinline__ double4 star_ray(const double *sk, int n_star, int i, int nth, int nph, double gx,
+// a ray direction in the field frame: (cos th, sin th, cos ph, sin ph)
+struct RayDir {
+    double ct, st, cp, sp;
+};
+__device__ __noinline__ RayDir star_ray(const double *sk, int n_star, int i, int nth, int nph, double gx,
                                          double gy, double gz, const double *f, float2 *wts) {
     double x1 = 1.0, x2 = 0.0, w = 0.0;
     if (i < n_star) {
@@ -225,7 +229,7 @@ __device__ __noinline__ double4 star_ray(const double *sk, int n_star, int i, in
     const double phb = atan2(f[3] * dx + f[4] * dy + f[5] * dz, f[3] * cx + f[4] * cy + f[5] * cz);
     *wts = make_float2((float)w, (float)(w * ((3.0 * mub * mub - 1.0) / 2.0) / sqrt(2.0)));
     const double th = acos(mub);
-    return make_double4(cos(th), sin(th), cos(phb), sin(phb));
+    return RayDir{cos(th), sin(th), cos(phb), sin(phb)};
 }
 
 // trace_node's star geometry (main_sub.f90:56-66) and star_all's ray counts
@@ -386,9 +390,9 @@ __global__ void __launch_bounds__(256, (NLG <= 5 && NS <= 5) ? 2 : 1) k_radiatio
                     bool tab = true;
                     if constexpr (BATCH) {
                         if (a.star) {
-                            const double4 r = star_ray(B.sk, vsn[0], k0 + lane, a.nth, a.nph, a.gx, a.gy, a.gz, f,
-                                                       &B.wts[lane]);
-                            mu = r.x; sth = r.y; cph = r.z; sph = r.w;
+                            const RayDir r = star_ray(B.sk, vsn[0], k0 + lane, a.nth, a.nph, a.gx, a.gy, a.gz, f,
+                                                      &B.wts[lane]);
+                            mu = r.ct; sth = r.st; cph = r.cp; sph = r.sp;
                             tab = false;
                         }
                     }

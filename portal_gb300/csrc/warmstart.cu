@@ -65,12 +65,12 @@ __global__ void k_features(int N, int L, double tx, double nu0, double nu1, cons
         Mi[8] = (a * d - b * b) / det;
         Mi[3] = Mi[1]; Mi[6] = Mi[2]; Mi[7] = Mi[5];
     }
-    double G[9], gn = 0.0;
+    // |G|^2 of the velocity gradient G = R Mi (Frobenius)
+    double gn = 0.0;
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
             double s = 0.0;
             for (int k = 0; k < 3; k++) s += R[3 * i + k] * Mi[3 * k + j];
-            G[3 * i + j] = s;
             gn += s * s;
         }
     // the local J^2_0 axis: principal axis of the traceless second moment,
