@@ -44,3 +44,14 @@ def test_bench_reads_the_profile_figures():
     assert bench.profile_constant("dram_bytes_per_segment") == pytest.approx(0.40)
     assert bench.profile_constant("warp_instructions_per_segment") == pytest.approx(373.0)
     assert bench.profile_constant("no_such_figure") is None
+
+
+def test_se_lu_rates():
+    """The SE stages' FP32 factorisation rate: 2/3 n^3 flop per node, against
+    SMs x 128 lanes x 2 flop x clock."""
+    import bench
+    r = bench.lu_rates(262144, 34, 15.0, 152, 2070.0)
+    assert r["fp32_lu_flop_per_s"] == pytest.approx(262144 * (2.0 / 3.0) * 34 ** 3 / 0.015)
+    assert r["fp32_peak_flop_per_s"] == pytest.approx(152 * 128 * 2 * 2070e6)
+    assert r["fp32_lu_frac"] == pytest.approx(r["fp32_lu_flop_per_s"] / r["fp32_peak_flop_per_s"])
+    assert set(bench.lu_rates(10, 34, 1.0)) == {"fp32_lu_flop_per_s"}
